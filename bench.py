@@ -1,0 +1,357 @@
+"""Benchmark of the GB300 SCAMP engine on the AB-join configuration.
+
+Workload (the configuration the headline metric is quoted on): AB-join of a
+random walk A (2^20 points) with a random walk B (2^19 points) sharing 64
+planted sinusoid motifs, 0.1% NaN samples, window m = 256, 1NN_INDEX in both
+directions (keep_rows); seeded synthetic data of those shapes.
+
+A step is one complete join.  ``value`` is comparisons/s of the mixed form
+with the series already resident in HBM (C-ABI scamp_gb300_join_dev);
+``e2e`` is the same metric through scamp_gb300_join with pinned host
+buffers, host<->device copies included.  The FP64 form runs the same join
+for the error check (max |r| difference of the two forms) and its own
+throughput.  The L2 (129 MB, larger than the 12 MB input) is flushed before
+every timed step by writing a 512 MB buffer.
+
+``--impl reference`` times the CPU path instead: the oracle's C restatement
+of the reference's CPU join (the reference tree does not exist on the GPU
+host, so its own sources cannot be compiled there) with every host thread,
+on a bounded sample of the workload per step.
+
+Multi-GPU (torchrun): every rank runs an independent replica of the join
+(the engine is single-GPU); the timed region is barrier-bracketed and the
+max over ranks is reported.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "gpu-scrimp-large_gb300"))
+
+METRIC = "pairwise comparisons/s (1 GB300), mixed-precision vs FP64 at max|r err|≤1e-5"
+WORKLOAD = ("AB-join: A = random walk 2^20, B = random walk 2^19, 64 planted sin motifs "
+            "(len 256), 0.1% NaN samples, m=256, 1NN_INDEX both directions (keep_rows)")
+NA, NB, M = 1 << 20, 1 << 19, 256
+# CPU sample: the same distributions, A[:2^17] x B[:2^16], both directions.
+CPU_NA, CPU_NB = 1 << 17, 1 << 16
+OPS_PER_CELL = 4  # FMA-pipe operations per comparison: 2 FMA + 2 MUL
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_workload(na=None, nb=None):
+    from scamp_gb300 import workloads
+
+    return workloads.cfg2_abjoin(na=na or NA, nb=nb or NB, m=M)
+
+
+def run_reference(args, world, rank):
+    """CPU path of the reference (oracle restatement), bounded sample."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+
+    oracle.load()
+    a, b, m = make_workload(1 << 20, 1 << 19)
+    a, b = a[:CPU_NA], b[:CPU_NB]
+    cells = (len(a) - m + 1) * (len(b) - m + 1)
+    threads = oracle.max_threads()
+    for _ in range(args.warmup):
+        oracle.join(a, b, m, keep_rows=True, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.join(a, b, m, keep_rows=True, threads=threads)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = cells / dt
+    sample = "A[:2^17] x B[:2^16] of the workload, both directions, DOUBLE"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "comparisons/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "comparisons/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "comparisons/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_leg():
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+
+    oracle.load()
+    a, b, m = make_workload(1 << 20, 1 << 19)
+    a, b = a[:CPU_NA], b[:CPU_NB]
+    cells = (len(a) - m + 1) * (len(b) - m + 1)
+    threads = oracle.max_threads()
+    t0 = time.perf_counter()
+    oracle.join(a, b, m, keep_rows=True, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": cells / dt, "unit": "comparisons/s", "cores": threads, "kind": "port",
+            "sample": "A[:2^17] x B[:2^16] of the workload, both directions, DOUBLE, "
+                      "%.1f s" % dt}
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--fp64-steps", type=int, default=1)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--na-log2", type=int, default=20,
+                   help="log2 length of A (B is half); smaller only for profiling captures")
+    p.add_argument("--profile-only", action="store_true",
+                   help="run only the timed mixed joins (for ncu captures); prints no JSON")
+    args = p.parse_args()
+    global NA, NB
+    NA, NB = 1 << args.na_log2, 1 << (args.na_log2 - 1)
+    world, rank, local = dist_env()
+
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+
+    import scamp_gb300
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    a_np, b_np, m = make_workload()
+    nsa, nsb = NA - m + 1, NB - m + 1
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    a_d = torch.from_numpy(a_np).to(dev)
+    b_d = torch.from_numpy(b_np).to(dev)
+    no_match = int(scamp_gb300.NO_MATCH)
+    prof_a = torch.empty(nsa, dtype=torch.int64, device=dev)
+    prof_b = torch.empty(nsb, dtype=torch.int64, device=dev)
+    corr_a = torch.empty(nsa, dtype=torch.float64, device=dev)
+    corr_b = torch.empty(nsb, dtype=torch.float64, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    nm = no_match - (1 << 64) if no_match >= (1 << 63) else no_match
+
+    def one(precision):
+        with torch.cuda.stream(stream):
+            prof_a.fill_(nm)
+            prof_b.fill_(nm)
+            flush.fill_(1)  # L2 flush before the timed join
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        r = scamp_gb300.join_device(
+            a_d.data_ptr(), NA, m, b_d.data_ptr(), NB, "1NN_INDEX", precision,
+            computing_rows=True, keep_rows=True, profile_a_ptr=prof_a.data_ptr(),
+            profile_b_ptr=prof_b.data_ptr(), corr_a_ptr=corr_a.data_ptr(),
+            corr_b_ptr=corr_b.data_ptr(), stream=stream.cuda_stream, device=local)
+        ev1.record(stream)
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1), r
+
+    # ---- mixed form (headline) ----
+    for _ in range(max(args.warmup, 3)):
+        one("mixed")
+    barrier()
+    torch.cuda.synchronize()
+    times, kernel_ms, launches = [], [], 0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            ms, r = one("mixed")
+            times.append(ms)
+            kernel_ms.append(r["join_kernel_ms"])
+            launches += r["gpu_launches"]
+    torch.cuda.synchronize()
+    barrier()
+    clocks = clk.summary()
+    if args.profile_only:
+        return
+    cells = r["comparisons"]
+    ms_step = sum(times) / len(times)
+    if dist is not None:
+        t = torch.tensor([ms_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = t.item()
+    value = cells * world / (ms_step * 1e-3)
+    mixed_corr = (corr_a.cpu().numpy().copy(), corr_b.cpu().numpy().copy())
+    mixed_idx = (prof_a.cpu().numpy().view(np.uint64) >> np.uint64(32),
+                 prof_b.cpu().numpy().view(np.uint64) >> np.uint64(32))
+
+    # ---- FP64 form: throughput and the accuracy reference ----
+    one("double")
+    fp64_ms, fp64_kernel = [], []
+    for _ in range(max(1, args.fp64_steps)):
+        ms, r64 = one("double")
+        fp64_ms.append(ms)
+        fp64_kernel.append(r64["join_kernel_ms"])
+    f_corr = (corr_a.cpu().numpy(), corr_b.cpu().numpy())
+    f_idx = (prof_a.cpu().numpy().view(np.uint64) >> np.uint64(32),
+             prof_b.cpu().numpy().view(np.uint64) >> np.uint64(32))
+    max_err, idx_agree, n_valid = 0.0, 0, 0
+    for k in range(2):
+        ok = f_corr[k] >= -1
+        if ok.any():
+            max_err = max(max_err, float(np.max(np.abs(mixed_corr[k][ok] - f_corr[k][ok]))))
+        idx_agree += int(np.sum(mixed_idx[k][ok] == f_idx[k][ok]))
+        n_valid += int(ok.sum())
+
+    # ---- e2e through the host-buffer C ABI ----
+    a_pin = torch.from_numpy(a_np).pin_memory().numpy()
+    b_pin = torch.from_numpy(b_np).pin_memory().numpy()
+    pa_pin = torch.empty(nsa, dtype=torch.int64).pin_memory().numpy().view(np.uint64)
+    pb_pin = torch.empty(nsb, dtype=torch.int64).pin_memory().numpy().view(np.uint64)
+    pa_pin[:] = scamp_gb300.NO_MATCH
+    pb_pin[:] = scamp_gb300.NO_MATCH
+    e2e_t = []
+    for it in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = scamp_gb300.join(a_pin, b_pin, m, "1NN_INDEX", "mixed", keep_rows=True,
+                             profile_a=pa_pin, profile_b=pb_pin, device=local, inplace=True)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            e2e_t.append(dt)
+            launches_e2e = r["gpu_launches"]
+    e2e_s = sum(e2e_t) / len(e2e_t)
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = t.item()
+    h2d = (NA + NB) * 8 + (nsa + nsb) * 8
+    d2h = (nsa + nsb) * 8
+
+    # ---- roofline: the join kernel against the measured FMA-pipe peaks ----
+    peak32 = scamp_gb300.pipe_peak("fp32", local)
+    peak64 = scamp_gb300.pipe_peak("fp64", local)
+    k_ms = sum(kernel_ms) / len(kernel_ms)
+    achieved = cells * OPS_PER_CELL / (k_ms * 1e-3)
+    k64 = sum(fp64_kernel) / len(fp64_kernel)
+    achieved64 = cells * OPS_PER_CELL / (k64 * 1e-3)
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "comparisons/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded random walks with planted motifs and NaNs)",
+        "config": {"workload": WORKLOAD, "form": "mixed (FP32 recurrence, FP64-centred anchors)",
+                   "comparisons_per_step": cells, "l2": "flushed (512 MB write) before each step",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "max_abs_r_err_vs_fp64": max_err,
+        "index_agreement_vs_fp64": idx_agree / max(n_valid, 1),
+        "fp64": {"value": cells / (sum(fp64_ms) / len(fp64_ms) * 1e-3), "unit": "comparisons/s",
+                 "ms_per_step": sum(fp64_ms) / len(fp64_ms),
+                 "roofline": {"bound": "fp64_fma_pipe", "achieved": achieved64 / 1e12,
+                              "peak": peak64 / 1e12, "unit": "Tops/s",
+                              "frac": achieved64 / peak64, "peak_source": "measured DFMA probe"}},
+        "speedup_mixed_vs_fp64": (sum(fp64_ms) / len(fp64_ms)) / ms_step,
+        "roofline": {"bound": "fp32_fma_pipe", "achieved": achieved / 1e12, "peak": peak32 / 1e12,
+                     "unit": "Tops/s", "frac": achieved / peak32, "traffic": None,
+                     "kernel": "join_mixed_kernel", "kernel_ms": k_ms,
+                     "ops_per_comparison": OPS_PER_CELL,
+                     "peak_source": "measured packed-FP32 FMA probe (scamp_gb300_pipe_peak)"},
+        "e2e": {"value": cells * world / e2e_s, "unit": "comparisons/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_leg()
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,617 @@
+// engine.cu -- host orchestration of a join and the C ABI (scamp_gb300.h).
+//
+// Replaces the reference's SCAMP_Operation (src/SCAMP.cpp:25-259) and Tile
+// (src/tile.cpp) host machinery.  Where the reference moves every tile's
+// series, statistics and best-so-far profile over PCIe and merges on the host
+// under a mutex (src/tile.cpp:312-544, src/common.cpp:364-415), this engine
+// keeps the whole problem resident in HBM:
+//   H2D(series, initial profile) -> stats kernel -> join kernel (persistent,
+//   device work queue over every band x segment unit) -> key->profile kernel
+//   -> D2H(profile)
+// with no host synchronisation in between.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+#include "scamp_gb300.h"
+
+namespace scamp_gb300 {
+
+int fp64_band_width();
+int fp64_slab_rows();
+int fp64_threads();
+int mixed_band_width();
+int mixed_slab_rows();
+int mixed_threads();
+size_t mixed_smem_bytes();
+int measure_pipe_peak(int device, int kind, double* ops_per_s);
+
+namespace {
+
+constexpr int kDefaultAnchorInterval = 1024;
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+void set_err(char* buf, size_t len, const std::string& msg) {
+  if (buf && len) {
+    std::snprintf(buf, len, "%s", msg.c_str());
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side planning (no GPU needed).
+// ---------------------------------------------------------------------------
+struct ProblemPlan {
+  int rows_series;  // 0 = A, 1 = B
+  int cols_series;
+  int64_t n_r, n_c;
+  int64_t d_lo, d_hi, x_lo, x_hi;
+  int col_target;   // 0 = profile A, 1 = profile B, -1 none
+  int row_target;
+};
+
+struct Plan {
+  bool self_join;
+  int64_t m, ns_a, ns_b;
+  std::vector<ProblemPlan> probs;
+  uint64_t cells;
+};
+
+// Mirrors SCAMPArgs::validate (src/common.cpp:417-436) plus the profile and
+// precision types this engine serves.
+int validate(const scamp_c_args* a, std::string* msg) {
+  if (!a) { *msg = "Error: Invalid arguments provided to SCAMP"; return SCAMP_ERR_INVALID_ARGS; }
+  if (a->window < 3) { *msg = "Error: Subsequence length must be at least 3"; return SCAMP_ERR_INVALID_ARGS; }
+  if (a->max_tile_size < 1024) { *msg = "Error: max tile size must be at least 1024"; return SCAMP_ERR_INVALID_ARGS; }
+  if (a->max_tile_size / 2 < a->window) {
+    *msg = "Error: Tile length and width must be at least 2x larger than the window size";
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  if (!a->timeseries_a || a->len_a < a->window || (a->has_b && (!a->timeseries_b || a->len_b < a->window))) {
+    *msg = "Error: Input time series must be at least 'subesequence window size' in length";
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  if (a->profile_type != SCAMP_PROFILE_1NN_INDEX && a->profile_type != SCAMP_PROFILE_SUM_THRESH) {
+    *msg = "Error: profile type not supported by this engine (1NN_INDEX, SUM_THRESH)";
+    return SCAMP_ERR_UNIMPLEMENTED;
+  }
+  if (a->precision_type < SCAMP_PRECISION_SINGLE || a->precision_type > SCAMP_PRECISION_ULTRA) {
+    *msg = "Error: invalid precision type";
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  const uint64_t nsa = a->len_a - a->window + 1;
+  const uint64_t nsb = a->has_b ? a->len_b - a->window + 1 : nsa;
+  if (nsa >= (1ull << 32) || nsb >= (1ull << 32)) {
+    *msg = "Error: series longer than 2^32 windows are not supported";
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  if (a->anchor_interval < 0) { *msg = "Error: anchor_interval must be >= 0"; return SCAMP_ERR_INVALID_ARGS; }
+  return SCAMP_OK;
+}
+
+uint64_t diag_cells(int64_t n_r, int64_t n_c, int64_t d_lo, int64_t d_hi) {
+  // sum over d in [d_lo, d_hi) of min(n_r, n_c - d), d_hi <= n_c
+  if (d_hi <= d_lo) return 0;
+  uint64_t total = 0;
+  // part with n_c - d >= n_r  <=> d <= n_c - n_r
+  const int64_t split = n_c - n_r;  // d <= split -> n_r rows
+  const int64_t a_hi = std::min(d_hi - 1, split);
+  if (a_hi >= d_lo) total += static_cast<uint64_t>(a_hi - d_lo + 1) * n_r;
+  const int64_t b_lo = std::max(d_lo, split + 1);
+  if (b_lo < d_hi) {
+    // sum_{d=b_lo}^{d_hi-1} (n_c - d)
+    const uint64_t first = n_c - b_lo, last = n_c - (d_hi - 1);
+    total += (first + last) * static_cast<uint64_t>(d_hi - b_lo) / 2;
+  }
+  return total;
+}
+
+Plan make_plan(const scamp_c_args* a) {
+  Plan p;
+  p.self_join = !a->has_b;
+  p.m = static_cast<int64_t>(a->window);
+  p.ns_a = static_cast<int64_t>(a->len_a - a->window + 1);
+  p.ns_b = a->has_b ? static_cast<int64_t>(a->len_b - a->window + 1) : p.ns_a;
+  const int64_t excl = p.m / 4;  // src/tile.cpp:14
+  p.cells = 0;
+  if (p.self_join) {
+    // Upper triangle, diagonals >= m/4 (src/tile.cpp:12-38).  Row results go to
+    // profile A unless keep_rows_separate (src/tile.cpp:532-541).
+    ProblemPlan q{0, 0, p.ns_a, p.ns_a, excl, p.ns_a, 0, 0,
+                  a->computing_columns ? 0 : -1,
+                  a->computing_rows ? (a->keep_rows_separate ? 1 : 0) : -1};
+    if (q.d_hi > q.d_lo) p.probs.push_back(q);
+  } else {
+    const int col_t = a->computing_columns ? 0 : -1;
+    const int row_t = (a->computing_rows && a->keep_rows_separate) ? 1 : -1;
+    // Above the main diagonal: rows = B, cols = A.  Below it, transposed:
+    // rows = A, cols = B, diagonals >= 1 (src/tile.cpp:645-707).
+    ProblemPlan up{1, 0, p.ns_b, p.ns_a, 0, p.ns_a, 0, 0, col_t, row_t};
+    ProblemPlan lo{0, 1, p.ns_a, p.ns_b, 1, p.ns_b, 0, 0, row_t, col_t};
+    if (a->is_aligned) {
+      // Trivial-match exclusion |global_col - global_row| < m/4
+      // (src/tile.cpp:44-138).
+      int64_t off = 0;
+      if (a->distributed_start_row >= 0 && a->distributed_start_col >= 0)
+        off = a->distributed_start_col - a->distributed_start_row;
+      up.x_lo = -off - excl + 1;
+      up.x_hi = -off + excl;
+      lo.x_lo = off - excl + 1;
+      lo.x_hi = off + excl;
+    }
+    if (up.d_hi > up.d_lo && (up.col_target >= 0 || up.row_target >= 0)) p.probs.push_back(up);
+    if (lo.d_hi > lo.d_lo && (lo.col_target >= 0 || lo.row_target >= 0)) p.probs.push_back(lo);
+  }
+  for (const auto& q : p.probs) {
+    uint64_t c = diag_cells(q.n_r, q.n_c, q.d_lo, q.d_hi);
+    // excluded diagonals inside the range
+    const int64_t xl = std::max(q.x_lo, q.d_lo), xh = std::min(q.x_hi, q.d_hi);
+    if (xh > xl) c -= diag_cells(q.n_r, q.n_c, xl, xh);
+    p.cells += c;
+  }
+  return p;
+}
+
+KeyLayout make_key_layout(int64_t ns_max) {
+  KeyLayout kl;
+  int bits = 1;
+  while ((1ll << bits) < ns_max + 1) ++bits;
+  bits = std::max(bits, 20);
+  kl.idx_bits = bits;
+  kl.frac_bits = 62 - bits;
+  kl.idx_mask = (1ull << bits) - 1;
+  return kl;
+}
+
+// ---------------------------------------------------------------------------
+// Device workspace (grow-only, one per device, one join at a time).
+// ---------------------------------------------------------------------------
+struct Buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Workspace {
+  std::mutex mu;
+  int device = -1;
+  int sms = 0;
+  std::vector<Buf> bufs;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t evk0 = nullptr, evk1 = nullptr;  // around the join kernel
+  bool timed_kernel = false;
+};
+
+Workspace g_ws[64];
+
+int ensure(Workspace& ws, size_t slot, size_t bytes, void** out, std::string* msg) {
+  if (ws.bufs.size() <= slot) ws.bufs.resize(slot + 1);
+  Buf& b = ws.bufs[slot];
+  if (b.bytes < bytes) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    const size_t want = std::max<size_t>(bytes, 256);
+    if (cudaMalloc(&b.p, want) != cudaSuccess) {
+      cudaGetLastError();
+      *msg = "Error: out of device memory allocating " + std::to_string(want) + " bytes";
+      return SCAMP_ERR_OUT_OF_MEMORY;
+    }
+    b.bytes = want;
+  }
+  *out = b.p;
+  return SCAMP_OK;
+}
+
+enum Slot {
+  S_RAW_A, S_RAW_B,
+  S_T_A, S_MEAN_A, S_INV_A, S_DF_A, S_DG_A, S_INV32_A, S_DF32_A, S_DG32_A,
+  S_T_B, S_MEAN_B, S_INV_B, S_DF_B, S_DG_B, S_INV32_B, S_DF32_B, S_DG32_B,
+  S_KEY_A, S_KEY_B, S_SUM_A, S_SUM_B, S_PROF_A, S_PROF_B, S_CORR_A, S_CORR_B,
+  S_PREFIX, S_COUNTER,
+};
+
+#define CUDA_TRY(expr)                                                     \
+  do {                                                                     \
+    cudaError_t e_ = (expr);                                               \
+    if (e_ != cudaSuccess) {                                               \
+      *msg = std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " \
+             + #expr;                                                      \
+      return SCAMP_ERR_CUDA;                                               \
+    }                                                                      \
+  } while (0)
+
+struct SeriesBufs {
+  double *T, *mean, *inv, *df, *dg;
+  float *inv32, *df32, *dg32;
+};
+
+int alloc_series(Workspace& ws, int which, int64_t n, int64_t ns, SeriesBufs* s,
+                 std::string* msg) {
+  const int base = which == 0 ? S_T_A : S_T_B;
+  void* p;
+  int rc;
+  if ((rc = ensure(ws, base + 0, n * 8, &p, msg))) return rc; s->T = (double*)p;
+  if ((rc = ensure(ws, base + 1, ns * 8, &p, msg))) return rc; s->mean = (double*)p;
+  if ((rc = ensure(ws, base + 2, ns * 8, &p, msg))) return rc; s->inv = (double*)p;
+  if ((rc = ensure(ws, base + 3, ns * 8, &p, msg))) return rc; s->df = (double*)p;
+  if ((rc = ensure(ws, base + 4, ns * 8, &p, msg))) return rc; s->dg = (double*)p;
+  if ((rc = ensure(ws, base + 5, ns * 4, &p, msg))) return rc; s->inv32 = (float*)p;
+  if ((rc = ensure(ws, base + 6, ns * 4, &p, msg))) return rc; s->df32 = (float*)p;
+  if ((rc = ensure(ws, base + 7, ns * 4, &p, msg))) return rc; s->dg32 = (float*)p;
+  return SCAMP_OK;
+}
+
+SeriesDev to_dev(const SeriesBufs& s, int64_t n, int64_t ns) {
+  SeriesDev d;
+  d.T = s.T; d.mean = s.mean; d.inv = s.inv; d.df = s.df; d.dg = s.dg;
+  d.inv32 = s.inv32; d.df32 = s.df32; d.dg32 = s.dg32;
+  d.n = n; d.ns = ns;
+  return d;
+}
+
+// Runs a join whose inputs are device pointers; profile_a/b (packed entries)
+// and sum_a/b are device pointers too and are merged in place.
+int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
+               const double* dA, const double* dB, uint64_t* dprof_a,
+               uint64_t* dprof_b, double* dsum_a, double* dsum_b,
+               double* dcorr_a, double* dcorr_b, cudaStream_t st,
+               std::string* msg) {
+  Plan plan = make_plan(a);
+  const bool is_1nn = a->profile_type == SCAMP_PROFILE_1NN_INDEX;
+  const bool mixed = a->precision_type == SCAMP_PRECISION_MIXED ||
+                     a->precision_type == SCAMP_PRECISION_SINGLE;
+  const bool ultra = a->precision_type == SCAMP_PRECISION_ULTRA;
+  const int64_t m = plan.m;
+  const int64_t na = static_cast<int64_t>(a->len_a);
+  const int64_t nb = a->has_b ? static_cast<int64_t>(a->len_b) : na;
+  uint32_t launches = 0;
+  int rc;
+
+  ws.timed_kernel = false;
+  CUDA_TRY(cudaEventRecord(ws.ev0, st));
+
+  // ---- statistics ----
+  SeriesBufs sa{}, sb{};
+  if ((rc = alloc_series(ws, 0, na, plan.ns_a, &sa, msg))) return rc;
+  const int chunk = 64;
+  {
+    const int64_t threads = (plan.ns_a + chunk - 1) / chunk;
+    stats_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, st>>>(
+        dA, na, m, ultra ? 1 : 0, chunk, sa.T, sa.mean, sa.inv, sa.df, sa.dg,
+        sa.inv32, sa.df32, sa.dg32);
+    ++launches;
+  }
+  if (a->has_b) {
+    if ((rc = alloc_series(ws, 1, nb, plan.ns_b, &sb, msg))) return rc;
+    const int64_t threads = (plan.ns_b + chunk - 1) / chunk;
+    stats_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, st>>>(
+        dB, nb, m, ultra ? 1 : 0, chunk, sb.T, sb.mean, sb.inv, sb.df, sb.dg,
+        sb.inv32, sb.df32, sb.dg32);
+    ++launches;
+  } else {
+    sb = sa;
+  }
+  CUDA_TRY(cudaGetLastError());
+  SeriesDev devA = to_dev(sa, na, plan.ns_a);
+  SeriesDev devB = to_dev(sb, nb, plan.ns_b);
+
+  // ---- profiles: packed entries -> merge keys ----
+  const KeyLayout kl = make_key_layout(std::max(plan.ns_a, plan.ns_b));
+  uint64_t* keys[2] = {nullptr, nullptr};
+  double* sums[2] = {dsum_a, dsum_b};
+  uint64_t* profs[2] = {dprof_a, dprof_b};
+  const int64_t nsz[2] = {plan.ns_a, plan.ns_b};
+  bool used[2] = {false, false};
+  for (const auto& q : plan.probs) {
+    if (q.col_target >= 0) used[q.col_target] = true;
+    if (q.row_target >= 0) used[q.row_target] = true;
+  }
+  if (is_1nn) {
+    for (int s = 0; s < 2; ++s) {
+      if (!used[s] && !(s == 0 && profs[0])) continue;
+      if (!profs[s]) { *msg = "Error: profile buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
+      void* p;
+      if ((rc = ensure(ws, s == 0 ? S_KEY_A : S_KEY_B, nsz[s] * 8, &p, msg))) return rc;
+      keys[s] = static_cast<uint64_t*>(p);
+      profile_to_keys_kernel<<<static_cast<unsigned>((nsz[s] + 255) / 256), 256, 0, st>>>(
+          profs[s], keys[s], nsz[s], kl);
+      ++launches;
+    }
+  } else {
+    for (int s = 0; s < 2; ++s)
+      if (used[s] && !sums[s]) { *msg = "Error: sum buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
+  }
+
+  // ---- work plan ----
+  const int W = mixed ? mixed_band_width() : fp64_band_width();
+  const int slab = mixed ? mixed_slab_rows() : fp64_slab_rows();
+  const int nthreads = mixed ? mixed_threads() : fp64_threads();
+  const size_t smem = mixed ? mixed_smem_bytes() : 0;
+  if (mixed) {
+    CUDA_TRY(cudaFuncSetAttribute(join_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(smem)));
+  }
+  int occ = 1;
+  if (mixed)
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, join_mixed_kernel, nthreads, smem));
+  else
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, join_fp64_kernel, nthreads, 0));
+  occ = std::max(occ, 1);
+  const int64_t resident = static_cast<int64_t>(ws.sms) * occ;
+  // Segment length K: the anchor interval for the mixed form; for FP64 long
+  // enough that seeds cost ~1/32 of the cells.  Both shrink (down to one
+  // slab) when the join is too small to give every resident CTA ~8 units.
+  int64_t K;
+  const double cells_d = static_cast<double>(plan.cells);
+  const int64_t k_lb = static_cast<int64_t>(cells_d / (8.0 * resident * 2.0 * W));
+  if (mixed) {
+    K = a->anchor_interval > 0 ? a->anchor_interval : kDefaultAnchorInterval;
+  } else {
+    K = std::max<int64_t>(8 * m, 2048);
+  }
+  K = std::min(K, std::max<int64_t>(k_lb, slab));
+  K = std::max<int64_t>(slab, (K / slab) * slab);
+
+  JoinParams P{};
+  std::vector<int64_t> prefix;
+  prefix.push_back(0);
+  int64_t band_total = 0;
+  P.nprob = 0;
+  for (const auto& q : plan.probs) {
+    Problem& pr = P.prob[P.nprob++];
+    pr.R = q.rows_series == 0 ? devA : devB;
+    pr.C = q.cols_series == 0 ? devA : devB;
+    pr.d_lo = q.d_lo; pr.d_hi = q.d_hi; pr.x_lo = q.x_lo; pr.x_hi = q.x_hi;
+    pr.key_col = is_1nn && q.col_target >= 0 ? keys[q.col_target] : nullptr;
+    pr.key_row = is_1nn && q.row_target >= 0 ? keys[q.row_target] : nullptr;
+    pr.sum_col = !is_1nn && q.col_target >= 0 ? sums[q.col_target] : nullptr;
+    pr.sum_row = !is_1nn && q.row_target >= 0 ? sums[q.row_target] : nullptr;
+    pr.band_begin = band_total;
+    pr.nbands = (q.d_hi - q.d_lo + W - 1) / W;
+    for (int64_t b = 0; b < pr.nbands; ++b) {
+      const int64_t D0 = q.d_lo + b * W;
+      const int64_t rows = band_rows(q.n_r, q.n_c, D0);
+      const int64_t units = (rows + 2 * K - 1) / (2 * K);
+      prefix.push_back(prefix.back() + units);
+    }
+    band_total += pr.nbands;
+  }
+  P.total_bands = band_total;
+  P.total_units = prefix.back();
+  P.m = m;
+  P.seg_len = K;
+  P.band_width = W;
+  P.profile_type = a->profile_type;
+  P.threshold = a->distance_threshold;
+  P.kl = kl;
+
+  if (!a->silent_mode) {
+    std::printf("scamp_gb300: %s %s join, m=%lld, %s, %llu cells, %lld units of %d diagonals x 2x%lld rows\n",
+                plan.self_join ? "self" : "AB", is_1nn ? "1NN_INDEX" : "SUM_THRESH",
+                static_cast<long long>(m), mixed ? "mixed" : "fp64",
+                static_cast<unsigned long long>(plan.cells),
+                static_cast<long long>(P.total_units), W, static_cast<long long>(K));
+  }
+
+  if (P.total_units > 0) {
+    void* p;
+    if ((rc = ensure(ws, S_PREFIX, prefix.size() * 8, &p, msg))) return rc;
+    int64_t* dprefix = static_cast<int64_t*>(p);
+    CUDA_TRY(cudaMemcpyAsync(dprefix, prefix.data(), prefix.size() * 8, cudaMemcpyHostToDevice, st));
+    if ((rc = ensure(ws, S_COUNTER, 64, &p, msg))) return rc;
+    CUDA_TRY(cudaMemsetAsync(p, 0, 64, st));
+    P.band_unit_prefix = dprefix;
+    P.unit_counter = static_cast<unsigned long long*>(p);
+    P.error_flag = reinterpret_cast<int*>(static_cast<char*>(p) + 32);
+    const int64_t grid = std::min<int64_t>(resident, P.total_units);
+    CUDA_TRY(cudaEventRecord(ws.evk0, st));
+    ws.timed_kernel = true;
+    if (mixed)
+      join_mixed_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
+    else
+      join_fp64_kernel<<<static_cast<unsigned>(grid), nthreads, 0, st>>>(P);
+    ++launches;
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventRecord(ws.evk1, st));
+  }
+
+  // ---- keys -> packed entries (+ optional double correlations) ----
+  if (is_1nn) {
+    double* corr[2] = {dcorr_a, dcorr_b};
+    for (int s = 0; s < 2; ++s) {
+      if (!keys[s]) continue;
+      keys_to_profile_kernel<<<static_cast<unsigned>((nsz[s] + 255) / 256), 256, 0, st>>>(
+          keys[s], profs[s], corr[s], nsz[s], kl);
+      ++launches;
+    }
+  }
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaEventRecord(ws.ev1, st));
+  if (res) {
+    res->comparisons = plan.cells;
+    res->gpu_launches = launches;
+  }
+  return SCAMP_OK;
+}
+
+void read_times(Workspace& ws, scamp_c_result* res) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ws.ev0, ws.ev1);
+  res->elapsed_ms = ms;
+  res->join_kernel_ms = 0;
+  if (ws.timed_kernel) {
+    float k = 0;
+    cudaEventElapsedTime(&k, ws.evk0, ws.evk1);
+    res->join_kernel_ms = k;
+  }
+}
+
+int init_workspace(int device, Workspace** out, std::string* msg) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    *msg = "Error: no CUDA device available (this engine has no CPU fallback)";
+    return SCAMP_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= ndev || device >= 64) {
+    *msg = "Error: invalid device ordinal";
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  Workspace& ws = g_ws[device];
+  CUDA_TRY(cudaSetDevice(device));
+  if (ws.device < 0) {
+    CUDA_TRY(cudaDeviceGetAttribute(&ws.sms, cudaDevAttrMultiProcessorCount, device));
+    CUDA_TRY(cudaStreamCreateWithFlags(&ws.stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&ws.ev0));
+    CUDA_TRY(cudaEventCreate(&ws.ev1));
+    CUDA_TRY(cudaEventCreate(&ws.evk0));
+    CUDA_TRY(cudaEventCreate(&ws.evk1));
+    ws.device = device;
+  }
+  *out = &ws;
+  return SCAMP_OK;
+}
+
+}  // namespace
+}  // namespace scamp_gb300
+
+using namespace scamp_gb300;
+
+extern "C" int scamp_gb300_validate(const scamp_c_args* args, char* errbuf, size_t errlen) {
+  std::string msg;
+  const int rc = validate(args, &msg);
+  if (rc) set_err(errbuf, errlen, msg);
+  return rc;
+}
+
+extern "C" uint64_t scamp_gb300_count_cells(const scamp_c_args* args) {
+  std::string msg;
+  if (validate(args, &msg)) return 0;
+  return make_plan(args).cells;
+}
+
+extern "C" int scamp_gb300_gpu_supported(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n > 0 ? 1 : 0;
+}
+
+extern "C" const char* scamp_gb300_version(void) { return "scamp_gb300 0.1.0 (sm_103a)"; }
+
+extern "C" int scamp_gb300_pipe_peak(int device, int kind, double* ops_per_s) {
+  if (!ops_per_s || (kind != 0 && kind != 1)) return SCAMP_ERR_INVALID_ARGS;
+  return measure_pipe_peak(device, kind, ops_per_s) ? SCAMP_ERR_CUDA : SCAMP_OK;
+}
+
+extern "C" int scamp_gb300_join_dev(const scamp_c_args* args, scamp_c_result* res,
+                                    void* stream, char* errbuf, size_t errlen) {
+  std::string msg;
+  int rc = validate(args, &msg);
+  if (rc) { set_err(errbuf, errlen, msg); return rc; }
+  Workspace* ws;
+  if ((rc = init_workspace(args->device, &ws, &msg))) { set_err(errbuf, errlen, msg); return rc; }
+  std::lock_guard<std::mutex> lock(ws->mu);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  rc = run_device(*ws, args, res, args->timeseries_a, args->has_b ? args->timeseries_b : args->timeseries_a,
+                  res->profile_a, res->profile_b, res->sum_a, res->sum_b, res->corr_a, res->corr_b, st, &msg);
+  if (rc == SCAMP_OK) {
+    cudaError_t e = cudaEventSynchronize(ws->ev1);
+    if (e != cudaSuccess) { msg = std::string("CUDA error: ") + cudaGetErrorString(e); rc = SCAMP_ERR_CUDA; }
+    else {
+      read_times(*ws, res);
+    }
+  }
+  if (rc) set_err(errbuf, errlen, msg);
+  return rc;
+}
+
+extern "C" int scamp_gb300_join(const scamp_c_args* args, scamp_c_result* res,
+                                char* errbuf, size_t errlen) {
+  std::string msg;
+  int rc = validate(args, &msg);
+  if (rc) { set_err(errbuf, errlen, msg); return rc; }
+  if (!res) { set_err(errbuf, errlen, "Error: result struct missing"); return SCAMP_ERR_INVALID_ARGS; }
+  Workspace* ws;
+  if ((rc = init_workspace(args->device, &ws, &msg))) { set_err(errbuf, errlen, msg); return rc; }
+  std::lock_guard<std::mutex> lock(ws->mu);
+  cudaStream_t st = ws->stream;
+  const bool is_1nn = args->profile_type == SCAMP_PROFILE_1NN_INDEX;
+  const int64_t na = static_cast<int64_t>(args->len_a);
+  const int64_t nb = args->has_b ? static_cast<int64_t>(args->len_b) : 0;
+  const int64_t nsa = na - static_cast<int64_t>(args->window) + 1;
+  const int64_t nsb = args->has_b ? nb - static_cast<int64_t>(args->window) + 1 : nsa;
+  auto fail = [&](int code) { set_err(errbuf, errlen, msg); return code; };
+#define HOST_CUDA(expr)                                                       \
+  do {                                                                        \
+    cudaError_t e_ = (expr);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      msg = std::string("CUDA error: ") + cudaGetErrorString(e_);             \
+      return fail(SCAMP_ERR_CUDA);                                            \
+    }                                                                         \
+  } while (0)
+  void *pa, *pb = nullptr;
+  if ((rc = ensure(*ws, S_RAW_A, na * 8, &pa, &msg))) return fail(rc);
+  HOST_CUDA(cudaMemcpyAsync(pa, args->timeseries_a, na * 8, cudaMemcpyHostToDevice, st));
+  if (args->has_b) {
+    if ((rc = ensure(*ws, S_RAW_B, nb * 8, &pb, &msg))) return fail(rc);
+    HOST_CUDA(cudaMemcpyAsync(pb, args->timeseries_b, nb * 8, cudaMemcpyHostToDevice, st));
+  }
+  const bool want_b = args->keep_rows_separate != 0;
+  uint64_t *dprof[2] = {nullptr, nullptr};
+  double *dsum[2] = {nullptr, nullptr}, *dcorr[2] = {nullptr, nullptr};
+  uint64_t* hprof[2] = {res->profile_a, res->profile_b};
+  double* hsum[2] = {res->sum_a, res->sum_b};
+  double* hcorr[2] = {res->corr_a, res->corr_b};
+  const int64_t nsz[2] = {nsa, nsb};
+  for (int s = 0; s < 2; ++s) {
+    if (s == 1 && !want_b) continue;
+    void* p;
+    if (is_1nn) {
+      if (!hprof[s]) { msg = "Error: profile buffer missing"; return fail(SCAMP_ERR_INVALID_ARGS); }
+      if ((rc = ensure(*ws, s ? S_PROF_B : S_PROF_A, nsz[s] * 8, &p, &msg))) return fail(rc);
+      dprof[s] = static_cast<uint64_t*>(p);
+      HOST_CUDA(cudaMemcpyAsync(p, hprof[s], nsz[s] * 8, cudaMemcpyHostToDevice, st));
+      if (hcorr[s]) {
+        if ((rc = ensure(*ws, s ? S_CORR_B : S_CORR_A, nsz[s] * 8, &p, &msg))) return fail(rc);
+        dcorr[s] = static_cast<double*>(p);
+      }
+    } else {
+      if (!hsum[s]) { msg = "Error: sum buffer missing"; return fail(SCAMP_ERR_INVALID_ARGS); }
+      if ((rc = ensure(*ws, s ? S_SUM_B : S_SUM_A, nsz[s] * 8, &p, &msg))) return fail(rc);
+      dsum[s] = static_cast<double*>(p);
+      HOST_CUDA(cudaMemcpyAsync(p, hsum[s], nsz[s] * 8, cudaMemcpyHostToDevice, st));
+    }
+  }
+  rc = run_device(*ws, args, res, static_cast<double*>(pa),
+                  args->has_b ? static_cast<double*>(pb) : static_cast<double*>(pa),
+                  dprof[0], dprof[1], dsum[0], dsum[1], dcorr[0], dcorr[1], st, &msg);
+  if (rc) return fail(rc);
+  for (int s = 0; s < 2; ++s) {
+    if (s == 1 && !want_b) continue;
+    if (is_1nn) {
+      HOST_CUDA(cudaMemcpyAsync(hprof[s], dprof[s], nsz[s] * 8, cudaMemcpyDeviceToHost, st));
+      if (hcorr[s]) HOST_CUDA(cudaMemcpyAsync(hcorr[s], dcorr[s], nsz[s] * 8, cudaMemcpyDeviceToHost, st));
+    } else {
+      HOST_CUDA(cudaMemcpyAsync(hsum[s], dsum[s], nsz[s] * 8, cudaMemcpyDeviceToHost, st));
+    }
+  }
+  HOST_CUDA(cudaStreamSynchronize(st));
+  read_times(*ws, res);
+  return SCAMP_OK;
+#undef HOST_CUDA
+}

@@ -1,0 +1,174 @@
+// engine.cuh -- device-side types and helpers shared by the join kernels.
+//
+// Terminology follows the reference (zpzim/GPU-SCRIMP-LARGE): a join compares
+// every window ("subsequence") of a row series with every window of a column
+// series; cell (i, j) lies on diagonal d = j - i; its covariance advances along
+// the diagonal with cov(i+1, j+1) = cov(i, j) + df_c[j]*dg_r[i] + df_r[i]*dg_c[j]
+// (src/cpu_kernels.cpp:166-171, src/kernels_compute.h:425-435) and its Pearson
+// correlation is r = cov * invnorm_c[j] * invnorm_r[i].
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace scamp_gb300 {
+
+// ---------------------------------------------------------------------------
+// Profile keys.
+//
+// The 1NN_INDEX profile is merged on device with one 64-bit atomicMax per
+// update.  key = (q << idx_bits) | (idx_mask - index), where
+// q = floor((r + 2) * 2^F), F = 62 - idx_bits, is an order-preserving
+// fixed-point image of the correlation r in [-2, 2).  A larger r gives a
+// larger key; equal q resolve to the smaller index.  Key 0 is "no match"
+// (the reference's {-2.0f, 0xFFFFFFFF}, src/common.cpp:294-299).  NaN maps
+// to q = 0, so a NaN correlation never wins (the reference's strict '>'
+// compare, src/kernel_gpu_utils.h:138-179).  With idx_bits = 27 (series up to
+// 2^27 windows) the key resolves r to 2^-35 ~ 2.9e-11.
+// ---------------------------------------------------------------------------
+struct KeyLayout {
+  int idx_bits;           // bits for the index
+  int frac_bits;          // F = 62 - idx_bits
+  uint64_t idx_mask;      // (1 << idx_bits) - 1
+};
+
+// q from the raw bits of a double, integer pipe only (the FP64 pipe is the
+// bottleneck of the FP64 form, so no FP64 instruction is spent here).
+__device__ __forceinline__ uint64_t q_from_double_bits(uint64_t bits, int F) {
+  const uint32_t hi = static_cast<uint32_t>(bits >> 32);
+  const int e = static_cast<int>((hi >> 20) & 0x7FF);
+  // NaN / inf / |r| >= 2 never occur for valid cells; treat as no match.
+  if (e >= 1024) return 0;
+  const uint64_t sig = (bits & 0x000FFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0);
+  // |r| * 2^F = sig * 2^(e - 1075 + F); shift right by s = 1075 - F - e.
+  const int s = 1075 - F - e;
+  uint64_t mag = (s >= 64) ? 0 : (s >= 0 ? (sig >> s) : (sig << (-s)));
+  const uint64_t two = 2ull << F;  // 2 * 2^F
+  return (bits >> 63) ? (two - mag) : (two + mag);
+}
+
+__device__ __forceinline__ uint64_t q_from_float_bits(uint32_t bits, int F) {
+  const int e = static_cast<int>((bits >> 23) & 0xFF);
+  if (e >= 128) return 0;  // NaN, inf, |r| >= 2
+  const uint64_t sig = (bits & 0x7FFFFFu) | (e ? (1u << 23) : 0);
+  const int s = 150 - F - e;
+  uint64_t mag = (s >= 64) ? 0 : (s >= 0 ? (sig >> s) : (sig << (-s)));
+  const uint64_t two = 2ull << F;
+  return (bits >> 31) ? (two - mag) : (two + mag);
+}
+
+__device__ __forceinline__ uint64_t make_key(uint64_t q, int64_t index,
+                                             const KeyLayout& kl) {
+  return q == 0 ? 0ull
+                : (q << kl.idx_bits) | (kl.idx_mask - static_cast<uint64_t>(index));
+}
+
+__host__ __device__ __forceinline__ double key_to_corr(uint64_t key,
+                                                       const KeyLayout& kl) {
+  const uint64_t q = key >> kl.idx_bits;
+  return static_cast<double>(q) / static_cast<double>(1ull << kl.frac_bits) - 2.0;
+}
+
+__host__ __device__ __forceinline__ int64_t key_to_index(uint64_t key,
+                                                         const KeyLayout& kl) {
+  return static_cast<int64_t>(kl.idx_mask - (key & kl.idx_mask));
+}
+
+// ---------------------------------------------------------------------------
+// Series statistics resident in HBM (one set per input series).
+// ---------------------------------------------------------------------------
+struct SeriesDev {
+  const double* T;     // cleaned series (non-finite -> 0), n samples
+  const double* mean;  // window means, ns
+  const double* inv;   // inverse norms, NaN for NaN / flat windows, ns
+  const double* df;    // (T[i+m]-T[i])/2, 0 at the last window
+  const double* dg;    // (T[i+m]-mu[i+1]) + (T[i]-mu[i]), 0 at the last window
+  const float* inv32;  // FP32 copies for the mixed form
+  const float* df32;
+  const float* dg32;
+  int64_t n;
+  int64_t ns;
+};
+
+// One band problem: the cells (i, i + d) for d in [d_lo, d_hi) of a
+// (rows x cols) matrix.  A self-join is one problem; an AB-join is two (the
+// part above the main diagonal, and the part below it run transposed, as the
+// reference does, src/tile.cpp:645-707).
+struct Problem {
+  SeriesDev R;  // row series
+  SeriesDev C;  // column series
+  int64_t d_lo, d_hi;   // diagonal range
+  int64_t x_lo, x_hi;   // excluded diagonals (is_aligned), empty if x_lo >= x_hi
+  uint64_t* key_col;    // 1NN_INDEX target of column results (or null)
+  uint64_t* key_row;    // 1NN_INDEX target of row results (or null)
+  double* sum_col;      // SUM_THRESH targets
+  double* sum_row;
+  int64_t band_begin;   // first global band of this problem
+  int64_t nbands;
+};
+
+constexpr int kMaxProblems = 2;
+
+// Everything a join kernel needs, passed by value.
+struct JoinParams {
+  Problem prob[kMaxProblems];
+  int nprob;
+  const int64_t* band_unit_prefix;  // [total_bands + 1] unit offsets
+  int64_t total_bands;
+  int64_t total_units;
+  unsigned long long* unit_counter; // persistent work queue head
+  int* error_flag;                  // device error word (0 = ok)
+  int64_t m;                        // window length
+  int64_t seg_len;                  // K: rows per segment (two per unit)
+  int64_t band_width;               // W: diagonals per band
+  int profile_type;                 // 1 = 1NN_INDEX, 2 = SUM_THRESH
+  double threshold;
+  KeyLayout kl;
+};
+
+// Locates global band `g` and unit-within-band for unit index `u`.
+__device__ __forceinline__ void decode_unit(const JoinParams& P, int64_t u,
+                                            int* prob, int64_t* band,
+                                            int64_t* unit_in_band) {
+  // binary search: largest g with prefix[g] <= u
+  int64_t lo = 0, hi = P.total_bands;
+  while (hi - lo > 1) {
+    int64_t mid = (lo + hi) >> 1;
+    if (P.band_unit_prefix[mid] <= u) lo = mid; else hi = mid;
+  }
+  int p = 0;
+  while (p + 1 < P.nprob && lo >= P.prob[p + 1].band_begin) ++p;
+  *prob = p;
+  *band = lo - P.prob[p].band_begin;
+  *unit_in_band = u - P.band_unit_prefix[lo];
+}
+
+// Rows of band b (first diagonal D0): every row whose cell on D0 is inside.
+__host__ __device__ __forceinline__ int64_t band_rows(int64_t n_r, int64_t n_c,
+                                                      int64_t D0) {
+  int64_t r = n_c - D0;
+  return r < n_r ? r : n_r;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels (launch wrappers live in engine.cu).
+// ---------------------------------------------------------------------------
+__global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
+                             int64_t m, int ultra, int chunk,
+                             double* __restrict__ T_clean,
+                             double* __restrict__ mean, double* __restrict__ inv,
+                             double* __restrict__ df, double* __restrict__ dg,
+                             float* __restrict__ inv32, float* __restrict__ df32,
+                             float* __restrict__ dg32);
+
+__global__ void join_fp64_kernel(JoinParams P);
+__global__ void join_mixed_kernel(JoinParams P);
+
+__global__ void profile_to_keys_kernel(const uint64_t* __restrict__ in,
+                                       uint64_t* __restrict__ keys, int64_t n,
+                                       KeyLayout kl);
+__global__ void keys_to_profile_kernel(const uint64_t* __restrict__ keys,
+                                       uint64_t* __restrict__ out,
+                                       double* __restrict__ corr, int64_t n,
+                                       KeyLayout kl);
+
+}  // namespace scamp_gb300

@@ -1,0 +1,334 @@
+"""scamp_gb300 -- GB300-native SCAMP matrix-profile engine, Python front.
+
+Drop-in for pyscamp's join functions (reference: python/SCAMP_python.cpp of
+zpzim/GPU-SCRIMP-LARGE): ``selfjoin``, ``abjoin``, ``selfjoin_sum``,
+``abjoin_sum`` and ``gpu_supported`` keep their names, arguments, keyword
+validation, defaults and output conventions.  Every join runs on the GPU
+through the C ABI in include/scamp_gb300.h; there is no CPU fallback.
+
+``join`` is the lower-level entry that exposes the full SCAMPArgs surface
+(keep_rows, aligned, distributed offsets, precision, profile buffers to merge
+into) and returns the reference's packed 1NN_INDEX entries.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import SCAMPError
+
+__all__ = [
+    "selfjoin", "abjoin", "selfjoin_sum", "abjoin_sum", "gpu_supported",
+    "join", "join_device", "SCAMPError", "count_cells", "pipe_peak",
+    "unpack_profile", "to_distance", "version",
+]
+
+_PRECISION = {
+    "single": _lib.PRECISION_SINGLE,
+    "mixed": _lib.PRECISION_MIXED,
+    "double": _lib.PRECISION_DOUBLE,
+    "ultra": _lib.PRECISION_ULTRA,
+}
+_PROFILE = {"1NN_INDEX": _lib.PROFILE_1NN_INDEX, "SUM_THRESH": _lib.PROFILE_SUM_THRESH}
+
+# 1NN_INDEX "no match" entry {corr = -2.0f, index = 0xFFFFFFFF}
+# (src/common.cpp:294-299).
+NO_MATCH = np.uint64((0xFFFFFFFF << 32) | int(np.float32(-2.0).view(np.uint32)))
+
+
+def version():
+    return _lib.load().scamp_gb300_version().decode()
+
+
+def gpu_supported():
+    """True when the engine library loads and a CUDA device is visible
+    (pyscamp gpu_supported, python/SCAMP_python.cpp:363-369)."""
+    try:
+        return bool(_lib.load().scamp_gb300_gpu_supported())
+    except OSError:
+        return False
+
+
+def _args(a, b, m, profile, precision, computing_rows, computing_cols,
+          keep_rows, aligned, threshold, start_row, start_col, max_tile_size,
+          anchor_interval, device, silent):
+    ca = _lib.CArgs()
+    ca.timeseries_a = a.ctypes.data if a is not None else None
+    ca.len_a = len(a) if a is not None else 0
+    ca.has_b = 1 if b is not None else 0
+    ca.timeseries_b = b.ctypes.data if b is not None else None
+    ca.len_b = len(b) if b is not None else 0
+    ca.window = int(m)
+    ca.max_tile_size = int(max_tile_size)
+    ca.distributed_start_row = int(start_row)
+    ca.distributed_start_col = int(start_col)
+    ca.distance_threshold = float(threshold)
+    ca.precision_type = _PRECISION[precision] if isinstance(precision, str) else int(precision)
+    ca.profile_type = _PROFILE[profile] if isinstance(profile, str) else int(profile)
+    ca.computing_rows = int(bool(computing_rows))
+    ca.computing_columns = int(bool(computing_cols))
+    ca.keep_rows_separate = int(bool(keep_rows))
+    ca.is_aligned = int(bool(aligned))
+    ca.silent_mode = int(bool(silent))
+    ca.anchor_interval = int(anchor_interval)
+    ca.device = int(device)
+    return ca
+
+
+def count_cells(len_a, m, len_b=None, aligned=False, start_row=-1, start_col=-1):
+    """Distance-matrix cells a join evaluates (host logic, no GPU needed)."""
+    lib = _lib.load()
+    a = np.zeros(1)
+    ca = _args(None, None, m, "1NN_INDEX", "double", True, True, False, aligned,
+               0.0, start_row, start_col, max(128000, 2 * m), 0, 0, True)
+    ca.timeseries_a = a.ctypes.data
+    ca.len_a = int(len_a)
+    if len_b is not None:
+        ca.has_b = 1
+        ca.timeseries_b = a.ctypes.data
+        ca.len_b = int(len_b)
+    return int(lib.scamp_gb300_count_cells(ctypes.byref(ca)))
+
+
+def pipe_peak(kind="fp32", device=0):
+    """Measured FMA lane-operations per second of the FP32 or FP64 pipe."""
+    out = ctypes.c_double(0)
+    rc = _lib.load().scamp_gb300_pipe_peak(int(device), 0 if kind == "fp32" else 1,
+                                           ctypes.byref(out))
+    if rc:
+        raise SCAMPError(rc, "pipe peak probe failed")
+    return out.value
+
+
+def _check(rc, err):
+    if rc != _lib.SCAMP_OK:
+        msg = err.value.decode(errors="replace") or _lib.ERROR_NAMES.get(rc, str(rc))
+        if rc == 100:
+            raise ValueError(msg)
+        raise SCAMPError(rc, msg)
+
+
+def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
+         computing_rows=True, computing_cols=True, keep_rows=False,
+         aligned=False, threshold=0.0, start_row=-1, start_col=-1,
+         max_tile_size=128000, anchor_interval=0, device=0, profile_a=None,
+         profile_b=None, return_corr=False, silent=True, inplace=False):
+    """Run one join (the C ABI's scamp_gb300_join, host buffers).
+
+    For 1NN_INDEX returns ``profile_a`` (and ``profile_b`` with keep_rows) as
+    uint64 arrays in the reference's packed layout; ``profile_a`` /
+    ``profile_b`` given on input are merged into, like a best-so-far profile
+    passed to do_SCAMP.  For SUM_THRESH returns ``sum_a`` / ``sum_b``.
+    ``corr_a`` / ``corr_b`` (double correlations) when return_corr.
+    With ``inplace`` the given profile arrays (contiguous uint64 / float64)
+    are updated directly instead of copied (e.g. pinned host buffers).
+    """
+    lib = _lib.load()
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if b is not None:
+        b = np.ascontiguousarray(b, dtype=np.float64)
+    if m is None:
+        raise ValueError("window m is required")
+    ca = _args(a, b, m, profile, precision, computing_rows, computing_cols,
+               keep_rows, aligned, threshold, start_row, start_col,
+               max_tile_size, anchor_interval, device, silent)
+    err = ctypes.create_string_buffer(1024)
+    rc = lib.scamp_gb300_validate(ctypes.byref(ca), err, 1024)
+    _check(rc, err)
+    nsa = len(a) - m + 1
+    nsb = (len(b) if b is not None else len(a)) - m + 1
+    res = _lib.CResult()
+    out = {}
+    is_1nn = ca.profile_type == _lib.PROFILE_1NN_INDEX
+
+    def _buf(given, n, dtype, fill):
+        if given is None:
+            return np.full(n, fill, dtype=dtype)
+        if len(given) != n:
+            raise ValueError("profile buffer has %d entries, expected %d" % (len(given), n))
+        if inplace and given.dtype == dtype and given.flags["C_CONTIGUOUS"]:
+            return given
+        return np.array(given, dtype=dtype, copy=True)
+
+    if is_1nn:
+        pa = _buf(profile_a, nsa, np.uint64, NO_MATCH)
+        out["profile_a"] = pa
+        res.profile_a = pa.ctypes.data
+        if keep_rows:
+            pb = _buf(profile_b, nsb, np.uint64, NO_MATCH)
+            out["profile_b"] = pb
+            res.profile_b = pb.ctypes.data
+        if return_corr:
+            out["corr_a"] = np.empty(nsa)
+            res.corr_a = out["corr_a"].ctypes.data
+            if keep_rows:
+                out["corr_b"] = np.empty(nsb)
+                res.corr_b = out["corr_b"].ctypes.data
+    else:
+        sa = _buf(profile_a, nsa, np.float64, 0.0)
+        out["sum_a"] = sa
+        res.sum_a = sa.ctypes.data
+        if keep_rows:
+            sb = _buf(profile_b, nsb, np.float64, 0.0)
+            out["sum_b"] = sb
+            res.sum_b = sb.ctypes.data
+    rc = lib.scamp_gb300_join(ctypes.byref(ca), ctypes.byref(res), err, 1024)
+    _check(rc, err)
+    out["elapsed_ms"] = res.elapsed_ms
+    out["join_kernel_ms"] = res.join_kernel_ms
+    out["comparisons"] = int(res.comparisons)
+    out["gpu_launches"] = int(res.gpu_launches)
+    return out
+
+
+def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
+                precision="double", computing_rows=True, computing_cols=True,
+                keep_rows=False, aligned=False, threshold=0.0,
+                profile_a_ptr=None, profile_b_ptr=None, sum_a_ptr=None,
+                sum_b_ptr=None, corr_a_ptr=None, corr_b_ptr=None, stream=0,
+                anchor_interval=0, device=0, max_tile_size=128000):
+    """scamp_gb300_join_dev: every pointer is device memory (integers, e.g.
+    ``tensor.data_ptr()``), results merged in place, ordered on ``stream``."""
+    lib = _lib.load()
+    ca = _args(None, None, m, profile, precision, computing_rows, computing_cols,
+               keep_rows, aligned, threshold, -1, -1, max_tile_size,
+               anchor_interval, device, True)
+    ca.timeseries_a = a_ptr
+    ca.len_a = int(len_a)
+    if b_ptr is not None:
+        ca.has_b = 1
+        ca.timeseries_b = b_ptr
+        ca.len_b = int(len_b)
+    res = _lib.CResult()
+    res.profile_a, res.profile_b = profile_a_ptr, profile_b_ptr
+    res.sum_a, res.sum_b = sum_a_ptr, sum_b_ptr
+    res.corr_a, res.corr_b = corr_a_ptr, corr_b_ptr
+    err = ctypes.create_string_buffer(1024)
+    rc = lib.scamp_gb300_join_dev(ctypes.byref(ca), ctypes.byref(res),
+                                  ctypes.c_void_p(stream), err, 1024)
+    _check(rc, err)
+    return {"elapsed_ms": res.elapsed_ms, "join_kernel_ms": res.join_kernel_ms,
+            "comparisons": int(res.comparisons),
+            "gpu_launches": int(res.gpu_launches)}
+
+
+def unpack_profile(packed):
+    """(float32 correlation, int64 index) from packed 1NN_INDEX entries;
+    index -1 where there was no match."""
+    packed = np.asarray(packed, dtype=np.uint64)
+    corr = (packed & np.uint64(0xFFFFFFFF)).astype(np.uint32).view(np.float32)
+    idx = (packed >> np.uint64(32)).astype(np.int64)
+    idx[corr < -1] = -1
+    return corr, idx
+
+
+def to_distance(corr, m):
+    """ConvertToEuclidean (src/scamp_utils.cpp:127-133): sqrt(max(2m(1-r), 0)),
+    NaN where there was no match (r < -1)."""
+    corr = np.asarray(corr, dtype=np.float64)
+    with np.errstate(invalid="ignore"):
+        d = np.sqrt(np.maximum(2.0 * m * (1.0 - corr), 0.0))
+    d[corr < -1] = np.nan
+    return d
+
+
+# ---------------------------------------------------------------------------
+# pyscamp-compatible surface (python/SCAMP_python.cpp).
+# ---------------------------------------------------------------------------
+_NN_KEYS = {"verbose", "precision", "pearson", "gpus", "threads"}
+_SUM_KEYS = _NN_KEYS | {"threshold"}
+
+
+def _parse_kwargs(kwargs, allowed):
+    """Keyword handling of get_args_based_on_kwargs
+    (python/SCAMP_python.cpp:91-177); errors are ValueError like pybind11's
+    mapping of std::invalid_argument."""
+    opts = {"precision": "double", "pearson": False, "silent": True,
+            "threshold": 0.0, "device": 0}
+    for key, val in kwargs.items():
+        if key not in allowed:
+            raise ValueError("Invalid keyword argument specified unknown argument: " + key)
+        if key == "threshold":
+            thr = float(val)
+            if thr > 1 or thr < -1:
+                raise ValueError("Invalid threshold specified: value must be between -1 and 1")
+            opts["threshold"] = thr
+        elif key == "verbose":
+            opts["silent"] = not bool(val)
+        elif key == "precision":
+            if val not in _PRECISION:
+                raise ValueError("Invalid precision type specified: valid options are single, "
+                                 "mixed, double, ultra")
+            opts["precision"] = val
+        elif key == "pearson":
+            opts["pearson"] = bool(val)
+        elif key == "gpus":
+            gpus = [int(x) for x in val]
+            # One GPU per engine instance: the first listed device is used.
+            if gpus:
+                opts["device"] = gpus[0]
+        elif key == "threads":
+            if int(val) < 0:
+                raise ValueError("Invalid number of cpu worker threads specified, must be "
+                                 "greater than or equal to 0.")
+            # Accepted for compatibility; this engine has no CPU workers.
+    return opts
+
+
+def _split_1nn(packed, pearson, m):
+    """SplitProfile1NNINDEX (python/SCAMP_python.cpp:12-29)."""
+    corr, _ = unpack_profile(packed)
+    idx = (np.asarray(packed, dtype=np.uint64) >> np.uint64(32)).astype(np.uint32).view(np.int32)
+    if pearson:
+        nn = corr.astype(np.float64)
+        nn[nn < -1] = np.nan
+    else:
+        nn = to_distance(corr, m)
+    return nn.astype(np.float32), idx.copy()
+
+
+def selfjoin(a, m, **kwargs):
+    """Matrix profile of series ``a`` with window ``m``: (distances float32,
+    indices int32).  Same contract as pyscamp.selfjoin."""
+    o = _parse_kwargs(kwargs, _NN_KEYS)
+    r = join(np.asarray(a, dtype=np.float64), None, int(m), "1NN_INDEX", o["precision"],
+             computing_rows=True, computing_cols=True, silent=o["silent"], device=o["device"])
+    return _split_1nn(r["profile_a"], o["pearson"], int(m))
+
+
+def abjoin(a, b, m, **kwargs):
+    """For each window of ``a``, its nearest neighbour in ``b``: (distances
+    float32, indices into b int32).  Same contract as pyscamp.abjoin."""
+    o = _parse_kwargs(kwargs, _NN_KEYS)
+    r = join(np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64), int(m),
+             "1NN_INDEX", o["precision"], computing_rows=False, computing_cols=True,
+             silent=o["silent"], device=o["device"])
+    return _split_1nn(r["profile_a"], o["pearson"], int(m))
+
+
+def _sum_out(v):
+    # vec2pyarr with its default pearson=true (python/SCAMP_python.cpp:52-65,
+    # 297): values below -1 come back as NaN.
+    v = np.array(v, dtype=np.float64)
+    v[v < -1] = np.nan
+    return v
+
+
+def selfjoin_sum(a, m, **kwargs):
+    """Per window of ``a``, the sum of correlations above ``threshold``
+    (default 0) to the other windows of ``a`` (pyscamp.selfjoin_sum)."""
+    o = _parse_kwargs(kwargs, _SUM_KEYS)
+    r = join(np.asarray(a, dtype=np.float64), None, int(m), "SUM_THRESH", o["precision"],
+             computing_rows=True, computing_cols=True, threshold=o["threshold"],
+             silent=o["silent"], device=o["device"])
+    return _sum_out(r["sum_a"])
+
+
+def abjoin_sum(a, b, m, **kwargs):
+    """Per window of ``a``, the sum of correlations above ``threshold`` to the
+    windows of ``b`` (pyscamp.abjoin_sum)."""
+    o = _parse_kwargs(kwargs, _SUM_KEYS)
+    r = join(np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64), int(m),
+             "SUM_THRESH", o["precision"], computing_rows=False, computing_cols=True,
+             threshold=o["threshold"], silent=o["silent"], device=o["device"])
+    return _sum_out(r["sum_a"])

@@ -1,0 +1,138 @@
+/*
+ * scamp_gb300.h -- C ABI of the GB300 SCAMP matrix-profile engine.
+ *
+ * The reference (zpzim/GPU-SCRIMP-LARGE) exposes this path through the C++
+ * entry SCAMP::do_SCAMP(SCAMPArgs*) (src/SCAMP.h:15-18, src/SCAMP.cpp:261-334)
+ * and pyscamp's selfjoin/abjoin (python/SCAMP_python.cpp:196-236).  Both sit on
+ * top of the functions below: the C++ shim (include/scamp/SCAMP.h) and the
+ * Python package (scamp_gb300) call scamp_gb300_join().  Plain C types only:
+ * no exceptions or C++ objects cross this boundary.
+ *
+ * Precision: SCAMP_PRECISION_DOUBLE runs every step in FP64.
+ * SCAMP_PRECISION_MIXED runs the diagonal recurrence and the compare in FP32,
+ * re-anchored from FP64-centred data every anchor_interval rows.
+ * SCAMP_PRECISION_SINGLE is served by the mixed engine; SCAMP_PRECISION_ULTRA
+ * is served by the FP64 engine with brute-force O(nm) window statistics.
+ */
+#ifndef SCAMP_GB300_H
+#define SCAMP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Values of the reference enums SCAMPProfileType / SCAMPPrecisionType
+ * (src/common.h:34-58). */
+enum {
+  SCAMP_PROFILE_1NN_INDEX = 1,
+  SCAMP_PROFILE_SUM_THRESH = 2,
+};
+enum {
+  SCAMP_PRECISION_SINGLE = 1,
+  SCAMP_PRECISION_MIXED = 2,
+  SCAMP_PRECISION_DOUBLE = 3,
+  SCAMP_PRECISION_ULTRA = 4,
+};
+
+/* Status codes (0 = success).  The first six mirror SCAMPError_t
+ * (src/common.h:359-367); the rest are boundary errors. */
+enum {
+  SCAMP_OK = 0,
+  SCAMP_ERR_UNIMPLEMENTED = 1,
+  SCAMP_ERR_CUDA = 3,
+  SCAMP_ERR_DIM_INCOMPATIBLE = 6,
+  SCAMP_ERR_INVALID_ARGS = 100,
+  SCAMP_ERR_NO_DEVICE = 101,
+  SCAMP_ERR_OUT_OF_MEMORY = 102,
+  SCAMP_ERR_DEVICE_TIMEOUT = 103,
+};
+
+/* Join arguments: the plain-C image of SCAMPArgs (src/common.h:164-188). */
+typedef struct scamp_c_args {
+  const double *timeseries_a; /* host or device memory, see *_dev entry */
+  uint64_t len_a;
+  const double *timeseries_b; /* ignored unless has_b */
+  uint64_t len_b;
+  int32_t has_b;              /* 0: self-join of A */
+  uint64_t window;            /* subsequence length m (>= 3) */
+  uint64_t max_tile_size;     /* validated as the reference does; work is
+                                 scheduled on device independently of it */
+  int64_t distributed_start_row; /* -1 when unused */
+  int64_t distributed_start_col; /* -1 when unused */
+  double distance_threshold;  /* SUM_THRESH: sum correlations > threshold */
+  int32_t precision_type;     /* SCAMP_PRECISION_* */
+  int32_t profile_type;       /* SCAMP_PROFILE_* */
+  int32_t computing_rows;
+  int32_t computing_columns;
+  int32_t keep_rows_separate;
+  int32_t is_aligned;
+  int32_t silent_mode;
+  /* Tuning overrides, 0 = automatic. */
+  int32_t anchor_interval;    /* mixed: rows between FP64-centred re-anchors */
+  int32_t device;             /* CUDA device ordinal */
+  int32_t reserved[6];
+} scamp_c_args;
+
+/* Results.  Profiles are in/out: on entry they hold the best-so-far values
+ * (InitProfileMemory semantics, src/scamp_utils.cpp:226-245: 1NN_INDEX
+ * entries {corr=-2.0f, index=0xFFFFFFFF}, SUM_THRESH zeros); the join merges
+ * into them exactly as the reference merges tiles (src/common.cpp:167-197).
+ * 1NN_INDEX entries use the reference layout (src/common.h:70-74): low 32
+ * bits = float32 Pearson correlation, high 32 bits = uint32 index. */
+typedef struct scamp_c_result {
+  uint64_t *profile_a;  /* 1NN_INDEX, len_a - window + 1 entries */
+  uint64_t *profile_b;  /* 1NN_INDEX rows when keep_rows_separate */
+  double *sum_a;        /* SUM_THRESH, len_a - window + 1 entries */
+  double *sum_b;        /* SUM_THRESH rows when keep_rows_separate */
+  double *corr_a;       /* optional: best correlation in double, -2 = none */
+  double *corr_b;       /* optional */
+  /* Filled by the engine. */
+  double elapsed_ms;    /* device time of the join (stats .. final profile) */
+  double join_kernel_ms;/* device time of the join kernel alone */
+  uint64_t comparisons; /* distance-matrix cells evaluated */
+  uint32_t gpu_launches;/* kernels launched by this call */
+  uint32_t reserved[5];
+} scamp_c_result;
+
+/* Runs one join.  Inputs and results are HOST memory; the engine copies them
+ * to the device, runs every step there and copies the profiles back.
+ * Returns SCAMP_OK or an error code; a message goes to errbuf (may be NULL).
+ * Replaces SCAMP::do_SCAMP (src/SCAMP.cpp:279-334), whose errors are thrown
+ * as SCAMPException (src/common.cpp:417-436, 539-547). */
+int scamp_gb300_join(const scamp_c_args *args, scamp_c_result *res,
+                     char *errbuf, size_t errlen);
+
+/* Same join with every pointer in args/res being DEVICE memory of
+ * args->device, ordered on `stream` (a cudaStream_t, NULL = default stream).
+ * Used when the inputs are already resident in HBM. */
+int scamp_gb300_join_dev(const scamp_c_args *args, scamp_c_result *res,
+                         void *stream, char *errbuf, size_t errlen);
+
+/* Checks arguments the way SCAMPArgs::validate does (src/common.cpp:417-436).
+ * Pure host logic, needs no GPU. */
+int scamp_gb300_validate(const scamp_c_args *args, char *errbuf, size_t errlen);
+
+/* Number of distance-matrix cells a join evaluates (the comparisons of the
+ * comparisons/s metric).  Pure host logic. */
+uint64_t scamp_gb300_count_cells(const scamp_c_args *args);
+
+/* 1 if a CUDA device is usable (pyscamp gpu_supported,
+ * python/SCAMP_python.cpp:363-369). */
+int scamp_gb300_gpu_supported(void);
+
+/* Measured throughput of one GPU pipe, for roofline denominators:
+ * kind 0 = FP32 FMA lane-ops/s (packed f32x2), 1 = FP64 FMA lane-ops/s.
+ * Has no counterpart in the reference. */
+int scamp_gb300_pipe_peak(int device, int kind, double *ops_per_s);
+
+/* Library version string. */
+const char *scamp_gb300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCAMP_GB300_H */

@@ -44,6 +44,7 @@ class _Args(ctypes.Structure):
         ("threads", ctypes.c_int),
         ("brute_force", ctypes.c_int),
         ("high_precision_stats", ctypes.c_int),
+        ("exact_flat", ctypes.c_int),
     ]
 
 
@@ -125,7 +126,7 @@ def pack(corr, idx):
 def join(a, b=None, m=None, profile="1NN_INDEX", computing_rows=True,
          computing_cols=True, keep_rows=False, aligned=False, start_row=-1,
          start_col=-1, threshold=0.0, threads=0, brute=False,
-         high_precision_stats=False):
+         high_precision_stats=False, exact_flat=False):
     """Matrix-profile join on the CPU oracle.
 
     Returns a dict with, per profile side that is produced, ``corr_*``
@@ -144,7 +145,7 @@ def join(a, b=None, m=None, profile="1NN_INDEX", computing_rows=True,
                  len(b) if has_b else 0, m, ptype, int(computing_rows),
                  int(computing_cols), int(keep_rows), int(aligned), start_row,
                  start_col, float(threshold), int(threads), int(brute),
-                 int(high_precision_stats))
+                 int(high_precision_stats), int(exact_flat))
     res = {}
     out = _Out()
     if ptype == PROFILE_1NN_INDEX:

@@ -203,6 +203,7 @@ typedef struct {
   int threads;      /* 0 = all available */
   int brute_force;  /* 1: every cell from a fresh compensated dot product */
   int high_precision_stats; /* 1: ULTRA-style brute force means / ssd */
+  int exact_flat; /* 1: decide flatness (ssd <= 1e-13) from an exact ssd */
 } oracle_args;
 
 typedef struct {
@@ -336,7 +337,7 @@ typedef struct {
 } series_t;
 
 static int series_init(series_t *s, const double *T, int64_t n, int64_t m,
-                       int hp) {
+                       int hp, int exact_flat) {
   s->n = n;
   s->ns = n - m + 1;
   s->T_clean = malloc(sizeof(double) * n);
@@ -349,6 +350,23 @@ static int series_init(series_t *s, const double *T, int64_t n, int64_t m,
     return -1;
   oracle_clean(T, n, m, s->T_clean, s->nanwin);
   oracle_stats(s->T_clean, s->nanwin, n, m, hp, s->mu, s->in, s->df, s->dg);
+  if (exact_flat) {
+    /* The reference's sequential ssd recurrence can leave a rounding residue
+     * above 1e-13 on exactly flat windows; this mode applies the flatness
+     * rule to a directly summed ssd instead. */
+    for (int64_t i = 0; i < s->ns; ++i) {
+      if (s->nanwin[i]) continue;
+      double mu = 0;
+      for (int64_t t = 0; t < m; ++t) mu += s->T_clean[i + t];
+      mu /= m;
+      double ss = 0;
+      for (int64_t t = 0; t < m; ++t) {
+        double v = s->T_clean[i + t] - mu;
+        ss += v * v;
+      }
+      s->in[i] = ss <= FLATNESS_EPSILON ? NAN : 1.0 / sqrt(ss);
+    }
+  }
   return 0;
 }
 
@@ -405,8 +423,11 @@ int oracle_join(const oracle_args *args, oracle_out *out) {
   if (ptype != ORACLE_PROFILE_1NN_INDEX && ptype != ORACLE_PROFILE_SUM_THRESH)
     return -2;
   series_t A, B;
-  if (series_init(&A, args->a, args->na, m, args->high_precision_stats)) return -3;
-  if (!self && series_init(&B, args->b, args->nb, m, args->high_precision_stats)) {
+  if (series_init(&A, args->a, args->na, m, args->high_precision_stats,
+                  args->exact_flat))
+    return -3;
+  if (!self && series_init(&B, args->b, args->nb, m, args->high_precision_stats,
+                           args->exact_flat)) {
     series_free(&A);
     return -3;
   }

@@ -1,0 +1,185 @@
+"""Pins the CPU oracle (oracle/scamp_oracle.c) before it is trusted.
+
+1. Against the golden outputs shipped with the reference
+   (test/SampleOutput/mp_*, mpi_*; tolerances of test/difference.py:24 and
+   test/run_tests.sh:36) -- read where the reference tree is present.
+2. Against the reference's own CPU path compiled from its sources
+   (oracle/_ref/libscampref.so) on seeded inputs -- where it was built.
+3. Against the committed fixtures tests/golden/*.npz, produced by that same
+   compiled reference (tests/golden/make_golden.py) -- always.
+4. Against a brute-force compensated-dot evaluation of every cell and
+   against numpy's corrcoef (the reference's distance_matrix_np,
+   test/distance_matrix_fast.py) -- always.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from parity import pair_corr
+
+REF = "/root/reference/test"
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+
+def _distance(oracle, packed, m):
+    c, i = oracle.unpack(packed)
+    return oracle.to_distance(c, m), i
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
+@pytest.mark.parametrize("name", ["randomwalk8K", "randomwalk16K", "randomwalk32K",
+                                  "randomwalk64K", "randomwalk64K_nan"])
+def test_oracle_vs_reference_goldens_selfjoin(oracle_mod, name):
+    a = np.loadtxt(os.path.join(REF, "SampleInput", name + ".txt"))
+    gd = np.loadtxt(os.path.join(REF, "SampleOutput", "mp_%s_w100.txt" % name))
+    gi = np.loadtxt(os.path.join(REF, "SampleOutput", "mpi_%s_w100.txt" % name)).astype(np.int64)
+    d, i = _distance(oracle_mod, oracle_mod.join(a, None, 100)["packed_a"], 100)
+    assert np.array_equal(np.isnan(d), np.isnan(gd))
+    ok = ~np.isnan(gd)
+    assert np.max(np.abs(d[ok] - gd[ok])) <= 0.01
+    assert np.max(np.abs(d[ok] - gd[ok])) <= 1e-5  # observed ~2e-6
+    assert np.sum(i != gi) <= len(gi) // 100
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
+@pytest.mark.parametrize("na,nb", [("randomwalk16K", "randomwalk32K"),
+                                   ("randomwalk32K", "randomwalk16K")])
+def test_oracle_vs_reference_goldens_abjoin(oracle_mod, na, nb):
+    a = np.loadtxt(os.path.join(REF, "SampleInput", na + ".txt"))
+    b = np.loadtxt(os.path.join(REF, "SampleInput", nb + ".txt"))
+    gd = np.loadtxt(os.path.join(REF, "SampleOutput", "mp_%s_%s_w100.txt" % (na, nb)))
+    gi = np.loadtxt(os.path.join(REF, "SampleOutput", "mpi_%s_%s_w100.txt" % (na, nb))).astype(np.int64)
+    d, i = _distance(oracle_mod, oracle_mod.join(a, b, 100, computing_rows=False)["packed_a"], 100)
+    assert np.max(np.abs(d - gd)) <= 1e-5
+    assert np.sum(i != gi) <= len(gi) // 100
+
+
+def _ref_cases():
+    rng = np.random.default_rng(99)
+    cases = []
+    for n, m in [(3000, 100), (2000, 7), (1777, 64)]:
+        a = np.cumsum(rng.standard_normal(n))
+        cases.append(("self%d" % n, a, None, m, {}))
+    a = np.cumsum(rng.standard_normal(2500))
+    b = np.cumsum(rng.standard_normal(1800))
+    b[rng.choice(1800, 9, replace=False)] = np.nan
+    cases.append(("ab_keep", a, b, 50, {"keep_rows": True}))
+    cases.append(("ab_cols", a, b, 50, {"computing_rows": False}))
+    cases.append(("ab_aligned", a, a.copy(), 50, {"aligned": True, "computing_rows": False}))
+    return cases
+
+
+@pytest.mark.parametrize("case", _ref_cases(), ids=lambda c: c[0])
+def test_oracle_vs_compiled_reference(oracle_mod, case):
+    if not oracle_mod.ref_available():
+        pytest.skip("reference CPU path not built here")
+    name, a, b, m, kw = case
+    want = oracle_mod.ref_join(a, b, m, threads=4, **kw)
+    got = oracle_mod.join(a, b, m, **kw)
+    for side in ("a", "b"):
+        key = "packed_" + side
+        if key not in want:
+            continue
+        wc, wi = oracle_mod.unpack(want[key])
+        gc, gi = oracle_mod.unpack(got[key])
+        assert np.array_equal(wc < -1, gc < -1)
+        ok = wc >= -1
+        # float32 correlations: bit-identical or one ulp apart
+        assert np.max(np.abs(wc[ok].astype(np.float64) - gc[ok])) <= 2.5e-7
+        # index mismatches only where the float32 correlations tie
+        # (test/test_common.py:3-16)
+        mism = ok & (wi != gi)
+        assert np.all(np.abs(wc[mism].astype(np.float64) - gc[mism]) <= 2.5e-7)
+
+
+@pytest.mark.parametrize("thr", [0.0, 0.5])
+def test_oracle_sum_vs_compiled_reference(oracle_mod, thr):
+    if not oracle_mod.ref_available():
+        pytest.skip("reference CPU path not built here")
+    rng = np.random.default_rng(5)
+    a = np.cumsum(rng.standard_normal(2000))
+    b = np.cumsum(rng.standard_normal(1500))
+    for bb, kw in ((None, {}), (b, {"keep_rows": True})):
+        want = oracle_mod.ref_join(a, bb, 64, profile="SUM_THRESH", threshold=thr, threads=2, **kw)
+        got = oracle_mod.join(a, bb, 64, profile="SUM_THRESH", threshold=thr, **kw)
+        for side in ("sum_a", "sum_b"):
+            if side in want:
+                np.testing.assert_allclose(got[side], want[side], rtol=1e-6, atol=1e-6)
+
+
+def test_oracle_vs_committed_golden_fixtures(oracle_mod):
+    files = sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+    assert files, "no golden fixtures committed"
+    for f in files:
+        z = np.load(f, allow_pickle=False)
+        kw = {k[3:]: (bool(z[k]) if z[k].dtype == bool else z[k].item())
+              for k in z.files if k.startswith("kw_")}
+        a = z["a"]
+        b = z["b"] if "b" in z.files else None
+        m = int(z["m"])
+        got = oracle_mod.join(a, b, m, **kw)
+        for side in ("a", "b"):
+            if "packed_" + side in z.files:
+                wc, wi = oracle_mod.unpack(z["packed_" + side])
+                gc, gi = oracle_mod.unpack(got["packed_" + side])
+                ok = wc >= -1
+                assert np.array_equal(wc < -1, gc < -1), f
+                assert np.max(np.abs(wc[ok].astype(np.float64) - gc[ok])) <= 2.5e-7, f
+            if "sum_" + side in z.files:
+                np.testing.assert_allclose(got["sum_" + side], z["sum_" + side], rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("m", [4, 10, 33])
+def test_oracle_recurrence_vs_brute_force(oracle_mod, m):
+    rng = np.random.default_rng(m)
+    a = np.cumsum(rng.standard_normal(700))
+    a[rng.choice(700, 3, replace=False)] = np.nan
+    b = np.cumsum(rng.standard_normal(500))
+    for bb, kw in ((None, {}), (b, {"keep_rows": True})):
+        fast = oracle_mod.join(a, bb, m, **kw)
+        brute = oracle_mod.join(a, bb, m, brute=True, **kw)
+        for side in ("a", "b"):
+            if "corr_" + side not in fast:
+                continue
+            assert np.array_equal(fast["idx_" + side] < 0, brute["idx_" + side] < 0)
+            ok = brute["idx_" + side] >= 0
+            assert np.max(np.abs(fast["corr_" + side][ok] - brute["corr_" + side][ok])) < 1e-10
+
+
+def test_oracle_vs_numpy_corrcoef(oracle_mod):
+    # distance_matrix_np (test/distance_matrix_fast.py): corrcoef over all
+    # window pairs, exclusion |i - j| < m/4 masked, column max.
+    rng = np.random.default_rng(8)
+    a = rng.standard_normal(400)
+    m = 20
+    W = np.lib.stride_tricks.sliding_window_view(a, m)
+    C = np.corrcoef(W)
+    ns = len(W)
+    ii, jj = np.meshgrid(np.arange(ns), np.arange(ns), indexing="ij")
+    C[np.abs(ii - jj) < m // 4] = -2
+    got = oracle_mod.join(a, None, m)
+    np.testing.assert_allclose(got["corr_a"], C.max(axis=0), atol=1e-12)
+    r = pair_corr(a, a, m, got["idx_a"], np.arange(ns))
+    np.testing.assert_allclose(r, C.max(axis=0), atol=1e-12)
+
+
+def test_oracle_stats_restatement(oracle_mod):
+    # compute_statistics_cpu semantics (src/cpu_stats.cpp:123-160)
+    rng = np.random.default_rng(2)
+    T = np.cumsum(rng.standard_normal(500))
+    T[100] = np.nan
+    T[300:340] = 1.5
+    m = 16
+    s = oracle_mod.stats(T, m)
+    assert s["nanwin"][85:101].all() and not s["nanwin"][84] and not s["nanwin"][101]
+    assert np.isnan(s["invnorm"][300:325]).all()  # flat windows
+    Tc = s["clean"]
+    ns = len(T) - m + 1
+    assert s["df"][ns - 1] == 0 and s["dg"][ns - 1] == 0
+    i = 50
+    assert np.isclose(s["df"][i], (Tc[i + m] - Tc[i]) / 2)
+    mu = np.array([Tc[k:k + m].mean() for k in range(ns)])
+    np.testing.assert_allclose(s["mean"], mu, rtol=1e-12, atol=1e-12)
