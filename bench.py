@@ -284,6 +284,9 @@ def main():
     pb_pin[:] = scamp_gb300.NO_MATCH
     e2e_t = []
     for it in range(args.warmup + args.steps):
+        # every step starts from an empty profile, like the device-resident leg
+        pa_pin[:] = scamp_gb300.NO_MATCH
+        pb_pin[:] = scamp_gb300.NO_MATCH
         with torch.cuda.stream(stream):
             flush.fill_(2)
         torch.cuda.synchronize()

@@ -32,6 +32,10 @@ int mixed_band_width();
 int mixed_slab_rows();
 int mixed_threads();
 size_t mixed_smem_bytes();
+int mixed_1nn_band_width();
+int mixed_1nn_slab_rows();
+int mixed_1nn_threads();
+size_t mixed_1nn_smem_bytes();
 int measure_pipe_peak(int device, int kind, double* ops_per_s);
 
 namespace {
@@ -219,7 +223,8 @@ enum Slot {
   S_T_A, S_MEAN_A, S_INV_A, S_DF_A, S_DG_A, S_INV32_A, S_DF32_A, S_DG32_A,
   S_T_B, S_MEAN_B, S_INV_B, S_DF_B, S_DG_B, S_INV32_B, S_DF32_B, S_DG32_B,
   S_KEY_A, S_KEY_B, S_SUM_A, S_SUM_B, S_PROF_A, S_PROF_B, S_CORR_A, S_CORR_B,
-  S_PREFIX, S_COUNTER,
+  S_PREFIX, S_COUNTER, S_T32_A, S_T32_B, S_BHI_A, S_BLO_A, S_MUREL_A,
+  S_BHI_B, S_BLO_B, S_MUREL_B,
 };
 
 #define CUDA_TRY(expr)                                                     \
@@ -234,8 +239,17 @@ enum Slot {
 
 struct SeriesBufs {
   double *T, *mean, *inv, *df, *dg;
-  float *inv32, *df32, *dg32;
+  float *inv32, *df32, *dg32, *T32, *bhi, *blo, *mu_rel;
+  int bshift;
 };
+
+// Block size of the locally offset FP32 copy: 32 samples, or m/16 for long
+// windows (a window then spans at most 17 blocks).
+int block_shift(int64_t m) {
+  int s = 5;
+  while ((1ll << s) * 16 < m) ++s;
+  return s;
+}
 
 int alloc_series(Workspace& ws, int which, int64_t n, int64_t ns, SeriesBufs* s,
                  std::string* msg) {
@@ -250,6 +264,11 @@ int alloc_series(Workspace& ws, int which, int64_t n, int64_t ns, SeriesBufs* s,
   if ((rc = ensure(ws, base + 5, ns * 4, &p, msg))) return rc; s->inv32 = (float*)p;
   if ((rc = ensure(ws, base + 6, ns * 4, &p, msg))) return rc; s->df32 = (float*)p;
   if ((rc = ensure(ws, base + 7, ns * 4, &p, msg))) return rc; s->dg32 = (float*)p;
+  if ((rc = ensure(ws, which == 0 ? S_T32_A : S_T32_B, n * 4, &p, msg))) return rc; s->T32 = (float*)p;
+  const int64_t nblk = (n >> s->bshift) + 1;
+  if ((rc = ensure(ws, which == 0 ? S_BHI_A : S_BHI_B, nblk * 4, &p, msg))) return rc; s->bhi = (float*)p;
+  if ((rc = ensure(ws, which == 0 ? S_BLO_A : S_BLO_B, nblk * 4, &p, msg))) return rc; s->blo = (float*)p;
+  if ((rc = ensure(ws, which == 0 ? S_MUREL_A : S_MUREL_B, ns * 4, &p, msg))) return rc; s->mu_rel = (float*)p;
   return SCAMP_OK;
 }
 
@@ -257,6 +276,7 @@ SeriesDev to_dev(const SeriesBufs& s, int64_t n, int64_t ns) {
   SeriesDev d;
   d.T = s.T; d.mean = s.mean; d.inv = s.inv; d.df = s.df; d.dg = s.dg;
   d.inv32 = s.inv32; d.df32 = s.df32; d.dg32 = s.dg32;
+  d.T32 = s.T32; d.bhi = s.bhi; d.blo = s.blo; d.mu_rel = s.mu_rel; d.bshift = s.bshift;
   d.n = n; d.ns = ns;
   return d;
 }
@@ -284,22 +304,23 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
 
   // ---- statistics ----
   SeriesBufs sa{}, sb{};
+  sa.bshift = sb.bshift = block_shift(m);
   if ((rc = alloc_series(ws, 0, na, plan.ns_a, &sa, msg))) return rc;
   const int chunk = 64;
   {
     const int64_t threads = (plan.ns_a + chunk - 1) / chunk;
     stats_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, st>>>(
-        dA, na, m, ultra ? 1 : 0, chunk, sa.T, sa.mean, sa.inv, sa.df, sa.dg,
-        sa.inv32, sa.df32, sa.dg32);
-    ++launches;
+        dA, na, m, ultra ? 1 : 0, chunk, sa.bshift, sa.T, sa.T32, sa.bhi, sa.blo, sa.mu_rel,
+        sa.mean, sa.inv, sa.df, sa.dg, sa.inv32, sa.df32, sa.dg32);
+    launches += 1;
   }
   if (a->has_b) {
     if ((rc = alloc_series(ws, 1, nb, plan.ns_b, &sb, msg))) return rc;
     const int64_t threads = (plan.ns_b + chunk - 1) / chunk;
     stats_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, st>>>(
-        dB, nb, m, ultra ? 1 : 0, chunk, sb.T, sb.mean, sb.inv, sb.df, sb.dg,
-        sb.inv32, sb.df32, sb.dg32);
-    ++launches;
+        dB, nb, m, ultra ? 1 : 0, chunk, sb.bshift, sb.T, sb.T32, sb.bhi, sb.blo, sb.mu_rel,
+        sb.mean, sb.inv, sb.df, sb.dg, sb.inv32, sb.df32, sb.dg32);
+    launches += 1;
   } else {
     sb = sa;
   }
@@ -335,19 +356,26 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   }
 
   // ---- work plan ----
-  const int W = mixed ? mixed_band_width() : fp64_band_width();
-  const int slab = mixed ? mixed_slab_rows() : fp64_slab_rows();
-  const int nthreads = mixed ? mixed_threads() : fp64_threads();
-  const size_t smem = mixed ? mixed_smem_bytes() : 0;
-  if (mixed) {
-    CUDA_TRY(cudaFuncSetAttribute(join_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  // Kernel choice: FP64 form; mixed 1NN_INDEX (FP32 filter + verified
+  // candidates); mixed SUM_THRESH (FP32, every cell accumulated).
+  enum { K_FP64, K_MIXED_1NN, K_MIXED_SUM } kind =
+      !mixed ? K_FP64 : (is_1nn ? K_MIXED_1NN : K_MIXED_SUM);
+  const void* kfn = kind == K_FP64 ? reinterpret_cast<const void*>(join_fp64_kernel)
+                  : kind == K_MIXED_1NN ? reinterpret_cast<const void*>(join_mixed_1nn_kernel)
+                                        : reinterpret_cast<const void*>(join_mixed_kernel);
+  const int W = kind == K_FP64 ? fp64_band_width()
+              : kind == K_MIXED_1NN ? mixed_1nn_band_width() : mixed_band_width();
+  const int slab = kind == K_FP64 ? fp64_slab_rows()
+                 : kind == K_MIXED_1NN ? mixed_1nn_slab_rows() : mixed_slab_rows();
+  const int nthreads = kind == K_FP64 ? fp64_threads()
+                     : kind == K_MIXED_1NN ? mixed_1nn_threads() : mixed_threads();
+  const size_t smem = kind == K_FP64 ? 0
+                    : kind == K_MIXED_1NN ? mixed_1nn_smem_bytes() : mixed_smem_bytes();
+  if (smem > 0)
+    CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(smem)));
-  }
   int occ = 1;
-  if (mixed)
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, join_mixed_kernel, nthreads, smem));
-  else
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, join_fp64_kernel, nthreads, 0));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, nthreads, smem));
   occ = std::max(occ, 1);
   const int64_t resident = static_cast<int64_t>(ws.sms) * occ;
   // Segment length K: the anchor interval for the mixed form; for FP64 long
@@ -396,6 +424,12 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   P.profile_type = a->profile_type;
   P.threshold = a->distance_threshold;
   P.kl = kl;
+  {
+    // FP32 anchor: blocks of up to 2^bshift terms, then the block sums.
+    const double blk = static_cast<double>(1 << sa.bshift);
+    const double e = std::sqrt(std::min<double>(m, blk)) + std::sqrt(std::ceil(m / blk) + 1.0);
+    P.anchor_vcoef = static_cast<float>(e * e / 8.0);  // per 8-row step units
+  }
 
   if (!a->silent_mode) {
     std::printf("scamp_gb300: %s %s join, m=%lld, %s, %llu cells, %lld units of %d diagonals x 2x%lld rows\n",
@@ -418,7 +452,9 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     const int64_t grid = std::min<int64_t>(resident, P.total_units);
     CUDA_TRY(cudaEventRecord(ws.evk0, st));
     ws.timed_kernel = true;
-    if (mixed)
+    if (kind == K_MIXED_1NN)
+      join_mixed_1nn_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
+    else if (kind == K_MIXED_SUM)
       join_mixed_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
     else
       join_fp64_kernel<<<static_cast<unsigned>(grid), nthreads, 0, st>>>(P);

@@ -85,6 +85,17 @@ struct SeriesDev {
   const float* inv32;  // FP32 copies for the mixed form
   const float* df32;
   const float* dg32;
+  // FP32 copy of the series relative to local offsets: the samples of block
+  // b = t >> bshift are stored as (float)(T[t] - boff[b]), boff[b] being the
+  // block's first sample, kept as an unevaluated float sum bhi[b] + blo[b].
+  // mu_rel[w] = (float)(mean[w] - boff[w >> bshift]).  Every quantity stays
+  // within the local variation of the series, so FP32 keeps its precision
+  // even where the series' level wanders far from any global offset.
+  const float* T32;
+  const float* bhi;
+  const float* blo;
+  const float* mu_rel;
+  int bshift;
   int64_t n;
   int64_t ns;
 };
@@ -123,6 +134,7 @@ struct JoinParams {
   int profile_type;                 // 1 = 1NN_INDEX, 2 = SUM_THRESH
   double threshold;
   KeyLayout kl;
+  float anchor_vcoef;               // initial drift estimate of an anchor / cov^2
 };
 
 // Locates global band `g` and unit-within-band for unit index `u`.
@@ -153,15 +165,18 @@ __host__ __device__ __forceinline__ int64_t band_rows(int64_t n_r, int64_t n_c,
 // Kernels (launch wrappers live in engine.cu).
 // ---------------------------------------------------------------------------
 __global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
-                             int64_t m, int ultra, int chunk,
-                             double* __restrict__ T_clean,
+                             int64_t m, int ultra, int chunk, int bshift,
+                             double* __restrict__ T_clean, float* __restrict__ T32,
+                             float* __restrict__ bhi, float* __restrict__ blo,
+                             float* __restrict__ mu_rel,
                              double* __restrict__ mean, double* __restrict__ inv,
                              double* __restrict__ df, double* __restrict__ dg,
                              float* __restrict__ inv32, float* __restrict__ df32,
                              float* __restrict__ dg32);
 
 __global__ void join_fp64_kernel(JoinParams P);
-__global__ void join_mixed_kernel(JoinParams P);
+__global__ void join_mixed_kernel(JoinParams P);      // SUM_THRESH
+__global__ void join_mixed_1nn_kernel(JoinParams P);  // 1NN_INDEX
 
 __global__ void profile_to_keys_kernel(const uint64_t* __restrict__ in,
                                        uint64_t* __restrict__ keys, int64_t n,

@@ -1,0 +1,552 @@
+// join_mixed_1nn.cu -- mixed-precision 1NN_INDEX join: FP32 filter, verified
+// candidates.
+//
+// Work decomposition as in join_fp64.cu (persistent kernel over a device
+// queue of units = band of kBand diagonals x two row segments of seg_len
+// rows; every thread advances kDiags diagonals in both segments as packed
+// f32x2 pairs, .x = first segment, .y = second).
+//
+// Per cell the hot loop issues exactly the reference's arithmetic
+// (src/kernels_compute.h:425-435): two FMAs advance the covariance and two
+// multiplies form r = cov * invnorm_col * invnorm_row -- as f32x2 pair
+// instructions, so the FP32 pipe, not the issue slot, bounds the loop.  What
+// the reference does per cell on top of that -- compare, select, index
+// bookkeeping (src/kernels_compute.h:25-113) -- is reduced to one running
+// maximum of the whole 8x8x2 block per thread (3-input max.f32, two cells per
+// instruction).
+//
+// A block whose maximum could beat the smallest best-so-far among its rows
+// and columns -- less an error margin -- is recomputed on the slow path cell
+// by cell.  The margin bounds the FP32 drift of the recurrence since the
+// diagonal's last anchor: the kernel accumulates sum(cov^2) per diagonal and
+// uses margin = C * 2^-24 * sqrt(rows * sum) * invnorm_col * invnorm_row.
+// On the slow path a candidate cell whose margin exceeds kTrust is verified
+// with a direct dot product of its two windows (FP32 data centred by the
+// windows' FP64 means) and the diagonal is re-anchored there, so drift after
+// large excursions of the series (level shifts, gaps) never reaches the
+// profile.  Candidates with a small margin keep their FP32 value.
+#include <cstdint>
+
+#include "engine.cuh"
+
+namespace scamp_gb300 {
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kDiags = 8;
+constexpr int kBand = kThreads * kDiags;  // 1024 diagonals per unit
+constexpr int kRows = 8;                  // rows per step
+constexpr int kSlab = 128;                // rows staged per slab
+constexpr int kSteps = kSlab / kRows;
+constexpr int kCols = kSlab + kBand;      // staged columns per slab
+constexpr int kBlocks = kCols / 8;        // 8-column blocks
+constexpr int kPad = kCols + kBlocks;     // padded slot c + c/8
+constexpr int kAnchorChunk = 1024;
+constexpr float kEps = 5.9604645e-8f;     // 2^-24
+constexpr float kBoundC = 4.0f;
+constexpr float kTrust = 8e-6f;
+constexpr float kNoTarget = 3.0e38f;      // best of a side that is not computed
+
+typedef unsigned long long u64;
+
+__device__ __forceinline__ u64 f2u(float2 v) {
+  return (static_cast<u64>(__float_as_uint(v.y)) << 32) | __float_as_uint(v.x);
+}
+__device__ __forceinline__ float2 u2f(u64 v) {
+  return make_float2(__uint_as_float(static_cast<uint32_t>(v)),
+                     __uint_as_float(static_cast<uint32_t>(v >> 32)));
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  u64 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2u(a)), "l"(f2u(b)), "l"(f2u(c)));
+  return u2f(d);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+  u64 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2u(a)), "l"(f2u(b)));
+  return u2f(d);
+}
+__device__ __forceinline__ float max3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float qnan() { return __int_as_float(0x7FC00000); }
+
+// Correlation encoded by a profile key, rounded down (a filter threshold may
+// only be lower than the true best).  Integer pipe only.
+__device__ __forceinline__ float key_corr_floor(u64 key, const KeyLayout& kl) {
+  const u64 q = key >> kl.idx_bits;
+  if (q == 0) return -3.0f;                       // no match yet
+  const int p = 63 - __clzll(static_cast<long long>(q));  // leading bit
+  const int e = p - kl.frac_bits;                 // (r + 2) in [2^e, 2^(e+1))
+  const uint32_t mant = static_cast<uint32_t>((q << (63 - p)) >> 40) & 0x7FFFFFu;
+  const float v = __uint_as_float((static_cast<uint32_t>(e + 127) << 23) | mant);
+  return v - 2.0f;                                 // exact for v in [1, 4)
+}
+
+struct Smem {
+  union {
+    struct {
+      float4 c_fg[kPad];  // {df.x, df.y, dg.x, dg.y} per staged column pair
+      float2 c_iv[kPad];  // {inv.x, inv.y}
+    } s;
+    struct {
+      float xr[2][kAnchorChunk];
+      float px[2][kAnchorChunk + 1];  // exclusive prefix sums of xr
+      float wsum[2][kThreads / 32];
+    } a;
+  } u;
+  float2 c_best[kCols];
+  float2 c_blkmin[kBlocks];
+  float2 c_blkmax_iv[kBlocks];
+  float4 c_blkmax_fg[kBlocks];  // max |df|, |dg| per 8-column block
+  float4 r_fg[kSlab];
+  float2 r_iv[kSlab];
+  float2 r_best[kSlab];
+  float2 r_stepmin[kSteps];
+  float2 r_stepmax_iv[kSteps];
+  float4 r_stepmax_fg[kSteps];
+  Problem prob;  // the current unit's band problem
+  long long unit;
+  int prob_idx;
+  long long band, unit_in_band;
+};
+
+__device__ __forceinline__ int padc(int c) { return c + (c >> 3); }
+
+// Offset of block b relative to block b0, as the float sum of the two
+// blocks' hi/lo parts: exact while the two offsets are within a factor of two.
+__device__ __forceinline__ float block_delta(const SeriesDev& S, int64_t b, int64_t b0) {
+  return (S.bhi[b] - S.bhi[b0]) + (S.blo[b] - S.blo[b0]);
+}
+
+// Covariance of row window i and column window j in FP32 from the locally
+// offset copies:  sum_t (x_t - mu_i)(y_t - mu_j)
+//   = sum_t xc_t * yl_t + sum_blocks (boff_c[b] - mu_j) * sum_{t in b} xc_t,
+// with xc the centred row window and yl the column samples relative to their
+// block offsets.  Summed per block run (at most 2^bshift terms).
+__device__ __noinline__ float verify_cov(const SeriesDev& R, const SeriesDev& C,
+                                         int64_t i, int64_t j, int64_t m) {
+  const int sh = R.bshift;
+  const int64_t bi = i >> sh, bj = j >> sh;
+  const float mri = R.mu_rel[i], mcj = C.mu_rel[j];
+  float acc = 0.f;
+  int64_t t = 0;
+  while (t < m) {
+    const int64_t br = (i + t) >> sh, bc = (j + t) >> sh;
+    int64_t te = ((br + 1) << sh) - i;
+    const int64_t te2 = ((bc + 1) << sh) - j;
+    if (te2 < te) te = te2;
+    if (m < te) te = m;
+    const float xc = block_delta(R, br, bi) - mri;
+    const float yd = block_delta(C, bc, bj) - mcj;
+    float p0 = 0.f, p1 = 0.f, sx = 0.f;
+    int64_t u = t;
+    for (; u + 1 < te; u += 2) {
+      const float x0 = R.T32[i + u] + xc, x1 = R.T32[i + u + 1] + xc;
+      p0 = fmaf(x0, C.T32[j + u], p0);
+      p1 = fmaf(x1, C.T32[j + u + 1], p1);
+      sx += x0 + x1;
+    }
+    if (u < te) {
+      const float x0 = R.T32[i + u] + xc;
+      p0 = fmaf(x0, C.T32[j + u], p0);
+      sx += x0;
+    }
+    acc += fmaf(yd, sx, p0 + p1);
+    t = te;
+  }
+  return acc;
+}
+
+struct SlowCtx {
+  const Problem* pr;
+  int64_t rbase[2];
+  int64_t d_my;
+  int64_t m;
+  KeyLayout kl;
+};
+
+// Slow path of one step: the block is recomputed cell by cell from the
+// covariances at the start of the step; every cell that may improve its row
+// or column is published (verified first when its margin is large).
+__device__ __forceinline__ void slow_step(Smem& sm, const SlowCtx& cx, int s, int t,
+                                          float2 (&cov)[kDiags], float2 (&V)[kDiags],
+                                          float2 W) {
+  const int r0 = s * kRows;
+  const int cbase = 8 * (s + t);
+  // Rewind the covariances to the start of the step.
+#pragma unroll 1
+  for (int rr = kRows - 1; rr >= 0; --rr) {
+    const float4 rf = sm.r_fg[r0 + rr];
+    const float2 ndfr = make_float2(-rf.x, -rf.y), dgr = make_float2(rf.z, rf.w);
+#pragma unroll
+    for (int k = 0; k < kDiags; ++k) {
+      const float4 cf = sm.u.s.c_fg[padc(cbase + rr + k)];
+      cov[k] = fma2(make_float2(-cf.x, -cf.y), dgr, cov[k]);
+      cov[k] = fma2(ndfr, make_float2(cf.z, cf.w), cov[k]);
+    }
+  }
+  const Problem& pr = *cx.pr;
+#pragma unroll 1
+  for (int rr = 0; rr < kRows; ++rr) {
+    const float4 rf = sm.r_fg[r0 + rr];
+    const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
+    const float2 ivr = sm.r_iv[r0 + rr];
+#pragma unroll
+    for (int k = 0; k < kDiags; ++k) {
+      const int c = cbase + rr + k;
+      const float4 cf = sm.u.s.c_fg[padc(c)];
+      const float2 ivc = sm.u.s.c_iv[padc(c)];
+      float2 r = mul2(mul2(cov[k], ivc), ivr);
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        float rv = g ? r.y : r.x;
+        const float icv = g ? ivc.y : ivc.x;
+        const float irv = g ? ivr.y : ivr.x;
+        const float vk = g ? V[k].y + W.y : V[k].x + W.x;
+        float mk = kBoundC * kEps * sqrtf(kRows * vk) * icv * irv;
+        const float rb = g ? sm.r_best[r0 + rr].y : sm.r_best[r0 + rr].x;
+        const float cb = g ? sm.c_best[c].y : sm.c_best[c].x;
+        if (rv + mk > fminf(rb, cb)) {
+          const int64_t i = cx.rbase[g] + r0 + rr;
+          const int64_t j = i + cx.d_my + k;
+          if (mk > kTrust) {
+            const float ce = verify_cov(pr.R, pr.C, i, j, cx.m);
+            rv = ce * icv * irv;
+            if (g) { cov[k].y = ce; V[k].y = 0.f; } else { cov[k].x = ce; V[k].x = 0.f; }
+          }
+          if (rv > rb) {
+            atomicMax(reinterpret_cast<u64*>(pr.key_row + i),
+                      make_key(q_from_float_bits(__float_as_uint(rv), cx.kl.frac_bits), j, cx.kl));
+            if (g) sm.r_best[r0 + rr].y = rv; else sm.r_best[r0 + rr].x = rv;
+          }
+          if (rv > cb) {
+            atomicMax(reinterpret_cast<u64*>(pr.key_col + j),
+                      make_key(q_from_float_bits(__float_as_uint(rv), cx.kl.frac_bits), i, cx.kl));
+            if (g) sm.c_best[c].y = rv; else sm.c_best[c].x = rv;
+          }
+        }
+      }
+      cov[k] = fma2(make_float2(cf.x, cf.y), dgr, cov[k]);
+      cov[k] = fma2(dfr, make_float2(cf.z, cf.w), cov[k]);
+    }
+  }
+}
+
+}  // namespace
+
+size_t mixed_1nn_smem_bytes() { return sizeof(Smem); }
+
+__global__ void __launch_bounds__(kThreads, 3)
+join_mixed_1nn_kernel(JoinParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+  const int t = threadIdx.x;
+  const int64_t K = P.seg_len;
+  const int64_t m = P.m;
+
+  for (;;) {
+    if (t == 0) {
+      const long long uu = static_cast<long long>(atomicAdd(P.unit_counter, 1ull));
+      sm.unit = uu;
+      if (uu < P.total_units) {
+        int pi;
+        int64_t bb, ubb;
+        decode_unit(P, uu, &pi, &bb, &ubb);
+        sm.prob = P.prob[pi];
+        sm.band = bb;
+        sm.unit_in_band = ubb;
+      }
+    }
+    __syncthreads();
+    const int64_t u = sm.unit;
+    if (u >= P.total_units) break;
+    const Problem& pr = sm.prob;
+    const int64_t band = sm.band, ub = sm.unit_in_band;
+    const int64_t D0 = pr.d_lo + band * kBand;
+    const int64_t rows_b = band_rows(pr.R.ns, pr.C.ns, D0);
+    int64_t seg_row[2], seg_len[2];
+    seg_row[0] = ub * 2 * K;
+    seg_row[1] = seg_row[0] + K;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      const int64_t l = rows_b - seg_row[g];
+      seg_len[g] = l < 0 ? 0 : (l > K ? K : l);
+    }
+    const int64_t d_my = D0 + t * kDiags;
+
+    // ---------------- anchors ----------------
+    // anchor_k = sum_t xc_t * yl(j_k + t) + sum_blocks (boff_c[b] - mu_jk) * S_b
+    // (the decomposition of verify_cov), with the centred row window xc and
+    // its prefix sums staged in shared memory, the column samples read per
+    // thread from L1/L2 and the per-block corrections summed at the end.
+    float acc[2][kDiags];
+    const int sh = pr.C.bshift;
+#pragma unroll
+    for (int g = 0; g < 2; ++g)
+#pragma unroll
+      for (int k = 0; k < kDiags; ++k) acc[g][k] = 0.f;
+    for (int64_t t0 = 0; t0 < m; t0 += kAnchorChunk) {
+      const int chunk = static_cast<int>((m - t0) < kAnchorChunk ? (m - t0) : kAnchorChunk);
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int64_t i = seg_row[g];
+        const bool live = seg_len[g] > 0;
+        const int64_t bi = i >> sh;
+        const float mri = live ? pr.R.mu_rel[i] : 0.f;
+        // each thread stages a contiguous run of the chunk and its local sum
+        const int per = (chunk + kThreads - 1) / kThreads;
+        const int x0 = t * per, x1 = (x0 + per < chunk) ? x0 + per : chunk;
+        float run = 0.f;
+        for (int x = x0; x < x1; ++x) {
+          float v = 0.f;
+          if (live) {
+            const int64_t p = i + t0 + x;
+            v = pr.R.T32[p] + (block_delta(pr.R, p >> sh, bi) - mri);
+          }
+          sm.u.a.xr[g][x] = v;
+          sm.u.a.px[g][x] = run;  // exclusive prefix within the run
+          run += v;
+        }
+        // scan of the run totals across the CTA
+        float incl = run;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const float nb = __shfl_up_sync(0xffffffffu, incl, o);
+          if ((t & 31) >= o) incl += nb;
+        }
+        if ((t & 31) == 31) sm.u.a.wsum[g][t >> 5] = incl;
+        __syncthreads();
+        float carry = incl - run;
+        for (int w = 0; w < (t >> 5); ++w) carry += sm.u.a.wsum[g][w];
+        for (int x = x0; x < x1; ++x) sm.u.a.px[g][x] += carry;
+        if (x1 == chunk && x0 < x1) sm.u.a.px[g][chunk] = carry + run;
+        if (chunk <= x0 && t == (chunk - 1) / per + 1) sm.u.a.px[g][chunk] = carry;
+        __syncthreads();
+      }
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        if (seg_len[g] == 0) continue;
+        const float* __restrict__ xr = sm.u.a.xr[g];
+        const int64_t j0 = seg_row[g] + d_my + t0;  // column sample of (k = 0, x = 0)
+        const float* __restrict__ yl = pr.C.T32;
+        const int64_t ylim = pr.C.n;
+        for (int b0 = 0; b0 < chunk; b0 += 32) {
+          float part[kDiags];
+#pragma unroll
+          for (int k = 0; k < kDiags; ++k) part[k] = 0.f;
+          const int b1 = (b0 + 32 < chunk) ? b0 + 32 : chunk;
+          for (int x = b0; x < b1; ++x) {
+            const float xv = xr[x];
+#pragma unroll
+            for (int k = 0; k < kDiags; ++k) {
+              const int64_t p = j0 + x + k;
+              part[k] = fmaf(xv, p < ylim ? yl[p] : 0.f, part[k]);
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < kDiags; ++k) acc[g][k] += part[k];
+        }
+        // block corrections of this chunk
+        const float* __restrict__ px = sm.u.a.px[g];
+#pragma unroll
+        for (int k = 0; k < kDiags; ++k) {
+          const int64_t j = seg_row[g] + d_my + k;
+          if (j >= pr.C.ns) continue;
+          const int64_t bj = j >> sh;
+          const float mcj = pr.C.mu_rel[j];
+          int64_t x = 0;
+          while (x < chunk) {
+            const int64_t b = (j + t0 + x) >> sh;
+            int64_t xe = ((b + 1) << sh) - (j + t0);
+            if (xe > chunk) xe = chunk;
+            acc[g][k] = fmaf(block_delta(pr.C, b, bj) - mcj, px[xe] - px[x], acc[g][k]);
+            x = xe;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    float2 cov[kDiags], V[kDiags];
+#pragma unroll
+    for (int k = 0; k < kDiags; ++k) {
+      const int64_t d = d_my + k;
+      const bool valid = d < pr.d_hi && !(d >= pr.x_lo && d < pr.x_hi);
+      // An excluded diagonal carries NaN: every r on it is NaN and never wins.
+      cov[k] = valid ? make_float2(acc[0][k], acc[1][k]) : make_float2(qnan(), qnan());
+      // initial drift estimate: the anchor's own rounding
+      V[k] = make_float2(P.anchor_vcoef * cov[k].x * cov[k].x, P.anchor_vcoef * cov[k].y * cov[k].y);
+    }
+    float2 W = make_float2(0.f, 0.f);  // accumulated squared increment bounds
+
+    SlowCtx cx;
+    cx.pr = &pr;
+    cx.d_my = d_my;
+    cx.m = m;
+    cx.kl = P.kl;
+
+    // ---------------- slabs ----------------
+    const int64_t nslabs = (seg_len[0] + kSlab - 1) / kSlab;
+    for (int64_t q = 0; q < nslabs; ++q) {
+      int64_t rbase[2], rend[2], cbase_g[2];
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        rbase[g] = seg_row[g] + q * kSlab;
+        rend[g] = seg_row[g] + seg_len[g];
+        cbase_g[g] = rbase[g] + D0;
+        cx.rbase[g] = rbase[g];
+      }
+      // rows
+      for (int x = t; x < kSlab; x += kThreads) {
+        const int64_t i0 = rbase[0] + x, i1 = rbase[1] + x;
+        const bool ok0 = i0 < rend[0], ok1 = i1 < rend[1];
+        float4 f;
+        f.x = ok0 ? pr.R.df32[i0] : 0.f;
+        f.y = ok1 ? pr.R.df32[i1] : 0.f;
+        f.z = ok0 ? pr.R.dg32[i0] : 0.f;
+        f.w = ok1 ? pr.R.dg32[i1] : 0.f;
+        sm.r_fg[x] = f;
+        const float2 iv = make_float2(ok0 ? pr.R.inv32[i0] : qnan(), ok1 ? pr.R.inv32[i1] : qnan());
+        sm.r_iv[x] = iv;
+        // A window that cannot match (padding, NaN or flat) must not lower
+        // the filter threshold: its best is "unreachable".
+        float2 b;
+        b.x = (pr.key_row && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_row[i0], P.kl) : kNoTarget;
+        b.y = (pr.key_row && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_row[i1], P.kl) : kNoTarget;
+        sm.r_best[x] = b;
+      }
+      // columns
+      for (int x = t; x < kCols; x += kThreads) {
+        const int64_t j0 = cbase_g[0] + x, j1 = cbase_g[1] + x;
+        const bool ok0 = seg_len[0] > 0 && j0 < pr.C.ns;
+        const bool ok1 = seg_len[1] > 0 && j1 < pr.C.ns;
+        float4 f;
+        f.x = ok0 ? pr.C.df32[j0] : 0.f;
+        f.y = ok1 ? pr.C.df32[j1] : 0.f;
+        f.z = ok0 ? pr.C.dg32[j0] : 0.f;
+        f.w = ok1 ? pr.C.dg32[j1] : 0.f;
+        sm.u.s.c_fg[padc(x)] = f;
+        const float2 iv = make_float2(ok0 ? pr.C.inv32[j0] : qnan(), ok1 ? pr.C.inv32[j1] : qnan());
+        sm.u.s.c_iv[padc(x)] = iv;
+        float2 b;
+        b.x = (pr.key_col && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_col[j0], P.kl) : kNoTarget;
+        b.y = (pr.key_col && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_col[j1], P.kl) : kNoTarget;
+        sm.c_best[x] = b;
+      }
+      __syncthreads();
+      // Per 8-column block: minimum best and maximum inverse norm; per step:
+      // the same over its rows.
+      for (int b = t; b < kBlocks; b += kThreads) {
+        float2 mn = make_float2(kNoTarget, kNoTarget), mx = make_float2(0.f, 0.f);
+        float4 mf = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int x = 0; x < 8; ++x) {
+          const float2 cb = sm.c_best[8 * b + x];
+          const float2 iv = sm.u.s.c_iv[padc(8 * b + x)];
+          const float4 fg = sm.u.s.c_fg[padc(8 * b + x)];
+          mn.x = fminf(mn.x, cb.x); mn.y = fminf(mn.y, cb.y);
+          mx.x = fmaxf(mx.x, iv.x); mx.y = fmaxf(mx.y, iv.y);
+          mf.x = fmaxf(mf.x, fabsf(fg.x)); mf.y = fmaxf(mf.y, fabsf(fg.y));
+          mf.z = fmaxf(mf.z, fabsf(fg.z)); mf.w = fmaxf(mf.w, fabsf(fg.w));
+        }
+        sm.c_blkmin[b] = mn;
+        sm.c_blkmax_iv[b] = mx;
+        sm.c_blkmax_fg[b] = mf;
+      }
+      if (t < kSteps) {
+        float2 mn = make_float2(kNoTarget, kNoTarget), mx = make_float2(0.f, 0.f);
+        float4 mf = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int x = 0; x < kRows; ++x) {
+          const float2 rb = sm.r_best[t * kRows + x];
+          const float2 iv = sm.r_iv[t * kRows + x];
+          const float4 fg = sm.r_fg[t * kRows + x];
+          mn.x = fminf(mn.x, rb.x); mn.y = fminf(mn.y, rb.y);
+          mx.x = fmaxf(mx.x, iv.x); mx.y = fmaxf(mx.y, iv.y);
+          mf.x = fmaxf(mf.x, fabsf(fg.x)); mf.y = fmaxf(mf.y, fabsf(fg.y));
+          mf.z = fmaxf(mf.z, fabsf(fg.z)); mf.w = fmaxf(mf.w, fabsf(fg.w));
+        }
+        sm.r_stepmin[t] = mn;
+        sm.r_stepmax_iv[t] = mx;
+        sm.r_stepmax_fg[t] = mf;
+      }
+      __syncthreads();
+
+      // ---------------- steps ----------------
+#pragma unroll 1
+      for (int s = 0; s < kSteps; ++s) {
+        const int r0 = s * kRows;
+        const int base = 9 * (s + t);  // padded slot of staged column 8(s+t)
+        // filter threshold and margin
+        const float2 bm0 = sm.c_blkmin[s + t], bm1 = sm.c_blkmin[s + t + 1];
+        const float2 rsm = sm.r_stepmin[s];
+        const float2 ic0 = sm.c_blkmax_iv[s + t], ic1 = sm.c_blkmax_iv[s + t + 1];
+        const float2 irm = sm.r_stepmax_iv[s];
+#pragma unroll
+        for (int k = 0; k < kDiags; ++k) V[k] = fma2(cov[k], cov[k], V[k]);
+        {
+          // bound of |df_c dg_r| + |df_r dg_c| over the step's cells
+          const float4 cf0 = sm.c_blkmax_fg[s + t], cf1 = sm.c_blkmax_fg[s + t + 1];
+          const float4 rfm = sm.r_stepmax_fg[s];
+          const float2 cdf = make_float2(fmaxf(cf0.x, cf1.x), fmaxf(cf0.y, cf1.y));
+          const float2 cdg = make_float2(fmaxf(cf0.z, cf1.z), fmaxf(cf0.w, cf1.w));
+          const float2 inc = fma2(make_float2(rfm.x, rfm.y), cdg,
+                                  mul2(make_float2(rfm.z, rfm.w), cdf));
+          W = fma2(inc, inc, W);
+        }
+        float vx = max3(V[0].x, V[1].x, V[2].x), vy = max3(V[0].y, V[1].y, V[2].y);
+        vx = max3(vx, V[3].x, V[4].x); vy = max3(vy, V[3].y, V[4].y);
+        vx = max3(vx, V[5].x, V[6].x); vy = max3(vy, V[5].y, V[6].y);
+        vx = fmaxf(vx, V[7].x) + W.x; vy = fmaxf(vy, V[7].y) + W.y;
+        const float tx = fminf(fminf(bm0.x, bm1.x), rsm.x) -
+                         kBoundC * kEps * sqrtf(kRows * vx) * fmaxf(ic0.x, ic1.x) * irm.x;
+        const float ty = fminf(fminf(bm0.y, bm1.y), rsm.y) -
+                         kBoundC * kEps * sqrtf(kRows * vy) * fmaxf(ic0.y, ic1.y) * irm.y;
+
+        // fast path: recurrence + block maximum
+        float bx = -3.f, by = -3.f;
+        float4 cf[kDiags + kRows - 1];
+        float2 ci[kDiags + kRows - 1];
+#pragma unroll
+        for (int x = 0; x < kDiags; ++x) {
+          cf[x] = sm.u.s.c_fg[base + x + (x >> 3)];
+          ci[x] = sm.u.s.c_iv[base + x + (x >> 3)];
+        }
+#pragma unroll
+        for (int rr = 0; rr < kRows; ++rr) {
+          if (rr > 0) {
+            const int x = rr + kDiags - 1;
+            cf[x] = sm.u.s.c_fg[base + x + (x >> 3)];
+            ci[x] = sm.u.s.c_iv[base + x + (x >> 3)];
+          }
+          const float4 rf = sm.r_fg[r0 + rr];
+          const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
+          const float2 ivr = sm.r_iv[r0 + rr];
+#pragma unroll
+          for (int k = 0; k < kDiags; k += 2) {
+            const int x = rr + k;
+            const float2 ra = mul2(mul2(cov[k], ci[x]), ivr);
+            const float2 rb = mul2(mul2(cov[k + 1], ci[x + 1]), ivr);
+            bx = max3(bx, ra.x, rb.x);
+            by = max3(by, ra.y, rb.y);
+            cov[k] = fma2(make_float2(cf[x].x, cf[x].y), dgr, cov[k]);
+            cov[k] = fma2(dfr, make_float2(cf[x].z, cf[x].w), cov[k]);
+            cov[k + 1] = fma2(make_float2(cf[x + 1].x, cf[x + 1].y), dgr, cov[k + 1]);
+            cov[k + 1] = fma2(dfr, make_float2(cf[x + 1].z, cf[x + 1].w), cov[k + 1]);
+          }
+        }
+        if (bx > tx || by > ty) slow_step(sm, cx, s, t, cov, V, W);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+int mixed_1nn_band_width() { return kBand; }
+int mixed_1nn_slab_rows() { return kSlab; }
+int mixed_1nn_threads() { return kThreads; }
+
+}  // namespace scamp_gb300

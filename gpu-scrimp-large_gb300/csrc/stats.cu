@@ -40,8 +40,10 @@ __device__ __forceinline__ void acc2(double& s, double& c, double x) {
 }  // namespace
 
 __global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
-                             int64_t m, int ultra, int chunk,
-                             double* __restrict__ T_clean,
+                             int64_t m, int ultra, int chunk, int bshift,
+                             double* __restrict__ T_clean, float* __restrict__ T32,
+                             float* __restrict__ bhi, float* __restrict__ blo,
+                             float* __restrict__ mu_rel,
                              double* __restrict__ mean, double* __restrict__ inv,
                              double* __restrict__ df, double* __restrict__ dg,
                              float* __restrict__ inv32, float* __restrict__ df32,
@@ -53,9 +55,22 @@ __global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
   const int64_t w1 = (w0 + chunk < ns) ? w0 + chunk : ns;
 
   // Cleaned samples owned by this chunk (the last chunk also owns the tail).
+  // Block offsets are the blocks' first (cleaned) samples.
+  auto block_off = [&](int64_t b) { return clean(T_raw[b << bshift]); };
   {
     const int64_t s_end = (w1 == ns) ? n : w1;
-    for (int64_t t = w0; t < s_end; ++t) T_clean[t] = clean(T_raw[t]);
+    for (int64_t t = w0; t < s_end; ++t) {
+      const double c = clean(T_raw[t]);
+      T_clean[t] = c;
+      const int64_t b = t >> bshift;
+      const double o = block_off(b);
+      T32[t] = static_cast<float>(c - o);
+      if ((b << bshift) == t) {
+        const float hi = static_cast<float>(o);
+        bhi[b] = hi;
+        blo[b] = static_cast<float>(o - static_cast<double>(hi));
+      }
+    }
   }
 
   // Mean and NaN status of window w0, and the position of the last
@@ -131,6 +146,7 @@ __global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
       g = ((b - mu_next) - mu_next_lo) + ((a - mu) - mu_lo);
     }
     mean[w] = mu;
+    mu_rel[w] = static_cast<float>((mu - block_off(w >> bshift)) + mu_lo);
     inv[w] = iv;
     df[w] = f;
     dg[w] = g;

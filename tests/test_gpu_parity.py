@@ -150,7 +150,13 @@ def test_merge_into_best_so_far(gpu_engine, oracle_mod, precision, tol):
     gc, gi = gpu_engine.unpack_profile(got)
     assert np.all(gc[keep] == 1.0) and np.all(gi[keep] == 7)
     others = np.setdiff1d(np.arange(len(prior)), keep)
-    assert np.array_equal(got[others], base[others])
+    if precision == "double":
+        assert np.array_equal(got[others], base[others])
+    else:
+        # The mixed form's work depends on the starting thresholds (which
+        # candidates get verified), so untouched entries agree to tolerance.
+        bc, bi = gpu_engine.unpack_profile(base)
+        assert np.max(np.abs(gc[others].astype(np.float64) - bc[others])) <= tol
 
 
 @pytest.mark.parametrize("precision,tol", PRECISIONS)
