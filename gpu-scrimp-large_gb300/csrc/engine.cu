@@ -448,6 +448,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     CUDA_TRY(cudaMemsetAsync(p, 0, 64, st));
     P.band_unit_prefix = dprefix;
     P.unit_counter = static_cast<unsigned long long*>(p);
+    P.counters = static_cast<unsigned long long*>(p) + 1;
     P.error_flag = reinterpret_cast<int*>(static_cast<char*>(p) + 32);
     const int64_t grid = std::min<int64_t>(resident, P.total_units);
     CUDA_TRY(cudaEventRecord(ws.evk0, st));
@@ -483,6 +484,15 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
 }
 
 void read_times(Workspace& ws, scamp_c_result* res) {
+  res->steps = res->slow_steps = res->verifications = 0;
+  if (ws.timed_kernel && ws.bufs.size() > S_COUNTER && ws.bufs[S_COUNTER].p) {
+    unsigned long long c[4] = {0, 0, 0, 0};
+    if (cudaMemcpy(c, ws.bufs[S_COUNTER].p, sizeof(c), cudaMemcpyDeviceToHost) == cudaSuccess) {
+      res->steps = c[1];
+      res->slow_steps = c[2];
+      res->verifications = c[3];
+    }
+  }
   float ms = 0;
   cudaEventElapsedTime(&ms, ws.ev0, ws.ev1);
   res->elapsed_ms = ms;

@@ -127,6 +127,7 @@ struct JoinParams {
   int64_t total_bands;
   int64_t total_units;
   unsigned long long* unit_counter; // persistent work queue head
+  unsigned long long* counters;     // [steps, slow steps, verifications]
   int* error_flag;                  // device error word (0 = ok)
   int64_t m;                        // window length
   int64_t seg_len;                  // K: rows per segment (two per unit)

@@ -86,6 +86,18 @@ __device__ __forceinline__ float key_corr_floor(u64 key, const KeyLayout& kl) {
   return v - 2.0f;                                 // exact for v in [1, 4)
 }
 
+// A block queued for the exact path: the owner's covariances at the END of
+// the step (the drain rewinds them), its drift state and position.
+struct SlowItem {
+  float2 cov[kDiags];
+  float2 V[kDiags];
+  float2 W;
+  int s;      // step within the slab
+  int owner;  // thread index of the owner
+};
+
+constexpr int kQueue = 32;  // queued blocks per warp before a drain
+
 struct Smem {
   union {
     struct {
@@ -93,9 +105,7 @@ struct Smem {
       float2 c_iv[kPad];  // {inv.x, inv.y}
     } s;
     struct {
-      float xr[2][kAnchorChunk];
-      float px[2][kAnchorChunk + 1];  // exclusive prefix sums of xr
-      float wsum[2][kThreads / 32];
+      float xr[2][kAnchorChunk];  // centred row window (chunk)
     } a;
   } u;
   float2 c_best[kCols];
@@ -108,6 +118,7 @@ struct Smem {
   float2 r_stepmin[kSteps];
   float2 r_stepmax_iv[kSteps];
   float4 r_stepmax_fg[kSteps];
+  SlowItem queue[kThreads / 32][kQueue];
   Problem prob;  // the current unit's band problem
   long long unit;
   int prob_idx;
@@ -123,10 +134,10 @@ __device__ __forceinline__ float block_delta(const SeriesDev& S, int64_t b, int6
 }
 
 // Covariance of row window i and column window j in FP32 from the locally
-// offset copies:  sum_t (x_t - mu_i)(y_t - mu_j)
-//   = sum_t xc_t * yl_t + sum_blocks (boff_c[b] - mu_j) * sum_{t in b} xc_t,
-// with xc the centred row window and yl the column samples relative to their
-// block offsets.  Summed per block run (at most 2^bshift terms).
+// offset copies: sum_t (x_t - mu_i)(y_t - mu_j), each factor formed in FP32
+// as (sample relative to its block offset) + (block offset - window mean), so
+// both stay within the windows' own variation.  Summed per block run (at most
+// 2^bshift terms), then across runs.
 __device__ __noinline__ float verify_cov(const SeriesDev& R, const SeriesDev& C,
                                          int64_t i, int64_t j, int64_t m) {
   const int sh = R.bshift;
@@ -140,22 +151,17 @@ __device__ __noinline__ float verify_cov(const SeriesDev& R, const SeriesDev& C,
     const int64_t te2 = ((bc + 1) << sh) - j;
     if (te2 < te) te = te2;
     if (m < te) te = m;
+    // both windows centred by their own means, element by element
     const float xc = block_delta(R, br, bi) - mri;
-    const float yd = block_delta(C, bc, bj) - mcj;
-    float p0 = 0.f, p1 = 0.f, sx = 0.f;
+    const float yc = block_delta(C, bc, bj) - mcj;
+    float p0 = 0.f, p1 = 0.f;
     int64_t u = t;
     for (; u + 1 < te; u += 2) {
-      const float x0 = R.T32[i + u] + xc, x1 = R.T32[i + u + 1] + xc;
-      p0 = fmaf(x0, C.T32[j + u], p0);
-      p1 = fmaf(x1, C.T32[j + u + 1], p1);
-      sx += x0 + x1;
+      p0 = fmaf(R.T32[i + u] + xc, C.T32[j + u] + yc, p0);
+      p1 = fmaf(R.T32[i + u + 1] + xc, C.T32[j + u + 1] + yc, p1);
     }
-    if (u < te) {
-      const float x0 = R.T32[i + u] + xc;
-      p0 = fmaf(x0, C.T32[j + u], p0);
-      sx += x0;
-    }
-    acc += fmaf(yd, sx, p0 + p1);
+    if (u < te) p0 = fmaf(R.T32[i + u] + xc, C.T32[j + u] + yc, p0);
+    acc += p0 + p1;
     t = te;
   }
   return acc;
@@ -164,7 +170,7 @@ __device__ __noinline__ float verify_cov(const SeriesDev& R, const SeriesDev& C,
 struct SlowCtx {
   const Problem* pr;
   int64_t rbase[2];
-  int64_t d_my;
+  int64_t D0;  // first diagonal of the unit; thread t owns D0 + t*kDiags ..
   int64_t m;
   KeyLayout kl;
 };
@@ -172,9 +178,10 @@ struct SlowCtx {
 // Slow path of one step: the block is recomputed cell by cell from the
 // covariances at the start of the step; every cell that may improve its row
 // or column is published (verified first when its margin is large).
-__device__ __forceinline__ void slow_step(Smem& sm, const SlowCtx& cx, int s, int t,
-                                          float2 (&cov)[kDiags], float2 (&V)[kDiags],
-                                          float2 W) {
+__device__ __forceinline__ int slow_step(Smem& sm, const SlowCtx& cx, int s, int t,
+                                         float2 (&cov)[kDiags], const float2 (&V)[kDiags],
+                                         float2 W) {
+  int verified = 0;
   const int r0 = s * kRows;
   const int cbase = 8 * (s + t);
   // Rewind the covariances to the start of the step.
@@ -212,11 +219,10 @@ __device__ __forceinline__ void slow_step(Smem& sm, const SlowCtx& cx, int s, in
         const float cb = g ? sm.c_best[c].y : sm.c_best[c].x;
         if (rv + mk > fminf(rb, cb)) {
           const int64_t i = cx.rbase[g] + r0 + rr;
-          const int64_t j = i + cx.d_my + k;
+          const int64_t j = i + cx.D0 + t * kDiags + k;
           if (mk > kTrust) {
-            const float ce = verify_cov(pr.R, pr.C, i, j, cx.m);
-            rv = ce * icv * irv;
-            if (g) { cov[k].y = ce; V[k].y = 0.f; } else { cov[k].x = ce; V[k].x = 0.f; }
+            ++verified;
+            rv = verify_cov(pr.R, pr.C, i, j, cx.m) * icv * irv;
           }
           if (rv > rb) {
             atomicMax(reinterpret_cast<u64*>(pr.key_row + i),
@@ -234,6 +240,25 @@ __device__ __forceinline__ void slow_step(Smem& sm, const SlowCtx& cx, int s, in
       cov[k] = fma2(dfr, make_float2(cf.z, cf.w), cov[k]);
     }
   }
+  return verified;
+}
+
+// Exact path for the queued blocks of one warp: lane q takes item q.
+__device__ __noinline__ int drain_queue(Smem& sm, const SlowCtx& cx, int warp, int count,
+                                        int lane) {
+  int verified = 0;
+  if (lane < count) {
+    SlowItem& it = sm.queue[warp][lane];
+    float2 cov[kDiags], V[kDiags];
+#pragma unroll
+    for (int k = 0; k < kDiags; ++k) {
+      cov[k] = it.cov[k];
+      V[k] = it.V[k];
+    }
+    verified = slow_step(sm, cx, it.s, it.owner, cov, V, it.W);
+  }
+  __syncwarp();
+  return verified;
 }
 
 }  // namespace
@@ -247,6 +272,9 @@ join_mixed_1nn_kernel(JoinParams P) {
   const int t = threadIdx.x;
   const int64_t K = P.seg_len;
   const int64_t m = P.m;
+  unsigned long long n_steps = 0, n_slow = 0, n_verify = 0;
+  const int lane = t & 31, warp = t >> 5;
+  int qn = 0;  // queued blocks of this warp (warp-uniform)
 
   for (;;) {
     if (t == 0) {
@@ -279,11 +307,14 @@ join_mixed_1nn_kernel(JoinParams P) {
     const int64_t d_my = D0 + t * kDiags;
 
     // ---------------- anchors ----------------
-    // anchor_k = sum_t xc_t * yl(j_k + t) + sum_blocks (boff_c[b] - mu_jk) * S_b
-    // (the decomposition of verify_cov), with the centred row window xc and
-    // its prefix sums staged in shared memory, the column samples read per
-    // thread from L1/L2 and the per-block corrections summed at the end.
+    // With the thread's first column window j0 and
+    // Y(p) = T32c[p] + (boff_c[p >> bshift] - mu_j0) (the column samples
+    // centred by that window's mean, shared by the thread's 8 windows):
+    //   anchor_k = sum_t xc_t * Y(j_k + t) - (mu_jk - mu_j0) * sum_t xc_t
+    // where xc is the row window centred by its FP64 mean (staged in shared
+    // memory); every factor stays within the windows' own variation.
     float acc[2][kDiags];
+    float xsum[2] = {0.f, 0.f};
     const int sh = pr.C.bshift;
 #pragma unroll
     for (int g = 0; g < 2; ++g)
@@ -297,78 +328,81 @@ join_mixed_1nn_kernel(JoinParams P) {
         const bool live = seg_len[g] > 0;
         const int64_t bi = i >> sh;
         const float mri = live ? pr.R.mu_rel[i] : 0.f;
-        // each thread stages a contiguous run of the chunk and its local sum
-        const int per = (chunk + kThreads - 1) / kThreads;
-        const int x0 = t * per, x1 = (x0 + per < chunk) ? x0 + per : chunk;
-        float run = 0.f;
-        for (int x = x0; x < x1; ++x) {
+        for (int x = t; x < chunk; x += kThreads) {
           float v = 0.f;
           if (live) {
             const int64_t p = i + t0 + x;
             v = pr.R.T32[p] + (block_delta(pr.R, p >> sh, bi) - mri);
           }
           sm.u.a.xr[g][x] = v;
-          sm.u.a.px[g][x] = run;  // exclusive prefix within the run
-          run += v;
         }
-        // scan of the run totals across the CTA
-        float incl = run;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const float nb = __shfl_up_sync(0xffffffffu, incl, o);
-          if ((t & 31) >= o) incl += nb;
-        }
-        if ((t & 31) == 31) sm.u.a.wsum[g][t >> 5] = incl;
-        __syncthreads();
-        float carry = incl - run;
-        for (int w = 0; w < (t >> 5); ++w) carry += sm.u.a.wsum[g][w];
-        for (int x = x0; x < x1; ++x) sm.u.a.px[g][x] += carry;
-        if (x1 == chunk && x0 < x1) sm.u.a.px[g][chunk] = carry + run;
-        if (chunk <= x0 && t == (chunk - 1) / per + 1) sm.u.a.px[g][chunk] = carry;
-        __syncthreads();
       }
+      __syncthreads();
 #pragma unroll
       for (int g = 0; g < 2; ++g) {
         if (seg_len[g] == 0) continue;
         const float* __restrict__ xr = sm.u.a.xr[g];
-        const int64_t j0 = seg_row[g] + d_my + t0;  // column sample of (k = 0, x = 0)
-        const float* __restrict__ yl = pr.C.T32;
-        const int64_t ylim = pr.C.n;
-        for (int b0 = 0; b0 < chunk; b0 += 32) {
+        const int64_t jb = seg_row[g] + d_my;      // the thread's first column window
+        const int64_t jc = jb < pr.C.ns ? jb : pr.C.ns - 1;
+        const int64_t b0 = jc >> sh;
+        const float mu0 = pr.C.mu_rel[jc];         // mu_j0 - boff_c[b0]
+        const int64_t plim = pr.C.n;
+        int64_t cur_b = -1;                        // block of the cached corrections
+        float dlo = 0.f, dhi = 0.f;
+        for (int c0 = 0; c0 < chunk; c0 += 32) {
           float part[kDiags];
 #pragma unroll
           for (int k = 0; k < kDiags; ++k) part[k] = 0.f;
-          const int b1 = (b0 + 32 < chunk) ? b0 + 32 : chunk;
-          for (int x = b0; x < b1; ++x) {
-            const float xv = xr[x];
+          float xs = 0.f;
+          const int c1 = (c0 + 32 < chunk) ? c0 + 32 : chunk;
+          // groups of 8 row samples: 16 column samples cover the 8 windows;
+          // 16 consecutive samples touch at most two blocks (blocks hold >= 32)
+          for (int xg = c0; xg < c1; xg += 8) {
+            const int64_t pg = jb + t0 + xg;
+            const int64_t bf = pg >> sh;
+            if (bf != cur_b) {
+              cur_b = bf;
+              dlo = (pg < plim) ? block_delta(pr.C, bf, b0) - mu0 : 0.f;
+              dhi = (((bf + 1) << sh) < plim) ? block_delta(pr.C, bf + 1, b0) - mu0 : 0.f;
+            }
+            const int64_t pbound = (bf + 1) << sh;  // first sample of the next block
+            float y[16];
 #pragma unroll
-            for (int k = 0; k < kDiags; ++k) {
-              const int64_t p = j0 + x + k;
-              part[k] = fmaf(xv, p < ylim ? yl[p] : 0.f, part[k]);
+            for (int q = 0; q < 16; ++q) {
+              const int64_t p = jb + t0 + xg + q;
+              y[q] = p < plim ? pr.C.T32[p] + (p < pbound ? dlo : dhi) : 0.f;
+            }
+#pragma unroll
+            for (int v = 0; v < 8; ++v) {
+              if (xg + v < c1) {
+                const float xv = xr[xg + v];
+                xs += xv;
+#pragma unroll
+                for (int k = 0; k < kDiags; ++k) part[k] = fmaf(xv, y[v + k], part[k]);
+              }
             }
           }
 #pragma unroll
           for (int k = 0; k < kDiags; ++k) acc[g][k] += part[k];
-        }
-        // block corrections of this chunk
-        const float* __restrict__ px = sm.u.a.px[g];
-#pragma unroll
-        for (int k = 0; k < kDiags; ++k) {
-          const int64_t j = seg_row[g] + d_my + k;
-          if (j >= pr.C.ns) continue;
-          const int64_t bj = j >> sh;
-          const float mcj = pr.C.mu_rel[j];
-          int64_t x = 0;
-          while (x < chunk) {
-            const int64_t b = (j + t0 + x) >> sh;
-            int64_t xe = ((b + 1) << sh) - (j + t0);
-            if (xe > chunk) xe = chunk;
-            acc[g][k] = fmaf(block_delta(pr.C, b, bj) - mcj, px[xe] - px[x], acc[g][k]);
-            x = xe;
-          }
+          xsum[g] += xs;
         }
       }
       __syncthreads();
+    }
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      if (seg_len[g] == 0) continue;
+      const int64_t jb = seg_row[g] + d_my;
+      const int64_t jc = jb < pr.C.ns ? jb : pr.C.ns - 1;
+      const int64_t b0 = jc >> sh;
+      const float mu0 = pr.C.mu_rel[jc];
+#pragma unroll
+      for (int k = 0; k < kDiags; ++k) {
+        const int64_t j = jb + k;
+        if (j >= pr.C.ns) continue;
+        const float ek = (pr.C.mu_rel[j] + block_delta(pr.C, j >> sh, b0)) - mu0;
+        acc[g][k] = fmaf(-ek, xsum[g], acc[g][k]);
+      }
     }
     float2 cov[kDiags], V[kDiags];
 #pragma unroll
@@ -384,7 +418,7 @@ join_mixed_1nn_kernel(JoinParams P) {
 
     SlowCtx cx;
     cx.pr = &pr;
-    cx.d_my = d_my;
+    cx.D0 = D0;
     cx.m = m;
     cx.kl = P.kl;
 
@@ -538,10 +572,48 @@ join_mixed_1nn_kernel(JoinParams P) {
             cov[k + 1] = fma2(dfr, make_float2(cf[x + 1].z, cf[x + 1].w), cov[k + 1]);
           }
         }
-        if (bx > tx || by > ty) slow_step(sm, cx, s, t, cov, V, W);
+        ++n_steps;
+        const bool trig = bx > tx || by > ty;
+        const unsigned tmask = __ballot_sync(0xffffffffu, trig);
+        if (tmask) {
+          const int nt = __popc(tmask);
+          if (qn + nt > kQueue) {
+            n_verify += drain_queue(sm, cx, warp, qn, lane);
+            qn = 0;
+          }
+          if (trig) {
+            SlowItem& it = sm.queue[warp][qn + __popc(tmask & ((1u << lane) - 1u))];
+#pragma unroll
+            for (int k = 0; k < kDiags; ++k) {
+              it.cov[k] = cov[k];
+              it.V[k] = V[k];
+            }
+            it.W = W;
+            it.s = s;
+            it.owner = t;
+          }
+          qn += nt;
+          n_slow += trig ? 1 : 0;
+        }
+      }
+      if (qn) {
+        n_verify += drain_queue(sm, cx, warp, qn, lane);
+        qn = 0;
       }
       __syncthreads();
     }
+  }
+  // per-CTA totals of the work counters
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    n_steps += __shfl_xor_sync(0xffffffffu, n_steps, o);
+    n_slow += __shfl_xor_sync(0xffffffffu, n_slow, o);
+    n_verify += __shfl_xor_sync(0xffffffffu, n_verify, o);
+  }
+  if ((t & 31) == 0 && P.counters) {
+    atomicAdd(P.counters + 0, n_steps);
+    atomicAdd(P.counters + 1, n_slow);
+    atomicAdd(P.counters + 2, n_verify);
   }
 }
 

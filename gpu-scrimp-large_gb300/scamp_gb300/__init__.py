@@ -178,6 +178,8 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
     out["join_kernel_ms"] = res.join_kernel_ms
     out["comparisons"] = int(res.comparisons)
     out["gpu_launches"] = int(res.gpu_launches)
+    out["counters"] = {"steps": int(res.steps), "slow_steps": int(res.slow_steps),
+                       "verifications": int(res.verifications)}
     return out
 
 
@@ -208,6 +210,8 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
                                   ctypes.c_void_p(stream), err, 1024)
     _check(rc, err)
     return {"elapsed_ms": res.elapsed_ms, "join_kernel_ms": res.join_kernel_ms,
+            "counters": {"steps": int(res.steps), "slow_steps": int(res.slow_steps),
+                         "verifications": int(res.verifications)},
             "comparisons": int(res.comparisons),
             "gpu_launches": int(res.gpu_launches)}
 

@@ -82,7 +82,11 @@ class CResult(ctypes.Structure):
         ("join_kernel_ms", ctypes.c_double),
         ("comparisons", ctypes.c_uint64),
         ("gpu_launches", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32 * 5),
+        ("reserved0", ctypes.c_uint32),
+        ("steps", ctypes.c_uint64),
+        ("slow_steps", ctypes.c_uint64),
+        ("verifications", ctypes.c_uint64),
+        ("reserved", ctypes.c_uint32 * 2),
     ]
 
 

@@ -94,7 +94,14 @@ typedef struct scamp_c_result {
   double join_kernel_ms;/* device time of the join kernel alone */
   uint64_t comparisons; /* distance-matrix cells evaluated */
   uint32_t gpu_launches;/* kernels launched by this call */
-  uint32_t reserved[5];
+  uint32_t reserved0;
+  /* Work counters of the mixed 1NN_INDEX form (0 otherwise): 8-row steps
+   * of one thread, steps recomputed on the exact path, and candidate cells
+   * verified by a direct dot product. */
+  uint64_t steps;
+  uint64_t slow_steps;
+  uint64_t verifications;
+  uint32_t reserved[2];
 } scamp_c_result;
 
 /* Runs one join.  Inputs and results are HOST memory; the engine copies them
