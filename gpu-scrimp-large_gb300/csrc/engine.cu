@@ -40,7 +40,7 @@ int measure_pipe_peak(int device, int kind, double* ops_per_s);
 
 namespace {
 
-constexpr int kDefaultAnchorInterval = 1024;
+constexpr int kDefaultAnchorInterval = 512;
 
 struct Error {
   int code;

@@ -16,15 +16,19 @@
 // instruction).
 //
 // A block whose maximum could beat the smallest best-so-far among its rows
-// and columns -- less an error margin -- is recomputed on the slow path cell
-// by cell.  The margin bounds the FP32 drift of the recurrence since the
-// diagonal's last anchor: the kernel accumulates sum(cov^2) per diagonal and
-// uses margin = C * 2^-24 * sqrt(rows * sum) * invnorm_col * invnorm_row.
-// On the slow path a candidate cell whose margin exceeds kTrust is verified
-// with a direct dot product of its two windows (FP32 data centred by the
-// windows' FP64 means) and the diagonal is re-anchored there, so drift after
-// large excursions of the series (level shifts, gaps) never reaches the
-// profile.  Candidates with a small margin keep their FP32 value.
+// and columns, less an error margin, is queued for the exact path.  The
+// margin bounds the FP32 drift since the diagonal's anchor: per diagonal the
+// kernel accumulates cov^2 and per thread the squared bound of the
+// increments |df_c dg_r| + |df_r dg_c|, and uses
+//   margin = C * 2^-24 * sqrt(rows * (sum cov^2 + sum inc^2)) * inv_c * inv_r.
+// Each warp drains its queue cooperatively (one queued block per lane):
+// cells that may improve their row or column are published with their FP32
+// value when the margin is below kTrust, otherwise verified first by a
+// direct dot product of the two windows computed by the whole warp.
+//
+// Anchors and verifications read an FP32 copy of each series stored relative
+// to local block offsets (stats.cu), with every factor centred by its
+// window's mean, so FP32 keeps its precision wherever the series wanders.
 #include <cstdint>
 
 #include "engine.cuh"
@@ -34,6 +38,7 @@ namespace scamp_gb300 {
 namespace {
 
 constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
 constexpr int kDiags = 8;
 constexpr int kBand = kThreads * kDiags;  // 1024 diagonals per unit
 constexpr int kRows = 8;                  // rows per step
@@ -42,7 +47,11 @@ constexpr int kSteps = kSlab / kRows;
 constexpr int kCols = kSlab + kBand;      // staged columns per slab
 constexpr int kBlocks = kCols / 8;        // 8-column blocks
 constexpr int kPad = kCols + kBlocks;     // padded slot c + c/8
-constexpr int kAnchorChunk = 1024;
+constexpr int kAnchorChunk = 512;         // row-window samples per anchor pass
+constexpr int kYSpan = kBand + kAnchorChunk + 16;     // staged column samples
+constexpr int kYPad = (kYSpan / 8) * 12;              // padded: 12 slots per 8
+constexpr int kQueue = 32;                // queued blocks per warp (>= lanes)
+constexpr int kVerify = 64;               // verification requests per warp
 constexpr float kEps = 5.9604645e-8f;     // 2^-24
 constexpr float kBoundC = 4.0f;
 constexpr float kTrust = 8e-6f;
@@ -78,25 +87,33 @@ __device__ __forceinline__ float qnan() { return __int_as_float(0x7FC00000); }
 // only be lower than the true best).  Integer pipe only.
 __device__ __forceinline__ float key_corr_floor(u64 key, const KeyLayout& kl) {
   const u64 q = key >> kl.idx_bits;
-  if (q == 0) return -3.0f;                       // no match yet
-  const int p = 63 - __clzll(static_cast<long long>(q));  // leading bit
-  const int e = p - kl.frac_bits;                 // (r + 2) in [2^e, 2^(e+1))
+  if (q == 0) return -3.0f;                                 // no match yet
+  const int p = 63 - __clzll(static_cast<long long>(q));    // leading bit
+  const int e = p - kl.frac_bits;                           // (r + 2) in [2^e, 2^(e+1))
   const uint32_t mant = static_cast<uint32_t>((q << (63 - p)) >> 40) & 0x7FFFFFu;
   const float v = __uint_as_float((static_cast<uint32_t>(e + 127) << 23) | mant);
-  return v - 2.0f;                                 // exact for v in [1, 4)
+  return v - 2.0f;                                          // exact for v in [1, 4)
 }
 
 // A block queued for the exact path: the owner's covariances at the END of
-// the step (the drain rewinds them), its drift state and position.
+// the step (the drain rewinds them), the step's drift estimate (largest
+// sum cov^2 over the owner's diagonals plus the increment bound) and the
+// block's position.
 struct SlowItem {
   float2 cov[kDiags];
-  float2 V[kDiags];
-  float2 W;
+  float2 vw;
   int s;      // step within the slab
   int owner;  // thread index of the owner
 };
 
-constexpr int kQueue = 32;  // queued blocks per warp before a drain
+// A cell whose FP32 value is not trusted: verified by its warp.
+struct VerifyReq {
+  long long i, j;   // row and column window
+  float f;          // inv_c * inv_r
+  short rslot;      // staged row of the cell
+  short cslot;      // staged column of the cell
+  int g;            // segment (0 = .x, 1 = .y)
+};
 
 struct Smem {
   union {
@@ -106,6 +123,7 @@ struct Smem {
     } s;
     struct {
       float xr[2][kAnchorChunk];  // centred row window (chunk)
+      float yc[2][kYPad];         // column samples (block-relative), padded
     } a;
   } u;
   float2 c_best[kCols];
@@ -118,14 +136,15 @@ struct Smem {
   float2 r_stepmin[kSteps];
   float2 r_stepmax_iv[kSteps];
   float4 r_stepmax_fg[kSteps];
-  SlowItem queue[kThreads / 32][kQueue];
+  SlowItem queue[kWarps][kQueue];
+  VerifyReq vreq[kWarps][kVerify];
+  int vcount[kWarps];
   Problem prob;  // the current unit's band problem
-  long long unit;
-  int prob_idx;
-  long long band, unit_in_band;
+  long long unit, band, unit_in_band;
 };
 
 __device__ __forceinline__ int padc(int c) { return c + (c >> 3); }
+__device__ __forceinline__ int pady(int x) { return x + (x >> 3) * 4; }
 
 // Offset of block b relative to block b0, as the float sum of the two
 // blocks' hi/lo parts: exact while the two offsets are within a factor of two.
@@ -133,13 +152,11 @@ __device__ __forceinline__ float block_delta(const SeriesDev& S, int64_t b, int6
   return (S.bhi[b] - S.bhi[b0]) + (S.blo[b] - S.blo[b0]);
 }
 
-// Covariance of row window i and column window j in FP32 from the locally
-// offset copies: sum_t (x_t - mu_i)(y_t - mu_j), each factor formed in FP32
-// as (sample relative to its block offset) + (block offset - window mean), so
-// both stay within the windows' own variation.  Summed per block run (at most
-// 2^bshift terms), then across runs.
-__device__ __noinline__ float verify_cov(const SeriesDev& R, const SeriesDev& C,
-                                         int64_t i, int64_t j, int64_t m) {
+// Covariance of row window i and column window j, FP32, one lane: each
+// factor formed as (sample relative to its block offset) + (block offset -
+// window mean), summed per block run.  Fallback of the warp-wide form.
+__device__ __noinline__ float verify_cov_lane(const SeriesDev& R, const SeriesDev& C,
+                                              int64_t i, int64_t j, int64_t m) {
   const int sh = R.bshift;
   const int64_t bi = i >> sh, bj = j >> sh;
   const float mri = R.mu_rel[i], mcj = C.mu_rel[j];
@@ -151,7 +168,6 @@ __device__ __noinline__ float verify_cov(const SeriesDev& R, const SeriesDev& C,
     const int64_t te2 = ((bc + 1) << sh) - j;
     if (te2 < te) te = te2;
     if (m < te) te = m;
-    // both windows centred by their own means, element by element
     const float xc = block_delta(R, br, bi) - mri;
     const float yc = block_delta(C, bc, bj) - mcj;
     float p0 = 0.f, p1 = 0.f;
@@ -167,6 +183,33 @@ __device__ __noinline__ float verify_cov(const SeriesDev& R, const SeriesDev& C,
   return acc;
 }
 
+// The same covariance computed by a whole warp: lane l sums the terms
+// t = l, l + 32, ...; the partial sums meet in a shuffle reduction.
+__device__ __forceinline__ float verify_cov_warp(const SeriesDev& R, const SeriesDev& C,
+                                                 int64_t i, int64_t j, int64_t m, int lane) {
+  const int sh = R.bshift;
+  const int64_t bi = i >> sh, bj = j >> sh;
+  const float mri = R.mu_rel[i], mcj = C.mu_rel[j];
+  const float hr0 = R.bhi[bi], lr0 = R.blo[bi], hc0 = C.bhi[bj], lc0 = C.blo[bj];
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int64_t t0 = lane; t0 < m; t0 += 128) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t t = t0 + 32 * u;
+      if (t < m) {
+        const int64_t br = (i + t) >> sh, bc = (j + t) >> sh;
+        const float x = R.T32[i + t] + (((R.bhi[br] - hr0) + (R.blo[br] - lr0)) - mri);
+        const float y = C.T32[j + t] + (((C.bhi[bc] - hc0) + (C.blo[bc] - lc0)) - mcj);
+        acc[u] = fmaf(x, y, acc[u]);
+      }
+    }
+  }
+  float a = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  return a;
+}
+
 struct SlowCtx {
   const Problem* pr;
   int64_t rbase[2];
@@ -175,90 +218,103 @@ struct SlowCtx {
   KeyLayout kl;
 };
 
-// Slow path of one step: the block is recomputed cell by cell from the
-// covariances at the start of the step; every cell that may improve its row
-// or column is published (verified first when its margin is large).
-__device__ __forceinline__ int slow_step(Smem& sm, const SlowCtx& cx, int s, int t,
-                                         float2 (&cov)[kDiags], const float2 (&V)[kDiags],
-                                         float2 W) {
-  int verified = 0;
-  const int r0 = s * kRows;
-  const int cbase = 8 * (s + t);
-  // Rewind the covariances to the start of the step.
-#pragma unroll 1
-  for (int rr = kRows - 1; rr >= 0; --rr) {
-    const float4 rf = sm.r_fg[r0 + rr];
-    const float2 ndfr = make_float2(-rf.x, -rf.y), dgr = make_float2(rf.z, rf.w);
-#pragma unroll
-    for (int k = 0; k < kDiags; ++k) {
-      const float4 cf = sm.u.s.c_fg[padc(cbase + rr + k)];
-      cov[k] = fma2(make_float2(-cf.x, -cf.y), dgr, cov[k]);
-      cov[k] = fma2(ndfr, make_float2(cf.z, cf.w), cov[k]);
-    }
-  }
+__device__ __forceinline__ void publish(Smem& sm, const SlowCtx& cx, float rv, int64_t i,
+                                        int64_t j, int rslot, int cslot, int g) {
   const Problem& pr = *cx.pr;
-#pragma unroll 1
-  for (int rr = 0; rr < kRows; ++rr) {
-    const float4 rf = sm.r_fg[r0 + rr];
-    const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
-    const float2 ivr = sm.r_iv[r0 + rr];
-#pragma unroll
-    for (int k = 0; k < kDiags; ++k) {
-      const int c = cbase + rr + k;
-      const float4 cf = sm.u.s.c_fg[padc(c)];
-      const float2 ivc = sm.u.s.c_iv[padc(c)];
-      float2 r = mul2(mul2(cov[k], ivc), ivr);
-#pragma unroll
-      for (int g = 0; g < 2; ++g) {
-        float rv = g ? r.y : r.x;
-        const float icv = g ? ivc.y : ivc.x;
-        const float irv = g ? ivr.y : ivr.x;
-        const float vk = g ? V[k].y + W.y : V[k].x + W.x;
-        float mk = kBoundC * kEps * sqrtf(kRows * vk) * icv * irv;
-        const float rb = g ? sm.r_best[r0 + rr].y : sm.r_best[r0 + rr].x;
-        const float cb = g ? sm.c_best[c].y : sm.c_best[c].x;
-        if (rv + mk > fminf(rb, cb)) {
-          const int64_t i = cx.rbase[g] + r0 + rr;
-          const int64_t j = i + cx.D0 + t * kDiags + k;
-          if (mk > kTrust) {
-            ++verified;
-            rv = verify_cov(pr.R, pr.C, i, j, cx.m) * icv * irv;
-          }
-          if (rv > rb) {
-            atomicMax(reinterpret_cast<u64*>(pr.key_row + i),
-                      make_key(q_from_float_bits(__float_as_uint(rv), cx.kl.frac_bits), j, cx.kl));
-            if (g) sm.r_best[r0 + rr].y = rv; else sm.r_best[r0 + rr].x = rv;
-          }
-          if (rv > cb) {
-            atomicMax(reinterpret_cast<u64*>(pr.key_col + j),
-                      make_key(q_from_float_bits(__float_as_uint(rv), cx.kl.frac_bits), i, cx.kl));
-            if (g) sm.c_best[c].y = rv; else sm.c_best[c].x = rv;
-          }
-        }
-      }
-      cov[k] = fma2(make_float2(cf.x, cf.y), dgr, cov[k]);
-      cov[k] = fma2(dfr, make_float2(cf.z, cf.w), cov[k]);
-    }
+  const float rb = g ? sm.r_best[rslot].y : sm.r_best[rslot].x;
+  const float cb = g ? sm.c_best[cslot].y : sm.c_best[cslot].x;
+  if (rv > rb) {
+    atomicMax(reinterpret_cast<u64*>(pr.key_row + i),
+              make_key(q_from_float_bits(__float_as_uint(rv), cx.kl.frac_bits), j, cx.kl));
+    // The float copies only filter candidates; a racing store of a smaller
+    // value costs extra work later, never a wrong result.
+    if (g) sm.r_best[rslot].y = rv; else sm.r_best[rslot].x = rv;
   }
-  return verified;
+  if (rv > cb) {
+    atomicMax(reinterpret_cast<u64*>(pr.key_col + j),
+              make_key(q_from_float_bits(__float_as_uint(rv), cx.kl.frac_bits), i, cx.kl));
+    if (g) sm.c_best[cslot].y = rv; else sm.c_best[cslot].x = rv;
+  }
 }
 
-// Exact path for the queued blocks of one warp: lane q takes item q.
+// Exact path of queued blocks, 16 lanes per block: lane (k, g) rewinds the
+// covariance of diagonal k, segment g to the start of the step, then walks
+// the step's 8 rows; every cell that may improve its row or column is
+// published with its FP32 value, or queued for verification when its margin
+// exceeds kTrust.  Two blocks per pass; then the warp verifies the queued
+// cells together.  Returns the number of verifications.
 __device__ __noinline__ int drain_queue(Smem& sm, const SlowCtx& cx, int warp, int count,
                                         int lane) {
-  int verified = 0;
-  if (lane < count) {
-    SlowItem& it = sm.queue[warp][lane];
-    float2 cov[kDiags], V[kDiags];
+  if (lane == 0) sm.vcount[warp] = 0;
+  __syncwarp();
+  const Problem& pr = *cx.pr;
+  const int k = (lane & 15) >> 1, g = lane & 1;
+  for (int p = 0; p < count; p += 2) {
+    const int item = p + (lane >> 4);
+    if (item < count) {
+      const SlowItem& it = sm.queue[warp][item];
+      float c = g ? it.cov[k].y : it.cov[k].x;
+      const float vw = g ? it.vw.y : it.vw.x;
+      const int r0 = it.s * kRows;
+      const int cb0 = 8 * (it.s + it.owner) + k;  // staged column at row 0
 #pragma unroll
-    for (int k = 0; k < kDiags; ++k) {
-      cov[k] = it.cov[k];
-      V[k] = it.V[k];
+      for (int rr = kRows - 1; rr >= 0; --rr) {
+        const float4 rf = sm.r_fg[r0 + rr];
+        const float4 cf = sm.u.s.c_fg[padc(cb0 + rr)];
+        const float dfr = g ? rf.y : rf.x, dgr = g ? rf.w : rf.z;
+        const float dfc = g ? cf.y : cf.x, dgc = g ? cf.w : cf.z;
+        c = fmaf(-dfr, dgc, c);
+        c = fmaf(-dfc, dgr, c);
+      }
+      const float vk = kBoundC * kEps * sqrtf(kRows * vw);
+#pragma unroll 1
+      for (int rr = 0; rr < kRows; ++rr) {
+        const int cs = cb0 + rr;
+        const float4 rf = sm.r_fg[r0 + rr];
+        const float4 cf = sm.u.s.c_fg[padc(cs)];
+        const float2 ivr2 = sm.r_iv[r0 + rr];
+        const float2 ivc2 = sm.u.s.c_iv[padc(cs)];
+        const float ivr = g ? ivr2.y : ivr2.x, ivc = g ? ivc2.y : ivc2.x;
+        const float rv = (c * ivc) * ivr;  // the fast path's rounding
+        const float mk = vk * ivc * ivr;
+        const float rb = g ? sm.r_best[r0 + rr].y : sm.r_best[r0 + rr].x;
+        const float cbv = g ? sm.c_best[cs].y : sm.c_best[cs].x;
+        if (rv + mk > fminf(rb, cbv)) {
+          const int64_t i = cx.rbase[g] + r0 + rr;
+          const int64_t j = i + cx.D0 + it.owner * kDiags + k;
+          if (mk > kTrust) {
+            const int slot = atomicAdd(&sm.vcount[warp], 1);
+            if (slot < kVerify) {
+              VerifyReq& q = sm.vreq[warp][slot];
+              q.i = i; q.j = j; q.f = ivc * ivr;
+              q.rslot = static_cast<short>(r0 + rr);
+              q.cslot = static_cast<short>(cs);
+              q.g = g;
+            } else {
+              publish(sm, cx, verify_cov_lane(pr.R, pr.C, i, j, cx.m) * ivc * ivr, i, j,
+                      r0 + rr, cs, g);
+            }
+          } else {
+            publish(sm, cx, rv, i, j, r0 + rr, cs, g);
+          }
+        }
+        const float dfr = g ? rf.y : rf.x, dgr = g ? rf.w : rf.z;
+        const float dfc = g ? cf.y : cf.x, dgc = g ? cf.w : cf.z;
+        c = fmaf(dfc, dgr, c);
+        c = fmaf(dfr, dgc, c);
+      }
     }
-    verified = slow_step(sm, cx, it.s, it.owner, cov, V, it.W);
   }
   __syncwarp();
-  return verified;
+  const int nreq = sm.vcount[warp];
+  const int nv = nreq < kVerify ? nreq : kVerify;
+  for (int q = 0; q < nv; ++q) {
+    const VerifyReq rq = sm.vreq[warp][q];
+    const float cv = verify_cov_warp(pr.R, pr.C, rq.i, rq.j, cx.m, lane);
+    if (lane == 0) publish(sm, cx, cv * rq.f, rq.i, rq.j, rq.rslot, rq.cslot, rq.g);
+    __syncwarp();
+  }
+  return nreq;
 }
 
 }  // namespace
@@ -270,10 +326,10 @@ join_mixed_1nn_kernel(JoinParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   const int t = threadIdx.x;
+  const int lane = t & 31, warp = t >> 5;
   const int64_t K = P.seg_len;
   const int64_t m = P.m;
   unsigned long long n_steps = 0, n_slow = 0, n_verify = 0;
-  const int lane = t & 31, warp = t >> 5;
   int qn = 0;  // queued blocks of this warp (warp-uniform)
 
   for (;;) {
@@ -305,17 +361,17 @@ join_mixed_1nn_kernel(JoinParams P) {
       seg_len[g] = l < 0 ? 0 : (l > K ? K : l);
     }
     const int64_t d_my = D0 + t * kDiags;
+    const int sh = pr.C.bshift;
 
     // ---------------- anchors ----------------
     // With the thread's first column window j0 and
     // Y(p) = T32c[p] + (boff_c[p >> bshift] - mu_j0) (the column samples
     // centred by that window's mean, shared by the thread's 8 windows):
     //   anchor_k = sum_t xc_t * Y(j_k + t) - (mu_jk - mu_j0) * sum_t xc_t
-    // where xc is the row window centred by its FP64 mean (staged in shared
-    // memory); every factor stays within the windows' own variation.
+    // where xc is the row window centred by its FP64 mean.  Both the row
+    // window and the CTA's column span are staged in shared memory.
     float acc[2][kDiags];
     float xsum[2] = {0.f, 0.f};
-    const int sh = pr.C.bshift;
 #pragma unroll
     for (int g = 0; g < 2; ++g)
 #pragma unroll
@@ -336,12 +392,18 @@ join_mixed_1nn_kernel(JoinParams P) {
           }
           sm.u.a.xr[g][x] = v;
         }
+        const int64_t cb = i + D0 + t0;
+        for (int x = t; x < kBand + chunk + 16; x += kThreads) {
+          const int64_t p = cb + x;
+          sm.u.a.yc[g][pady(x)] = (live && p < pr.C.n) ? pr.C.T32[p] : 0.f;
+        }
       }
       __syncthreads();
 #pragma unroll
       for (int g = 0; g < 2; ++g) {
         if (seg_len[g] == 0) continue;
         const float* __restrict__ xr = sm.u.a.xr[g];
+        const float* __restrict__ ycs = sm.u.a.yc[g];
         const int64_t jb = seg_row[g] + d_my;      // the thread's first column window
         const int64_t jc = jb < pr.C.ns ? jb : pr.C.ns - 1;
         const int64_t b0 = jc >> sh;
@@ -366,12 +428,16 @@ join_mixed_1nn_kernel(JoinParams P) {
               dhi = (((bf + 1) << sh) < plim) ? block_delta(pr.C, bf + 1, b0) - mu0 : 0.f;
             }
             const int64_t pbound = (bf + 1) << sh;  // first sample of the next block
+            const int o = pady(t * kDiags + xg);      // 16-byte aligned slot
+            const float4 v0 = *reinterpret_cast<const float4*>(ycs + o);
+            const float4 v1 = *reinterpret_cast<const float4*>(ycs + o + 4);
+            const float4 v2 = *reinterpret_cast<const float4*>(ycs + o + 12);
+            const float4 v3 = *reinterpret_cast<const float4*>(ycs + o + 16);
+            const float yv[16] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w,
+                                  v2.x, v2.y, v2.z, v2.w, v3.x, v3.y, v3.z, v3.w};
             float y[16];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-              const int64_t p = jb + t0 + xg + q;
-              y[q] = p < plim ? pr.C.T32[p] + (p < pbound ? dlo : dhi) : 0.f;
-            }
+            for (int q = 0; q < 16; ++q) y[q] = yv[q] + (pg + q < pbound ? dlo : dhi);
 #pragma unroll
             for (int v = 0; v < 8; ++v) {
               if (xg + v < c1) {
@@ -412,7 +478,8 @@ join_mixed_1nn_kernel(JoinParams P) {
       // An excluded diagonal carries NaN: every r on it is NaN and never wins.
       cov[k] = valid ? make_float2(acc[0][k], acc[1][k]) : make_float2(qnan(), qnan());
       // initial drift estimate: the anchor's own rounding
-      V[k] = make_float2(P.anchor_vcoef * cov[k].x * cov[k].x, P.anchor_vcoef * cov[k].y * cov[k].y);
+      V[k] = make_float2(P.anchor_vcoef * cov[k].x * cov[k].x,
+                         P.anchor_vcoef * cov[k].y * cov[k].y);
     }
     float2 W = make_float2(0.f, 0.f);  // accumulated squared increment bounds
 
@@ -433,28 +500,12 @@ join_mixed_1nn_kernel(JoinParams P) {
         cbase_g[g] = rbase[g] + D0;
         cx.rbase[g] = rbase[g];
       }
-      // rows
-      for (int x = t; x < kSlab; x += kThreads) {
-        const int64_t i0 = rbase[0] + x, i1 = rbase[1] + x;
-        const bool ok0 = i0 < rend[0], ok1 = i1 < rend[1];
-        float4 f;
-        f.x = ok0 ? pr.R.df32[i0] : 0.f;
-        f.y = ok1 ? pr.R.df32[i1] : 0.f;
-        f.z = ok0 ? pr.R.dg32[i0] : 0.f;
-        f.w = ok1 ? pr.R.dg32[i1] : 0.f;
-        sm.r_fg[x] = f;
-        const float2 iv = make_float2(ok0 ? pr.R.inv32[i0] : qnan(), ok1 ? pr.R.inv32[i1] : qnan());
-        sm.r_iv[x] = iv;
-        // A window that cannot match (padding, NaN or flat) must not lower
-        // the filter threshold: its best is "unreachable".
-        float2 b;
-        b.x = (pr.key_row && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_row[i0], P.kl) : kNoTarget;
-        b.y = (pr.key_row && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_row[i1], P.kl) : kNoTarget;
-        sm.r_best[x] = b;
-      }
-      // columns
-      for (int x = t; x < kCols; x += kThreads) {
-        const int64_t j0 = cbase_g[0] + x, j1 = cbase_g[1] + x;
+      // Staging, coalesced: thread t stages columns t, t + kThreads, ... and
+      // row t; then the per-block and per-step filter tables are built from
+      // shared memory.
+#pragma unroll 3
+      for (int c = t; c < kCols; c += kThreads) {
+        const int64_t j0 = cbase_g[0] + c, j1 = cbase_g[1] + c;
         const bool ok0 = seg_len[0] > 0 && j0 < pr.C.ns;
         const bool ok1 = seg_len[1] > 0 && j1 < pr.C.ns;
         float4 f;
@@ -462,29 +513,46 @@ join_mixed_1nn_kernel(JoinParams P) {
         f.y = ok1 ? pr.C.df32[j1] : 0.f;
         f.z = ok0 ? pr.C.dg32[j0] : 0.f;
         f.w = ok1 ? pr.C.dg32[j1] : 0.f;
-        sm.u.s.c_fg[padc(x)] = f;
         const float2 iv = make_float2(ok0 ? pr.C.inv32[j0] : qnan(), ok1 ? pr.C.inv32[j1] : qnan());
-        sm.u.s.c_iv[padc(x)] = iv;
-        float2 b;
-        b.x = (pr.key_col && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_col[j0], P.kl) : kNoTarget;
-        b.y = (pr.key_col && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_col[j1], P.kl) : kNoTarget;
-        sm.c_best[x] = b;
+        // A window that cannot match (padding, NaN or flat) must not lower
+        // the filter threshold: its best is "unreachable".
+        float2 cbv;
+        cbv.x = (pr.key_col && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_col[j0], P.kl) : kNoTarget;
+        cbv.y = (pr.key_col && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_col[j1], P.kl) : kNoTarget;
+        sm.u.s.c_fg[padc(c)] = f;
+        sm.u.s.c_iv[padc(c)] = iv;
+        sm.c_best[c] = cbv;
+      }
+      for (int r = t; r < kSlab; r += kThreads) {
+        const int64_t i0 = rbase[0] + r, i1 = rbase[1] + r;
+        const bool ok0 = i0 < rend[0], ok1 = i1 < rend[1];
+        float4 f;
+        f.x = ok0 ? pr.R.df32[i0] : 0.f;
+        f.y = ok1 ? pr.R.df32[i1] : 0.f;
+        f.z = ok0 ? pr.R.dg32[i0] : 0.f;
+        f.w = ok1 ? pr.R.dg32[i1] : 0.f;
+        const float2 iv = make_float2(ok0 ? pr.R.inv32[i0] : qnan(), ok1 ? pr.R.inv32[i1] : qnan());
+        float2 rbv;
+        rbv.x = (pr.key_row && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_row[i0], P.kl) : kNoTarget;
+        rbv.y = (pr.key_row && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_row[i1], P.kl) : kNoTarget;
+        sm.r_fg[r] = f;
+        sm.r_iv[r] = iv;
+        sm.r_best[r] = rbv;
       }
       __syncthreads();
-      // Per 8-column block: minimum best and maximum inverse norm; per step:
-      // the same over its rows.
       for (int b = t; b < kBlocks; b += kThreads) {
         float2 mn = make_float2(kNoTarget, kNoTarget), mx = make_float2(0.f, 0.f);
         float4 mf = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int x = 0; x < 8; ++x) {
-          const float2 cb = sm.c_best[8 * b + x];
-          const float2 iv = sm.u.s.c_iv[padc(8 * b + x)];
-          const float4 fg = sm.u.s.c_fg[padc(8 * b + x)];
-          mn.x = fminf(mn.x, cb.x); mn.y = fminf(mn.y, cb.y);
+          const int c = 8 * b + x;
+          const float4 f = sm.u.s.c_fg[padc(c)];
+          const float2 iv = sm.u.s.c_iv[padc(c)];
+          const float2 cbv = sm.c_best[c];
+          mn.x = fminf(mn.x, cbv.x); mn.y = fminf(mn.y, cbv.y);
           mx.x = fmaxf(mx.x, iv.x); mx.y = fmaxf(mx.y, iv.y);
-          mf.x = fmaxf(mf.x, fabsf(fg.x)); mf.y = fmaxf(mf.y, fabsf(fg.y));
-          mf.z = fmaxf(mf.z, fabsf(fg.z)); mf.w = fmaxf(mf.w, fabsf(fg.w));
+          mf.x = fmaxf(mf.x, fabsf(f.x)); mf.y = fmaxf(mf.y, fabsf(f.y));
+          mf.z = fmaxf(mf.z, fabsf(f.z)); mf.w = fmaxf(mf.w, fabsf(f.w));
         }
         sm.c_blkmin[b] = mn;
         sm.c_blkmax_iv[b] = mx;
@@ -495,13 +563,14 @@ join_mixed_1nn_kernel(JoinParams P) {
         float4 mf = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int x = 0; x < kRows; ++x) {
-          const float2 rb = sm.r_best[t * kRows + x];
-          const float2 iv = sm.r_iv[t * kRows + x];
-          const float4 fg = sm.r_fg[t * kRows + x];
-          mn.x = fminf(mn.x, rb.x); mn.y = fminf(mn.y, rb.y);
+          const int r = t * kRows + x;
+          const float4 f = sm.r_fg[r];
+          const float2 iv = sm.r_iv[r];
+          const float2 rbv = sm.r_best[r];
+          mn.x = fminf(mn.x, rbv.x); mn.y = fminf(mn.y, rbv.y);
           mx.x = fmaxf(mx.x, iv.x); mx.y = fmaxf(mx.y, iv.y);
-          mf.x = fmaxf(mf.x, fabsf(fg.x)); mf.y = fmaxf(mf.y, fabsf(fg.y));
-          mf.z = fmaxf(mf.z, fabsf(fg.z)); mf.w = fmaxf(mf.w, fabsf(fg.w));
+          mf.x = fmaxf(mf.x, fabsf(f.x)); mf.y = fmaxf(mf.y, fabsf(f.y));
+          mf.z = fmaxf(mf.z, fabsf(f.z)); mf.w = fmaxf(mf.w, fabsf(f.w));
         }
         sm.r_stepmin[t] = mn;
         sm.r_stepmax_iv[t] = mx;
@@ -584,11 +653,8 @@ join_mixed_1nn_kernel(JoinParams P) {
           if (trig) {
             SlowItem& it = sm.queue[warp][qn + __popc(tmask & ((1u << lane) - 1u))];
 #pragma unroll
-            for (int k = 0; k < kDiags; ++k) {
-              it.cov[k] = cov[k];
-              it.V[k] = V[k];
-            }
-            it.W = W;
+            for (int k = 0; k < kDiags; ++k) it.cov[k] = cov[k];
+            it.vw = make_float2(vx, vy);
             it.s = s;
             it.owner = t;
           }
@@ -608,9 +674,8 @@ join_mixed_1nn_kernel(JoinParams P) {
   for (int o = 16; o > 0; o >>= 1) {
     n_steps += __shfl_xor_sync(0xffffffffu, n_steps, o);
     n_slow += __shfl_xor_sync(0xffffffffu, n_slow, o);
-    n_verify += __shfl_xor_sync(0xffffffffu, n_verify, o);
   }
-  if ((t & 31) == 0 && P.counters) {
+  if (lane == 0 && P.counters) {
     atomicAdd(P.counters + 0, n_steps);
     atomicAdd(P.counters + 1, n_slow);
     atomicAdd(P.counters + 2, n_verify);
