@@ -391,6 +391,12 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   }
   K = std::min(K, std::max<int64_t>(k_lb, slab));
   K = std::max<int64_t>(slab, (K / slab) * slab);
+  {
+    // The mixed 1NN kernel pairs the two segments of a unit; their column
+    // spans must be a whole number of FP32-copy blocks apart.
+    const int64_t blk = 1ll << block_shift(m);
+    if (K % blk) K = std::max<int64_t>(blk, (K / blk) * blk);
+  }
 
   JoinParams P{};
   std::vector<int64_t> prefix;

@@ -49,8 +49,10 @@ constexpr int kBlocks = kCols / 8;        // 8-column blocks
 constexpr int kPad = kCols + kBlocks;     // padded slot c + c/8
 constexpr int kAnchorChunk = 512;         // row-window samples per anchor pass
 constexpr int kYSpan = kBand + kAnchorChunk + 16;     // staged column samples
-constexpr int kYPad = (kYSpan / 8) * 12;              // padded: 12 slots per 8
-constexpr int kQueue = 32;                // queued blocks per warp (>= lanes)
+constexpr int kYPad = (kYSpan / 8) * 10;              // padded: 10 pairs per 8
+// blocks hold >= 32 samples: the span plus the block after its end
+constexpr int kSpanBlk = kYSpan / 32 + 3;
+constexpr int kQueue = 16;                // queued blocks per warp
 constexpr int kVerify = 64;               // verification requests per warp
 constexpr float kEps = 5.9604645e-8f;     // 2^-24
 constexpr float kBoundC = 4.0f;
@@ -83,6 +85,17 @@ __device__ __forceinline__ float max3(float a, float b, float c) {
 }
 __device__ __forceinline__ float qnan() { return __int_as_float(0x7FC00000); }
 
+// Largest |cov| over the 8 diagonals, per segment (NaN entries ignored).
+__device__ __forceinline__ float2 absmax8(const float2 (&c)[8]) {
+  float x = max3(fabsf(c[0].x), fabsf(c[1].x), fabsf(c[2].x));
+  float y = max3(fabsf(c[0].y), fabsf(c[1].y), fabsf(c[2].y));
+  x = max3(x, fabsf(c[3].x), fabsf(c[4].x));
+  y = max3(y, fabsf(c[3].y), fabsf(c[4].y));
+  x = max3(x, fabsf(c[5].x), fabsf(c[6].x));
+  y = max3(y, fabsf(c[5].y), fabsf(c[6].y));
+  return make_float2(fmaxf(x, fabsf(c[7].x)), fmaxf(y, fabsf(c[7].y)));
+}
+
 // Correlation encoded by a profile key, rounded down (a filter threshold may
 // only be lower than the true best).  Integer pipe only.
 __device__ __forceinline__ float key_corr_floor(u64 key, const KeyLayout& kl) {
@@ -106,15 +119,6 @@ struct SlowItem {
   int owner;  // thread index of the owner
 };
 
-// A cell whose FP32 value is not trusted: verified by its warp.
-struct VerifyReq {
-  long long i, j;   // row and column window
-  float f;          // inv_c * inv_r
-  short rslot;      // staged row of the cell
-  short cslot;      // staged column of the cell
-  int g;            // segment (0 = .x, 1 = .y)
-};
-
 struct Smem {
   union {
     struct {
@@ -122,8 +126,9 @@ struct Smem {
       float2 c_iv[kPad];  // {inv.x, inv.y}
     } s;
     struct {
-      float xr[2][kAnchorChunk];  // centred row window (chunk)
-      float yc[2][kYPad];         // column samples (block-relative), padded
+      float2 xr[kAnchorChunk];    // centred row windows of both segments (chunk)
+      float2 yc[kYPad];           // column samples (block-relative), padded
+      float2 cb[2][kSpanBlk];     // {bhi, blo} of the blocks of the staged span
     } a;
   } u;
   float2 c_best[kCols];
@@ -137,14 +142,18 @@ struct Smem {
   float2 r_stepmax_iv[kSteps];
   float4 r_stepmax_fg[kSteps];
   SlowItem queue[kWarps][kQueue];
-  VerifyReq vreq[kWarps][kVerify];
+  // cells to verify: rslot | cslot << 7 | segment << 18
+  uint32_t vreq[kWarps][kVerify];
   int vcount[kWarps];
   Problem prob;  // the current unit's band problem
   long long unit, band, unit_in_band;
 };
 
+// Four CTAs per SM: 4 x (shared memory + 1 KB reserved) within 228 KB.
+static_assert(sizeof(Smem) + 1024 <= 228 * 1024 / 4, "shared memory exceeds 4 CTAs/SM");
+
 __device__ __forceinline__ int padc(int c) { return c + (c >> 3); }
-__device__ __forceinline__ int pady(int x) { return x + (x >> 3) * 4; }
+__device__ __forceinline__ int pady2(int x) { return x + (x >> 3) * 2; }
 
 // Offset of block b relative to block b0, as the float sum of the two
 // blocks' hi/lo parts: exact while the two offsets are within a factor of two.
@@ -152,62 +161,44 @@ __device__ __forceinline__ float block_delta(const SeriesDev& S, int64_t b, int6
   return (S.bhi[b] - S.bhi[b0]) + (S.blo[b] - S.blo[b0]);
 }
 
-// Covariance of row window i and column window j, FP32, one lane: each
-// factor formed as (sample relative to its block offset) + (block offset -
-// window mean), summed per block run.  Fallback of the warp-wide form.
-__device__ __noinline__ float verify_cov_lane(const SeriesDev& R, const SeriesDev& C,
-                                              int64_t i, int64_t j, int64_t m) {
+// Partial covariance of row window i and column window j over the terms
+// t in [tb, te), FP32: each factor formed as (sample relative to its block
+// offset) + (block offset - window mean), summed per run of terms that share
+// both blocks.
+__device__ __forceinline__ float cov_part(const SeriesDev& R, const SeriesDev& C,
+                                          int64_t i, int64_t j, int64_t tb, int64_t te_all) {
   const int sh = R.bshift;
   const int64_t bi = i >> sh, bj = j >> sh;
   const float mri = R.mu_rel[i], mcj = C.mu_rel[j];
   float acc = 0.f;
-  int64_t t = 0;
-  while (t < m) {
+  int64_t t = tb;
+  while (t < te_all) {
     const int64_t br = (i + t) >> sh, bc = (j + t) >> sh;
     int64_t te = ((br + 1) << sh) - i;
     const int64_t te2 = ((bc + 1) << sh) - j;
     if (te2 < te) te = te2;
-    if (m < te) te = m;
+    if (te_all < te) te = te_all;
     const float xc = block_delta(R, br, bi) - mri;
     const float yc = block_delta(C, bc, bj) - mcj;
-    float p0 = 0.f, p1 = 0.f;
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
     int64_t u = t;
-    for (; u + 1 < te; u += 2) {
+    for (; u + 3 < te; u += 4) {
       p0 = fmaf(R.T32[i + u] + xc, C.T32[j + u] + yc, p0);
       p1 = fmaf(R.T32[i + u + 1] + xc, C.T32[j + u + 1] + yc, p1);
+      p2 = fmaf(R.T32[i + u + 2] + xc, C.T32[j + u + 2] + yc, p2);
+      p3 = fmaf(R.T32[i + u + 3] + xc, C.T32[j + u + 3] + yc, p3);
     }
-    if (u < te) p0 = fmaf(R.T32[i + u] + xc, C.T32[j + u] + yc, p0);
-    acc += p0 + p1;
+    for (; u < te; ++u) p0 = fmaf(R.T32[i + u] + xc, C.T32[j + u] + yc, p0);
+    acc += (p0 + p1) + (p2 + p3);
     t = te;
   }
   return acc;
 }
 
-// The same covariance computed by a whole warp: lane l sums the terms
-// t = l, l + 32, ...; the partial sums meet in a shuffle reduction.
-__device__ __forceinline__ float verify_cov_warp(const SeriesDev& R, const SeriesDev& C,
-                                                 int64_t i, int64_t j, int64_t m, int lane) {
-  const int sh = R.bshift;
-  const int64_t bi = i >> sh, bj = j >> sh;
-  const float mri = R.mu_rel[i], mcj = C.mu_rel[j];
-  const float hr0 = R.bhi[bi], lr0 = R.blo[bi], hc0 = C.bhi[bj], lc0 = C.blo[bj];
-  float acc[4] = {0.f, 0.f, 0.f, 0.f};
-  for (int64_t t0 = lane; t0 < m; t0 += 128) {
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int64_t t = t0 + 32 * u;
-      if (t < m) {
-        const int64_t br = (i + t) >> sh, bc = (j + t) >> sh;
-        const float x = R.T32[i + t] + (((R.bhi[br] - hr0) + (R.blo[br] - lr0)) - mri);
-        const float y = C.T32[j + t] + (((C.bhi[bc] - hc0) + (C.blo[bc] - lc0)) - mcj);
-        acc[u] = fmaf(x, y, acc[u]);
-      }
-    }
-  }
-  float a = (acc[0] + acc[1]) + (acc[2] + acc[3]);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-  return a;
+// The whole covariance, one lane (used when a warp's request list is full).
+__device__ __noinline__ float verify_cov_lane(const SeriesDev& R, const SeriesDev& C,
+                                              int64_t i, int64_t j, int64_t m) {
+  return cov_part(R, C, i, j, 0, m);
 }
 
 struct SlowCtx {
@@ -246,7 +237,7 @@ __device__ __forceinline__ void publish(Smem& sm, const SlowCtx& cx, float rv, i
 __device__ __noinline__ int drain_queue(Smem& sm, const SlowCtx& cx, int warp, int count,
                                         int lane) {
   if (lane == 0) sm.vcount[warp] = 0;
-  __syncwarp();
+  __syncwarp();  // the queue was written by other lanes
   const Problem& pr = *cx.pr;
   const int k = (lane & 15) >> 1, g = lane & 1;
   for (int p = 0; p < count; p += 2) {
@@ -285,11 +276,9 @@ __device__ __noinline__ int drain_queue(Smem& sm, const SlowCtx& cx, int warp, i
           if (mk > kTrust) {
             const int slot = atomicAdd(&sm.vcount[warp], 1);
             if (slot < kVerify) {
-              VerifyReq& q = sm.vreq[warp][slot];
-              q.i = i; q.j = j; q.f = ivc * ivr;
-              q.rslot = static_cast<short>(r0 + rr);
-              q.cslot = static_cast<short>(cs);
-              q.g = g;
+              sm.vreq[warp][slot] = static_cast<uint32_t>(r0 + rr) |
+                                    (static_cast<uint32_t>(cs) << 7) |
+                                    (static_cast<uint32_t>(g) << 18);
             } else {
               publish(sm, cx, verify_cov_lane(pr.R, pr.C, i, j, cx.m) * ivc * ivr, i, j,
                       r0 + rr, cs, g);
@@ -306,14 +295,40 @@ __device__ __noinline__ int drain_queue(Smem& sm, const SlowCtx& cx, int warp, i
     }
   }
   __syncwarp();
+  // Verification, four cells at a time: 8 lanes per cell, each summing a
+  // contiguous eighth of the window, so that the loads of 4 cells are in
+  // flight together.
   const int nreq = sm.vcount[warp];
   const int nv = nreq < kVerify ? nreq : kVerify;
-  for (int q = 0; q < nv; ++q) {
-    const VerifyReq rq = sm.vreq[warp][q];
-    const float cv = verify_cov_warp(pr.R, pr.C, rq.i, rq.j, cx.m, lane);
-    if (lane == 0) publish(sm, cx, cv * rq.f, rq.i, rq.j, rq.rslot, rq.cslot, rq.g);
-    __syncwarp();
+  const int sub = lane & 7;
+  const int64_t L = (cx.m + 7) >> 3;
+  for (int q0 = 0; q0 < nv; q0 += 4) {
+    const int q = q0 + (lane >> 3);
+    float part = 0.f;
+    int rs = 0, cs = 0, g = 0;
+    int64_t i = 0, j = 0;
+    if (q < nv) {
+      const uint32_t rq = sm.vreq[warp][q];
+      rs = static_cast<int>(rq & 127u);
+      cs = static_cast<int>((rq >> 7) & 2047u);
+      g = static_cast<int>(rq >> 18);
+      i = cx.rbase[g] + rs;
+      j = i + cx.D0 + (cs - rs);
+      const int64_t tb = sub * L;
+      const int64_t te = tb + L < cx.m ? tb + L : cx.m;
+      part = cov_part(pr.R, pr.C, i, j, tb, te);
+    }
+    part += __shfl_xor_sync(0xffffffffu, part, 4);
+    part += __shfl_xor_sync(0xffffffffu, part, 2);
+    part += __shfl_xor_sync(0xffffffffu, part, 1);
+    if (q < nv && sub == 0) {
+      const float2 ivr2 = sm.r_iv[rs];
+      const float2 ivc2 = sm.u.s.c_iv[padc(cs)];
+      const float f = g ? ivc2.y * ivr2.y : ivc2.x * ivr2.x;
+      publish(sm, cx, part * f, i, j, rs, cs, g);
+    }
   }
+  __syncwarp();
   return nreq;
 }
 
@@ -321,7 +336,7 @@ __device__ __noinline__ int drain_queue(Smem& sm, const SlowCtx& cx, int warp, i
 
 size_t mixed_1nn_smem_bytes() { return sizeof(Smem); }
 
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, 4)
 join_mixed_1nn_kernel(JoinParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
@@ -368,120 +383,145 @@ join_mixed_1nn_kernel(JoinParams P) {
     // Y(p) = T32c[p] + (boff_c[p >> bshift] - mu_j0) (the column samples
     // centred by that window's mean, shared by the thread's 8 windows):
     //   anchor_k = sum_t xc_t * Y(j_k + t) - (mu_jk - mu_j0) * sum_t xc_t
-    // where xc is the row window centred by its FP64 mean.  Both the row
-    // window and the CTA's column span are staged in shared memory.
-    float acc[2][kDiags];
-    float xsum[2] = {0.f, 0.f};
+    // where xc is the row window centred by its FP64 mean.  The two segments
+    // run as f32x2 pairs: their column spans are seg_len apart, a multiple of
+    // the block size, so both halves cross block boundaries together.  The
+    // row windows and the CTA's column spans are staged in shared memory.
+    float2 acc2[kDiags];
+    float2 xsum2 = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int g = 0; g < 2; ++g)
-#pragma unroll
-      for (int k = 0; k < kDiags; ++k) acc[g][k] = 0.f;
-    for (int64_t t0 = 0; t0 < m; t0 += kAnchorChunk) {
-      const int chunk = static_cast<int>((m - t0) < kAnchorChunk ? (m - t0) : kAnchorChunk);
-#pragma unroll
-      for (int g = 0; g < 2; ++g) {
-        const int64_t i = seg_row[g];
-        const bool live = seg_len[g] > 0;
-        const int64_t bi = i >> sh;
-        const float mri = live ? pr.R.mu_rel[i] : 0.f;
-        for (int x = t; x < chunk; x += kThreads) {
-          float v = 0.f;
-          if (live) {
-            const int64_t p = i + t0 + x;
-            v = pr.R.T32[p] + (block_delta(pr.R, p >> sh, bi) - mri);
-          }
-          sm.u.a.xr[g][x] = v;
-        }
-        const int64_t cb = i + D0 + t0;
-        for (int x = t; x < kBand + chunk + 16; x += kThreads) {
-          const int64_t p = cb + x;
-          sm.u.a.yc[g][pady(x)] = (live && p < pr.C.n) ? pr.C.T32[p] : 0.f;
-        }
-      }
-      __syncthreads();
-#pragma unroll
-      for (int g = 0; g < 2; ++g) {
-        if (seg_len[g] == 0) continue;
-        const float* __restrict__ xr = sm.u.a.xr[g];
-        const float* __restrict__ ycs = sm.u.a.yc[g];
-        const int64_t jb = seg_row[g] + d_my;      // the thread's first column window
-        const int64_t jc = jb < pr.C.ns ? jb : pr.C.ns - 1;
-        const int64_t b0 = jc >> sh;
-        const float mu0 = pr.C.mu_rel[jc];         // mu_j0 - boff_c[b0]
-        const int64_t plim = pr.C.n;
-        int64_t cur_b = -1;                        // block of the cached corrections
-        float dlo = 0.f, dhi = 0.f;
-        for (int c0 = 0; c0 < chunk; c0 += 32) {
-          float part[kDiags];
-#pragma unroll
-          for (int k = 0; k < kDiags; ++k) part[k] = 0.f;
-          float xs = 0.f;
-          const int c1 = (c0 + 32 < chunk) ? c0 + 32 : chunk;
-          // groups of 8 row samples: 16 column samples cover the 8 windows;
-          // 16 consecutive samples touch at most two blocks (blocks hold >= 32)
-          for (int xg = c0; xg < c1; xg += 8) {
-            const int64_t pg = jb + t0 + xg;
-            const int64_t bf = pg >> sh;
-            if (bf != cur_b) {
-              cur_b = bf;
-              dlo = (pg < plim) ? block_delta(pr.C, bf, b0) - mu0 : 0.f;
-              dhi = (((bf + 1) << sh) < plim) ? block_delta(pr.C, bf + 1, b0) - mu0 : 0.f;
-            }
-            const int64_t pbound = (bf + 1) << sh;  // first sample of the next block
-            const int o = pady(t * kDiags + xg);      // 16-byte aligned slot
-            const float4 v0 = *reinterpret_cast<const float4*>(ycs + o);
-            const float4 v1 = *reinterpret_cast<const float4*>(ycs + o + 4);
-            const float4 v2 = *reinterpret_cast<const float4*>(ycs + o + 12);
-            const float4 v3 = *reinterpret_cast<const float4*>(ycs + o + 16);
-            const float yv[16] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w,
-                                  v2.x, v2.y, v2.z, v2.w, v3.x, v3.y, v3.z, v3.w};
-            float y[16];
-#pragma unroll
-            for (int q = 0; q < 16; ++q) y[q] = yv[q] + (pg + q < pbound ? dlo : dhi);
-#pragma unroll
-            for (int v = 0; v < 8; ++v) {
-              if (xg + v < c1) {
-                const float xv = xr[xg + v];
-                xs += xv;
-#pragma unroll
-                for (int k = 0; k < kDiags; ++k) part[k] = fmaf(xv, y[v + k], part[k]);
-              }
-            }
-          }
-#pragma unroll
-          for (int k = 0; k < kDiags; ++k) acc[g][k] += part[k];
-          xsum[g] += xs;
-        }
-      }
-      __syncthreads();
-    }
+    for (int k = 0; k < kDiags; ++k) acc2[k] = make_float2(0.f, 0.f);
+    int64_t jb[2], b0s[2];
+    float mu0[2];
+    float2 o0[2];                 // {bhi, blo} of the block of mu_j0
 #pragma unroll
     for (int g = 0; g < 2; ++g) {
-      if (seg_len[g] == 0) continue;
-      const int64_t jb = seg_row[g] + d_my;
-      const int64_t jc = jb < pr.C.ns ? jb : pr.C.ns - 1;
-      const int64_t b0 = jc >> sh;
-      const float mu0 = pr.C.mu_rel[jc];
+      jb[g] = seg_row[g] + d_my;  // the thread's first column window
+      const int64_t jc = jb[g] < pr.C.ns ? jb[g] : pr.C.ns - 1;
+      b0s[g] = jc >> sh;
+      mu0[g] = pr.C.mu_rel[jc];   // mu_j0 - boff_c[b0]
+      o0[g] = make_float2(pr.C.bhi[b0s[g]], pr.C.blo[b0s[g]]);
+    }
+    const bool live1 = seg_len[1] > 0;
+    const int64_t nblk_c = (pr.C.n + (int64_t{1} << sh) - 1) >> sh;
+    int64_t span_b0 = 0;
+    for (int64_t t0 = 0; t0 < m; t0 += kAnchorChunk) {
+      const int chunk = static_cast<int>((m - t0) < kAnchorChunk ? (m - t0) : kAnchorChunk);
+      {
+        const int64_t i0 = seg_row[0], i1 = seg_row[1];
+        const int64_t bi0 = i0 >> sh, bi1 = i1 >> sh;
+        const float mr0 = pr.R.mu_rel[i0], mr1 = live1 ? pr.R.mu_rel[i1] : 0.f;
+        for (int x = t; x < chunk; x += kThreads) {
+          const int64_t p0 = i0 + t0 + x, p1 = i1 + t0 + x;
+          float2 v;
+          v.x = pr.R.T32[p0] + (block_delta(pr.R, p0 >> sh, bi0) - mr0);
+          v.y = live1 ? pr.R.T32[p1] + (block_delta(pr.R, p1 >> sh, bi1) - mr1) : 0.f;
+          sm.u.a.xr[x] = v;
+        }
+        const int64_t cb0 = i0 + D0 + t0, cb1 = i1 + D0 + t0;
+        for (int x = t; x < kBand + chunk + 16; x += kThreads) {
+          const int64_t p0 = cb0 + x, p1 = cb1 + x;
+          float2 v;
+          v.x = p0 < pr.C.n ? pr.C.T32[p0] : 0.f;
+          v.y = (live1 && p1 < pr.C.n) ? pr.C.T32[p1] : 0.f;
+          sm.u.a.yc[pady2(x)] = v;
+        }
+        if (t < 2 * kSpanBlk) {
+          const int g = t >= kSpanBlk, x = t - g * kSpanBlk;
+          const int64_t b = ((g ? cb1 : cb0) >> sh) + x;
+          const bool ok = (g == 0 || live1) && b < nblk_c;
+          sm.u.a.cb[g][x] = ok ? make_float2(pr.C.bhi[b], pr.C.blo[b]) : make_float2(0.f, 0.f);
+        }
+        span_b0 = cb0 >> sh;
+      }
+      __syncthreads();
+      const int64_t plim0 = pr.C.n;
+      int64_t cur_b = -1;                        // block of the cached corrections
+      float2 dlo = make_float2(0.f, 0.f), dhi = make_float2(0.f, 0.f);
+      for (int c0 = 0; c0 < chunk; c0 += 32) {
+        float2 part[kDiags];
 #pragma unroll
-      for (int k = 0; k < kDiags; ++k) {
-        const int64_t j = jb + k;
-        if (j >= pr.C.ns) continue;
-        const float ek = (pr.C.mu_rel[j] + block_delta(pr.C, j >> sh, b0)) - mu0;
-        acc[g][k] = fmaf(-ek, xsum[g], acc[g][k]);
+        for (int k = 0; k < kDiags; ++k) part[k] = make_float2(0.f, 0.f);
+        float2 xs = make_float2(0.f, 0.f);
+        const int c1 = (c0 + 32 < chunk) ? c0 + 32 : chunk;
+        // groups of 8 row samples: 16 column samples cover the 8 windows;
+        // 16 consecutive samples touch at most two blocks (blocks hold >= 32)
+        for (int xg = c0; xg < c1; xg += 8) {
+          const int64_t pg = jb[0] + t0 + xg;
+          const int64_t bf = pg >> sh;
+          if (bf != cur_b) {
+            // the same sums as block_delta(), from the staged offsets; the
+            // second segment's blocks sit at the same span positions
+            cur_b = bf;
+            const int x = static_cast<int>(bf - span_b0);
+            const float2 l0 = sm.u.a.cb[0][x], h0 = sm.u.a.cb[0][x + 1];
+            const float2 l1 = sm.u.a.cb[1][x], h1 = sm.u.a.cb[1][x + 1];
+            dlo.x = (pg < plim0) ? ((l0.x - o0[0].x) + (l0.y - o0[0].y)) - mu0[0] : 0.f;
+            dhi.x = (((bf + 1) << sh) < plim0) ? ((h0.x - o0[0].x) + (h0.y - o0[0].y)) - mu0[0] : 0.f;
+            dlo.y = (live1 && pg + K < plim0) ? ((l1.x - o0[1].x) + (l1.y - o0[1].y)) - mu0[1] : 0.f;
+            dhi.y = (live1 && ((bf + 1) << sh) + K < plim0)
+                        ? ((h1.x - o0[1].x) + (h1.y - o0[1].y)) - mu0[1] : 0.f;
+          }
+          const int nb = static_cast<int>(((bf + 1) << sh) - pg);  // samples left in block bf
+          const int o = pady2(t * kDiags + xg);      // 16-byte aligned slot
+          float2 y[16];
+#pragma unroll
+          for (int q = 0; q < 16; q += 2) {
+            const float4 v = *reinterpret_cast<const float4*>(&sm.u.a.yc[o + q + (q >> 3) * 2]);
+            y[q] = make_float2(v.x, v.y);
+            y[q + 1] = make_float2(v.z, v.w);
+          }
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const float2 d = q < nb ? dlo : dhi;
+            y[q] = make_float2(y[q].x + d.x, y[q].y + d.y);
+          }
+#pragma unroll
+          for (int v = 0; v < 8; ++v) {
+            if (xg + v < c1) {
+              const float2 xv = sm.u.a.xr[xg + v];
+              xs = make_float2(xs.x + xv.x, xs.y + xv.y);
+#pragma unroll
+              for (int k = 0; k < kDiags; ++k) part[k] = fma2(xv, y[v + k], part[k]);
+            }
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < kDiags; ++k)
+          acc2[k] = make_float2(acc2[k].x + part[k].x, acc2[k].y + part[k].y);
+        xsum2 = make_float2(xsum2.x + xs.x, xsum2.y + xs.y);
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < kDiags; ++k) {
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int64_t j = jb[g] + k;
+        if (j >= pr.C.ns || (g == 1 && !live1)) continue;
+        const float ek = (pr.C.mu_rel[j] + block_delta(pr.C, j >> sh, b0s[g])) - mu0[g];
+        if (g) acc2[k].y = fmaf(-ek, xsum2.y, acc2[k].y);
+        else acc2[k].x = fmaf(-ek, xsum2.x, acc2[k].x);
       }
     }
-    float2 cov[kDiags], V[kDiags];
+    float2 cov[kDiags];
 #pragma unroll
     for (int k = 0; k < kDiags; ++k) {
       const int64_t d = d_my + k;
       const bool valid = d < pr.d_hi && !(d >= pr.x_lo && d < pr.x_hi);
       // An excluded diagonal carries NaN: every r on it is NaN and never wins.
-      cov[k] = valid ? make_float2(acc[0][k], acc[1][k]) : make_float2(qnan(), qnan());
-      // initial drift estimate: the anchor's own rounding
-      V[k] = make_float2(P.anchor_vcoef * cov[k].x * cov[k].x,
-                         P.anchor_vcoef * cov[k].y * cov[k].y);
+      cov[k] = valid ? acc2[k] : make_float2(qnan(), qnan());
     }
-    float2 W = make_float2(0.f, 0.f);  // accumulated squared increment bounds
+    // Drift state of the thread, per segment: the sum over steps of the
+    // largest cov^2 among its diagonals (an upper bound of every diagonal's
+    // own sum), starting from the anchors' rounding; and the sum of squared
+    // increment bounds.
+    float2 Vt;
+    {
+      const float2 cm = absmax8(cov);
+      Vt = make_float2(P.anchor_vcoef * cm.x * cm.x, P.anchor_vcoef * cm.y * cm.y);
+    }
+    float2 W = make_float2(0.f, 0.f);
 
     SlowCtx cx;
     cx.pr = &pr;
@@ -588,8 +628,10 @@ join_mixed_1nn_kernel(JoinParams P) {
         const float2 rsm = sm.r_stepmin[s];
         const float2 ic0 = sm.c_blkmax_iv[s + t], ic1 = sm.c_blkmax_iv[s + t + 1];
         const float2 irm = sm.r_stepmax_iv[s];
-#pragma unroll
-        for (int k = 0; k < kDiags; ++k) V[k] = fma2(cov[k], cov[k], V[k]);
+        {
+          const float2 cm = absmax8(cov);
+          Vt = fma2(cm, cm, Vt);
+        }
         {
           // bound of |df_c dg_r| + |df_r dg_c| over the step's cells
           const float4 cf0 = sm.c_blkmax_fg[s + t], cf1 = sm.c_blkmax_fg[s + t + 1];
@@ -600,10 +642,7 @@ join_mixed_1nn_kernel(JoinParams P) {
                                   mul2(make_float2(rfm.z, rfm.w), cdf));
           W = fma2(inc, inc, W);
         }
-        float vx = max3(V[0].x, V[1].x, V[2].x), vy = max3(V[0].y, V[1].y, V[2].y);
-        vx = max3(vx, V[3].x, V[4].x); vy = max3(vy, V[3].y, V[4].y);
-        vx = max3(vx, V[5].x, V[6].x); vy = max3(vy, V[5].y, V[6].y);
-        vx = fmaxf(vx, V[7].x) + W.x; vy = fmaxf(vy, V[7].y) + W.y;
+        const float vx = Vt.x + W.x, vy = Vt.y + W.y;
         const float tx = fminf(fminf(bm0.x, bm1.x), rsm.x) -
                          kBoundC * kEps * sqrtf(kRows * vx) * fmaxf(ic0.x, ic1.x) * irm.x;
         const float ty = fminf(fminf(bm0.y, bm1.y), rsm.y) -
@@ -611,6 +650,7 @@ join_mixed_1nn_kernel(JoinParams P) {
 
         // fast path: recurrence + block maximum
         float bx = -3.f, by = -3.f;
+        float2 rprev;
         float4 cf[kDiags + kRows - 1];
         float2 ci[kDiags + kRows - 1];
 #pragma unroll
@@ -628,37 +668,54 @@ join_mixed_1nn_kernel(JoinParams P) {
           const float4 rf = sm.r_fg[r0 + rr];
           const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
           const float2 ivr = sm.r_iv[r0 + rr];
+          // the row's largest cov * inv_c, times inv_r (> 0): the largest r
+          // of the row, rounded exactly as (cov * inv_c) * inv_r per cell
+          float2 p[kDiags];
 #pragma unroll
-          for (int k = 0; k < kDiags; k += 2) {
+          for (int k = 0; k < kDiags; ++k) p[k] = mul2(cov[k], ci[rr + k]);
+          float mx = max3(p[0].x, p[1].x, p[2].x), my = max3(p[0].y, p[1].y, p[2].y);
+          mx = max3(mx, p[3].x, p[4].x); my = max3(my, p[3].y, p[4].y);
+          mx = max3(mx, p[5].x, p[6].x); my = max3(my, p[5].y, p[6].y);
+          mx = fmaxf(mx, p[7].x); my = fmaxf(my, p[7].y);
+          const float2 rm = mul2(make_float2(mx, my), ivr);
+          if (rr & 1) {
+            bx = max3(bx, rprev.x, rm.x);
+            by = max3(by, rprev.y, rm.y);
+          } else {
+            rprev = rm;
+          }
+#pragma unroll
+          for (int k = 0; k < kDiags; ++k) {
             const int x = rr + k;
-            const float2 ra = mul2(mul2(cov[k], ci[x]), ivr);
-            const float2 rb = mul2(mul2(cov[k + 1], ci[x + 1]), ivr);
-            bx = max3(bx, ra.x, rb.x);
-            by = max3(by, ra.y, rb.y);
             cov[k] = fma2(make_float2(cf[x].x, cf[x].y), dgr, cov[k]);
             cov[k] = fma2(dfr, make_float2(cf[x].z, cf[x].w), cov[k]);
-            cov[k + 1] = fma2(make_float2(cf[x + 1].x, cf[x + 1].y), dgr, cov[k + 1]);
-            cov[k + 1] = fma2(dfr, make_float2(cf[x + 1].z, cf[x + 1].w), cov[k + 1]);
           }
         }
         ++n_steps;
         const bool trig = bx > tx || by > ty;
         const unsigned tmask = __ballot_sync(0xffffffffu, trig);
         if (tmask) {
+          // enqueue the triggered lanes in rank order, draining whenever the
+          // queue is full (warp-uniform loop)
           const int nt = __popc(tmask);
-          if (qn + nt > kQueue) {
-            n_verify += drain_queue(sm, cx, warp, qn, lane);
-            qn = 0;
-          }
-          if (trig) {
-            SlowItem& it = sm.queue[warp][qn + __popc(tmask & ((1u << lane) - 1u))];
+          const int rank = __popc(tmask & ((1u << lane) - 1u));
+          for (int done = 0; done < nt;) {
+            if (qn == kQueue) {
+              n_verify += drain_queue(sm, cx, warp, qn, lane);
+              qn = 0;
+            }
+            const int take = (nt - done) < (kQueue - qn) ? (nt - done) : (kQueue - qn);
+            if (trig && rank >= done && rank < done + take) {
+              SlowItem& it = sm.queue[warp][qn + rank - done];
 #pragma unroll
-            for (int k = 0; k < kDiags; ++k) it.cov[k] = cov[k];
-            it.vw = make_float2(vx, vy);
-            it.s = s;
-            it.owner = t;
+              for (int k = 0; k < kDiags; ++k) it.cov[k] = cov[k];
+              it.vw = make_float2(vx, vy);
+              it.s = s;
+              it.owner = t;
+            }
+            qn += take;
+            done += take;
           }
-          qn += nt;
           n_slow += trig ? 1 : 0;
         }
       }
