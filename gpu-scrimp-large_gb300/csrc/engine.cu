@@ -193,9 +193,19 @@ struct Workspace {
   std::vector<Buf> bufs;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t evk0 = nullptr, evk1 = nullptr;  // around the join kernel
+  cudaEvent_t evk0 = nullptr, evk1 = nullptr;  // around the join kernels
+  cudaEvent_t evkv = nullptr;                   // before the verification kernel
   bool timed_kernel = false;
+  bool timed_verify = false;
+  // Verification requests of the mixed 1NN join: capacity of the buffer, and
+  // the largest count a join asked for (the buffer grows to it on the next
+  // join; requests beyond the capacity are verified inline, more slowly).
+  int64_t vreq_cap = 0;
+  int64_t vreq_seen = 0;
 };
+
+constexpr int64_t kMinVerifyReqs = int64_t{1} << 22;
+constexpr int64_t kMaxVerifyReqs = int64_t{1} << 27;  // 2 GiB of requests
 
 Workspace g_ws[64];
 
@@ -224,7 +234,7 @@ enum Slot {
   S_T_B, S_MEAN_B, S_INV_B, S_DF_B, S_DG_B, S_INV32_B, S_DF32_B, S_DG32_B,
   S_KEY_A, S_KEY_B, S_SUM_A, S_SUM_B, S_PROF_A, S_PROF_B, S_CORR_A, S_CORR_B,
   S_PREFIX, S_COUNTER, S_T32_A, S_T32_B, S_BHI_A, S_BLO_A, S_MUREL_A,
-  S_BHI_B, S_BLO_B, S_MUREL_B,
+  S_BHI_B, S_BLO_B, S_MUREL_B, S_VREQ,
 };
 
 #define CUDA_TRY(expr)                                                     \
@@ -300,6 +310,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   int rc;
 
   ws.timed_kernel = false;
+  ws.timed_verify = false;
   CUDA_TRY(cudaEventRecord(ws.ev0, st));
 
   // ---- statistics ----
@@ -455,13 +466,29 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     P.band_unit_prefix = dprefix;
     P.unit_counter = static_cast<unsigned long long*>(p);
     P.counters = static_cast<unsigned long long*>(p) + 1;
-    P.error_flag = reinterpret_cast<int*>(static_cast<char*>(p) + 32);
+    P.error_flag = reinterpret_cast<int*>(static_cast<char*>(p) + 48);
+    if (kind == K_MIXED_1NN) {
+      // random-walk-like series ask for ~7 requests per window
+      int64_t want = std::max<int64_t>(kMinVerifyReqs, 16 * (nsz[0] + nsz[1]));
+      want = std::max<int64_t>(want, ws.vreq_seen + ws.vreq_seen / 4);
+      want = std::max<int64_t>(std::min<int64_t>(want, kMaxVerifyReqs), ws.vreq_cap);
+      void* q;
+      if ((rc = ensure(ws, S_VREQ, static_cast<size_t>(want) * sizeof(VerifyReq), &q, msg)))
+        return rc;
+      ws.vreq_cap = want;
+      P.vreq = static_cast<VerifyReq*>(q);
+      P.vreq_cap = want;
+    }
     const int64_t grid = std::min<int64_t>(resident, P.total_units);
     CUDA_TRY(cudaEventRecord(ws.evk0, st));
     ws.timed_kernel = true;
-    if (kind == K_MIXED_1NN)
+    if (kind == K_MIXED_1NN) {
       join_mixed_1nn_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
-    else if (kind == K_MIXED_SUM)
+      ++launches;
+      CUDA_TRY(cudaEventRecord(ws.evkv, st));
+      ws.timed_verify = true;
+      verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
+    } else if (kind == K_MIXED_SUM)
       join_mixed_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
     else
       join_fp64_kernel<<<static_cast<unsigned>(grid), nthreads, 0, st>>>(P);
@@ -492,21 +519,27 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
 void read_times(Workspace& ws, scamp_c_result* res) {
   res->steps = res->slow_steps = res->verifications = 0;
   if (ws.timed_kernel && ws.bufs.size() > S_COUNTER && ws.bufs[S_COUNTER].p) {
-    unsigned long long c[4] = {0, 0, 0, 0};
+    unsigned long long c[5] = {0, 0, 0, 0, 0};
     if (cudaMemcpy(c, ws.bufs[S_COUNTER].p, sizeof(c), cudaMemcpyDeviceToHost) == cudaSuccess) {
       res->steps = c[1];
       res->slow_steps = c[2];
       res->verifications = c[3];
+      ws.vreq_seen = std::max<int64_t>(ws.vreq_seen, static_cast<int64_t>(c[4]));
     }
   }
   float ms = 0;
   cudaEventElapsedTime(&ms, ws.ev0, ws.ev1);
   res->elapsed_ms = ms;
   res->join_kernel_ms = 0;
+  res->verify_kernel_ms = 0;
   if (ws.timed_kernel) {
     float k = 0;
     cudaEventElapsedTime(&k, ws.evk0, ws.evk1);
     res->join_kernel_ms = k;
+    if (ws.timed_verify) {
+      cudaEventElapsedTime(&k, ws.evkv, ws.evk1);
+      res->verify_kernel_ms = k;
+    }
   }
 }
 
@@ -530,6 +563,7 @@ int init_workspace(int device, Workspace** out, std::string* msg) {
     CUDA_TRY(cudaEventCreate(&ws.ev1));
     CUDA_TRY(cudaEventCreate(&ws.evk0));
     CUDA_TRY(cudaEventCreate(&ws.evk1));
+    CUDA_TRY(cudaEventCreate(&ws.evkv));
     ws.device = device;
   }
   *out = &ws;

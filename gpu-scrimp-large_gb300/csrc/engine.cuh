@@ -119,6 +119,14 @@ struct Problem {
 
 constexpr int kMaxProblems = 2;
 
+// A cell of the mixed 1NN join whose FP32 value is not trusted, settled after
+// the join by verify_requests_kernel.
+struct VerifyReq {
+  uint64_t i;   // row window | problem index << 62
+  uint32_t d;   // diagonal: column window = i + d
+  float ub;     // upper bound of the cell's r (FP32 value + margin)
+};
+
 // Everything a join kernel needs, passed by value.
 struct JoinParams {
   Problem prob[kMaxProblems];
@@ -127,7 +135,9 @@ struct JoinParams {
   int64_t total_bands;
   int64_t total_units;
   unsigned long long* unit_counter; // persistent work queue head
-  unsigned long long* counters;     // [steps, slow steps, verifications]
+  unsigned long long* counters;     // [steps, slow steps, verifications, requests]
+  VerifyReq* vreq;                  // verification requests (mixed 1NN)
+  int64_t vreq_cap;
   int* error_flag;                  // device error word (0 = ok)
   int64_t m;                        // window length
   int64_t seg_len;                  // K: rows per segment (two per unit)
@@ -178,6 +188,7 @@ __global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
 __global__ void join_fp64_kernel(JoinParams P);
 __global__ void join_mixed_kernel(JoinParams P);      // SUM_THRESH
 __global__ void join_mixed_1nn_kernel(JoinParams P);  // 1NN_INDEX
+__global__ void verify_requests_kernel(JoinParams P);
 
 __global__ void profile_to_keys_kernel(const uint64_t* __restrict__ in,
                                        uint64_t* __restrict__ keys, int64_t n,

@@ -53,7 +53,6 @@ constexpr int kYPad = (kYSpan / 8) * 10;              // padded: 10 pairs per 8
 // blocks hold >= 32 samples: the span plus the block after its end
 constexpr int kSpanBlk = kYSpan / 32 + 3;
 constexpr int kQueue = 16;                // queued blocks per warp
-constexpr int kVerify = 64;               // verification requests per warp
 constexpr float kEps = 5.9604645e-8f;     // 2^-24
 constexpr float kBoundC = 4.0f;
 constexpr float kTrust = 8e-6f;
@@ -113,16 +112,33 @@ __device__ __forceinline__ float key_corr_floor(u64 key, const KeyLayout& kl) {
 // sum cov^2 over the owner's diagonals plus the increment bound) and the
 // block's position.
 struct SlowItem {
-  float2 cov[kDiags];
+  float2 cov[kDiags];  // covariances after the item's last step
   float2 vw;
-  int s;      // step within the slab
+  int s;      // first step within the slab | number of steps (1 or 2) << 8
   int owner;  // thread index of the owner
+};
+
+// CTA-uniform context of the exact path, kept in shared memory.
+struct SlowCtx {
+  const Problem* pr;
+  int64_t rbase[2];
+  int64_t D0;  // first diagonal of the unit; thread t owns D0 + t*kDiags ..
+  int64_t m;
+  KeyLayout kl;
+  int prob;                        // index of the problem in JoinParams
+  VerifyReq* vreq;                 // deferred verification requests
+  unsigned long long* vcount;      // their count (may exceed vcap)
+  int64_t vcap;
 };
 
 struct Smem {
   union {
     struct {
-      float4 c_fg[kPad];  // {df.x, df.y, dg.x, dg.y} per staged column pair
+      // {df.x, df.y} and {dg.x, dg.y} per staged column pair: separate
+      // 8-byte arrays, so that 64-bit loads at a stride of 9 slots meet no
+      // bank conflict
+      float2 c_df[kPad];
+      float2 c_dg[kPad];
       float2 c_iv[kPad];  // {inv.x, inv.y}
     } s;
     struct {
@@ -142,17 +158,71 @@ struct Smem {
   float2 r_stepmax_iv[kSteps];
   float4 r_stepmax_fg[kSteps];
   SlowItem queue[kWarps][kQueue];
-  // cells to verify: rslot | cslot << 7 | segment << 18
-  uint32_t vreq[kWarps][kVerify];
-  int vcount[kWarps];
   Problem prob;  // the current unit's band problem
   long long unit, band, unit_in_band;
+  int prob_index;
+  SlowCtx cx;
 };
+
+// Filter-table entry: smallest best, largest inverse norm, largest |df|,
+// |dg| (per segment), over a set of columns or rows.
+struct TableEntry {
+  float2 mn, mx;
+  float4 mf;
+};
+
+// One column's or row's entry; a NaN inverse norm (window that cannot match)
+// counts as 0, as fmaxf against a 0 start would.
+__device__ __forceinline__ TableEntry table_entry(float4 f, float2 iv, float2 best) {
+  TableEntry e;
+  e.mn = best;
+  e.mx = make_float2(fmaxf(0.f, iv.x), fmaxf(0.f, iv.y));
+  e.mf = make_float4(fabsf(f.x), fabsf(f.y), fabsf(f.z), fabsf(f.w));
+  return e;
+}
+
+__device__ __forceinline__ void combine(TableEntry& a, const TableEntry& b) {
+  a.mn = make_float2(fminf(a.mn.x, b.mn.x), fminf(a.mn.y, b.mn.y));
+  a.mx = make_float2(fmaxf(a.mx.x, b.mx.x), fmaxf(a.mx.y, b.mx.y));
+  a.mf = make_float4(fmaxf(a.mf.x, b.mf.x), fmaxf(a.mf.y, b.mf.y),
+                     fmaxf(a.mf.z, b.mf.z), fmaxf(a.mf.w, b.mf.w));
+}
+
+// Reduces an entry over aligned groups of 8 lanes (whole warp active).
+__device__ __forceinline__ void reduce8(TableEntry& e) {
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) {
+    TableEntry x;
+    x.mn.x = __shfl_xor_sync(0xffffffffu, e.mn.x, o);
+    x.mn.y = __shfl_xor_sync(0xffffffffu, e.mn.y, o);
+    x.mx.x = __shfl_xor_sync(0xffffffffu, e.mx.x, o);
+    x.mx.y = __shfl_xor_sync(0xffffffffu, e.mx.y, o);
+    x.mf.x = __shfl_xor_sync(0xffffffffu, e.mf.x, o);
+    x.mf.y = __shfl_xor_sync(0xffffffffu, e.mf.y, o);
+    x.mf.z = __shfl_xor_sync(0xffffffffu, e.mf.z, o);
+    x.mf.w = __shfl_xor_sync(0xffffffffu, e.mf.w, o);
+    combine(e, x);
+  }
+}
+
+template <int P>
+struct Parity {
+  static constexpr int value = P;
+};
+
+static_assert(kSlab == kThreads, "one staged row per thread");
+static_assert(kCols % kThreads == 0, "whole warps stage the columns");
 
 // Four CTAs per SM: 4 x (shared memory + 1 KB reserved) within 228 KB.
 static_assert(sizeof(Smem) + 1024 <= 228 * 1024 / 4, "shared memory exceeds 4 CTAs/SM");
 
 __device__ __forceinline__ int padc(int c) { return c + (c >> 3); }
+
+// {df.x, df.y, dg.x, dg.y} of the staged column in padded slot `slot`.
+__device__ __forceinline__ float4 col_fg(const Smem& sm, int slot) {
+  const float2 a = sm.u.s.c_df[slot], b = sm.u.s.c_dg[slot];
+  return make_float4(a.x, a.y, b.x, b.y);
+}
 __device__ __forceinline__ int pady2(int x) { return x + (x >> 3) * 2; }
 
 // Offset of block b relative to block b0, as the float sum of the two
@@ -195,19 +265,39 @@ __device__ __forceinline__ float cov_part(const SeriesDev& R, const SeriesDev& C
   return acc;
 }
 
-// The whole covariance, one lane (used when a warp's request list is full).
+// The same covariance computed by a whole warp: lane l sums the terms
+// t = l, l + 32, ...; the partial sums meet in a shuffle reduction.
+__device__ __forceinline__ float verify_cov_warp(const SeriesDev& R, const SeriesDev& C,
+                                                 int64_t i, int64_t j, int64_t m, int lane) {
+  const int sh = R.bshift;
+  const int64_t bi = i >> sh, bj = j >> sh;
+  const float mri = R.mu_rel[i], mcj = C.mu_rel[j];
+  const float hr0 = R.bhi[bi], lr0 = R.blo[bi], hc0 = C.bhi[bj], lc0 = C.blo[bj];
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int64_t t0 = lane; t0 < m; t0 += 128) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t t = t0 + 32 * u;
+      if (t < m) {
+        const int64_t br = (i + t) >> sh, bc = (j + t) >> sh;
+        const float x = R.T32[i + t] + (((R.bhi[br] - hr0) + (R.blo[br] - lr0)) - mri);
+        const float y = C.T32[j + t] + (((C.bhi[bc] - hc0) + (C.blo[bc] - lc0)) - mcj);
+        acc[u] = fmaf(x, y, acc[u]);
+      }
+    }
+  }
+  float a = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  return a;
+}
+
+// The whole covariance, one lane (used when the request buffer is full).
 __device__ __noinline__ float verify_cov_lane(const SeriesDev& R, const SeriesDev& C,
                                               int64_t i, int64_t j, int64_t m) {
   return cov_part(R, C, i, j, 0, m);
 }
 
-struct SlowCtx {
-  const Problem* pr;
-  int64_t rbase[2];
-  int64_t D0;  // first diagonal of the unit; thread t owns D0 + t*kDiags ..
-  int64_t m;
-  KeyLayout kl;
-};
 
 __device__ __forceinline__ void publish(Smem& sm, const SlowCtx& cx, float rv, int64_t i,
                                         int64_t j, int rslot, int cslot, int g) {
@@ -229,103 +319,91 @@ __device__ __forceinline__ void publish(Smem& sm, const SlowCtx& cx, float rv, i
 }
 
 // Exact path of queued blocks, 16 lanes per block: lane (k, g) rewinds the
-// covariance of diagonal k, segment g to the start of the step, then walks
-// the step's 8 rows; every cell that may improve its row or column is
-// published with its FP32 value, or queued for verification when its margin
-// exceeds kTrust.  Two blocks per pass; then the warp verifies the queued
-// cells together.  Returns the number of verifications.
-__device__ __noinline__ int drain_queue(Smem& sm, const SlowCtx& cx, int warp, int count,
-                                        int lane) {
-  if (lane == 0) sm.vcount[warp] = 0;
+// covariance of diagonal k, segment g to the start of the block's first
+// step, then walks the block's rows (8 per step); every cell that may improve its row or column is
+// published with its FP32 value when its margin is within kTrust.  A cell
+// with a larger margin is published with the lower bound rv - margin (so the
+// filters rise at once) and appended to the verification requests, which
+// verify_requests_kernel settles after the join.  Two blocks per pass.
+// Returns the lane's number of requests.
+__device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane) {
   __syncwarp();  // the queue was written by other lanes
+  const SlowCtx& cx = sm.cx;
   const Problem& pr = *cx.pr;
   const int k = (lane & 15) >> 1, g = lane & 1;
+  int nreq = 0;
   for (int p = 0; p < count; p += 2) {
+    // every lane runs the pass (warp-wide request reservation); a lane
+    // without a block carries the first queued one and checks nothing
     const int item = p + (lane >> 4);
-    if (item < count) {
-      const SlowItem& it = sm.queue[warp][item];
-      float c = g ? it.cov[k].y : it.cov[k].x;
-      const float vw = g ? it.vw.y : it.vw.x;
-      const int r0 = it.s * kRows;
-      const int cb0 = 8 * (it.s + it.owner) + k;  // staged column at row 0
-#pragma unroll
-      for (int rr = kRows - 1; rr >= 0; --rr) {
-        const float4 rf = sm.r_fg[r0 + rr];
-        const float4 cf = sm.u.s.c_fg[padc(cb0 + rr)];
-        const float dfr = g ? rf.y : rf.x, dgr = g ? rf.w : rf.z;
-        const float dfc = g ? cf.y : cf.x, dgc = g ? cf.w : cf.z;
-        c = fmaf(-dfr, dgc, c);
-        c = fmaf(-dfc, dgr, c);
-      }
-      const float vk = kBoundC * kEps * sqrtf(kRows * vw);
+    const bool act = item < count;
+    const SlowItem& it = sm.queue[warp][act ? item : 0];
+    float c = g ? it.cov[k].y : it.cov[k].x;
+    const float vw = g ? it.vw.y : it.vw.x;
+    const int s0 = it.s & 255;
+    const int nrows = act ? kRows * (it.s >> 8) : 0;
+    // the two blocks of a pass may differ in length: the row loop below runs
+    // the longer length on every lane (its ballot needs the whole warp)
+    const int nrows_w = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(nrows)));
+    const int r0 = s0 * kRows;
+    const int cb0 = 8 * (s0 + it.owner) + k;  // staged column at row 0
+#pragma unroll 8
+    for (int rr = nrows - 1; rr >= 0; --rr) {
+      const float4 rf = sm.r_fg[r0 + rr];
+      const float4 cf = col_fg(sm, padc(cb0 + rr));
+      const float dfr = g ? rf.y : rf.x, dgr = g ? rf.w : rf.z;
+      const float dfc = g ? cf.y : cf.x, dgc = g ? cf.w : cf.z;
+      c = fmaf(-dfr, dgc, c);
+      c = fmaf(-dfc, dgr, c);
+    }
+    const float vk = kBoundC * kEps * sqrtf(kRows * vw);
 #pragma unroll 1
-      for (int rr = 0; rr < kRows; ++rr) {
-        const int cs = cb0 + rr;
-        const float4 rf = sm.r_fg[r0 + rr];
-        const float4 cf = sm.u.s.c_fg[padc(cs)];
-        const float2 ivr2 = sm.r_iv[r0 + rr];
-        const float2 ivc2 = sm.u.s.c_iv[padc(cs)];
-        const float ivr = g ? ivr2.y : ivr2.x, ivc = g ? ivc2.y : ivc2.x;
-        const float rv = (c * ivc) * ivr;  // the fast path's rounding
-        const float mk = vk * ivc * ivr;
-        const float rb = g ? sm.r_best[r0 + rr].y : sm.r_best[r0 + rr].x;
-        const float cbv = g ? sm.c_best[cs].y : sm.c_best[cs].x;
-        if (rv + mk > fminf(rb, cbv)) {
-          const int64_t i = cx.rbase[g] + r0 + rr;
-          const int64_t j = i + cx.D0 + it.owner * kDiags + k;
-          if (mk > kTrust) {
-            const int slot = atomicAdd(&sm.vcount[warp], 1);
-            if (slot < kVerify) {
-              sm.vreq[warp][slot] = static_cast<uint32_t>(r0 + rr) |
-                                    (static_cast<uint32_t>(cs) << 7) |
-                                    (static_cast<uint32_t>(g) << 18);
-            } else {
-              publish(sm, cx, verify_cov_lane(pr.R, pr.C, i, j, cx.m) * ivc * ivr, i, j,
-                      r0 + rr, cs, g);
-            }
-          } else {
-            publish(sm, cx, rv, i, j, r0 + rr, cs, g);
-          }
-        }
-        const float dfr = g ? rf.y : rf.x, dgr = g ? rf.w : rf.z;
-        const float dfc = g ? cf.y : cf.x, dgc = g ? cf.w : cf.z;
-        c = fmaf(dfc, dgr, c);
-        c = fmaf(dfr, dgc, c);
-      }
-    }
-  }
-  __syncwarp();
-  // Verification, four cells at a time: 8 lanes per cell, each summing a
-  // contiguous eighth of the window, so that the loads of 4 cells are in
-  // flight together.
-  const int nreq = sm.vcount[warp];
-  const int nv = nreq < kVerify ? nreq : kVerify;
-  const int sub = lane & 7;
-  const int64_t L = (cx.m + 7) >> 3;
-  for (int q0 = 0; q0 < nv; q0 += 4) {
-    const int q = q0 + (lane >> 3);
-    float part = 0.f;
-    int rs = 0, cs = 0, g = 0;
-    int64_t i = 0, j = 0;
-    if (q < nv) {
-      const uint32_t rq = sm.vreq[warp][q];
-      rs = static_cast<int>(rq & 127u);
-      cs = static_cast<int>((rq >> 7) & 2047u);
-      g = static_cast<int>(rq >> 18);
-      i = cx.rbase[g] + rs;
-      j = i + cx.D0 + (cs - rs);
-      const int64_t tb = sub * L;
-      const int64_t te = tb + L < cx.m ? tb + L : cx.m;
-      part = cov_part(pr.R, pr.C, i, j, tb, te);
-    }
-    part += __shfl_xor_sync(0xffffffffu, part, 4);
-    part += __shfl_xor_sync(0xffffffffu, part, 2);
-    part += __shfl_xor_sync(0xffffffffu, part, 1);
-    if (q < nv && sub == 0) {
-      const float2 ivr2 = sm.r_iv[rs];
+    for (int rw = 0; rw < nrows_w; ++rw) {
+      const bool live = rw < nrows;
+      const int rr = live ? rw : 0;  // rows past the block's end read row 0
+      const int cs = cb0 + rr;
+      const float4 rf = sm.r_fg[r0 + rr];
+      const float4 cf = col_fg(sm, padc(cs));
+      const float2 ivr2 = sm.r_iv[r0 + rr];
       const float2 ivc2 = sm.u.s.c_iv[padc(cs)];
-      const float f = g ? ivc2.y * ivr2.y : ivc2.x * ivr2.x;
-      publish(sm, cx, part * f, i, j, rs, cs, g);
+      const float ivr = g ? ivr2.y : ivr2.x, ivc = g ? ivc2.y : ivc2.x;
+      const float rv = (c * ivc) * ivr;  // the fast path's rounding
+      const float mk = vk * ivc * ivr;
+      const float rb = g ? sm.r_best[r0 + rr].y : sm.r_best[r0 + rr].x;
+      const float cbv = g ? sm.c_best[cs].y : sm.c_best[cs].x;
+      const bool cand = live && rv + mk > fminf(rb, cbv);
+      const bool req = cand && mk > kTrust;
+      const unsigned rmask = __ballot_sync(0xffffffffu, req);
+      unsigned long long slot = 0;
+      if (rmask) {
+        const int leader = __ffs(rmask) - 1;
+        if (lane == leader) slot = atomicAdd(cx.vcount, static_cast<unsigned long long>(__popc(rmask)));
+        slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(rmask & ((1u << lane) - 1u));
+      }
+      if (cand) {
+        const int64_t i = cx.rbase[g] + r0 + rr;
+        const int64_t j = i + cx.D0 + it.owner * kDiags + k;
+        if (req) {
+          ++nreq;
+          if (slot < static_cast<unsigned long long>(cx.vcap)) {
+            publish(sm, cx, rv - mk, i, j, r0 + rr, cs, g);
+            VerifyReq q;
+            q.i = static_cast<uint64_t>(i) | (static_cast<uint64_t>(cx.prob) << 62);
+            q.d = static_cast<uint32_t>(j - i);
+            q.ub = rv + mk;
+            cx.vreq[slot] = q;
+          } else {
+            publish(sm, cx, verify_cov_lane(pr.R, pr.C, i, j, cx.m) * ivc * ivr, i, j,
+                    r0 + rr, cs, g);
+          }
+        } else {
+          publish(sm, cx, rv, i, j, r0 + rr, cs, g);
+        }
+      }
+      const float dfr = g ? rf.y : rf.x, dgr = g ? rf.w : rf.z;
+      const float dfc = g ? cf.y : cf.x, dgc = g ? cf.w : cf.z;
+      c = fmaf(dfc, dgr, c);
+      c = fmaf(dfr, dgc, c);
     }
   }
   __syncwarp();
@@ -356,6 +434,7 @@ join_mixed_1nn_kernel(JoinParams P) {
         int64_t bb, ubb;
         decode_unit(P, uu, &pi, &bb, &ubb);
         sm.prob = P.prob[pi];
+        sm.prob_index = pi;
         sm.band = bb;
         sm.unit_in_band = ubb;
       }
@@ -523,11 +602,18 @@ join_mixed_1nn_kernel(JoinParams P) {
     }
     float2 W = make_float2(0.f, 0.f);
 
-    SlowCtx cx;
-    cx.pr = &pr;
-    cx.D0 = D0;
-    cx.m = m;
-    cx.kl = P.kl;
+    if (t == 0) {
+      // read by the exact path only after the slab's first barrier
+      SlowCtx& cx = sm.cx;
+      cx.pr = &sm.prob;
+      cx.D0 = D0;
+      cx.m = m;
+      cx.kl = P.kl;
+      cx.prob = sm.prob_index;
+      cx.vreq = P.vreq;
+      cx.vcount = P.counters + 3;
+      cx.vcap = P.vreq_cap;
+    }
 
     // ---------------- slabs ----------------
     const int64_t nslabs = (seg_len[0] + kSlab - 1) / kSlab;
@@ -538,11 +624,13 @@ join_mixed_1nn_kernel(JoinParams P) {
         rbase[g] = seg_row[g] + q * kSlab;
         rend[g] = seg_row[g] + seg_len[g];
         cbase_g[g] = rbase[g] + D0;
-        cx.rbase[g] = rbase[g];
+        if (t == 0) sm.cx.rbase[g] = rbase[g];
       }
       // Staging, coalesced: thread t stages columns t, t + kThreads, ... and
-      // row t; then the per-block and per-step filter tables are built from
-      // shared memory.
+      // row t.  The filter tables are reduced on the way, 8 lanes (8
+      // consecutive columns or rows) at a time: per 8-column block and per
+      // 8-row step the smallest best, the largest inverse norm and the
+      // largest |df|, |dg|.
 #pragma unroll 3
       for (int c = t; c < kCols; c += kThreads) {
         const int64_t j0 = cbase_g[0] + c, j1 = cbase_g[1] + c;
@@ -559,11 +647,20 @@ join_mixed_1nn_kernel(JoinParams P) {
         float2 cbv;
         cbv.x = (pr.key_col && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_col[j0], P.kl) : kNoTarget;
         cbv.y = (pr.key_col && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_col[j1], P.kl) : kNoTarget;
-        sm.u.s.c_fg[padc(c)] = f;
+        sm.u.s.c_df[padc(c)] = make_float2(f.x, f.y);
+        sm.u.s.c_dg[padc(c)] = make_float2(f.z, f.w);
         sm.u.s.c_iv[padc(c)] = iv;
         sm.c_best[c] = cbv;
+        TableEntry e = table_entry(f, iv, cbv);
+        reduce8(e);
+        if ((lane & 7) == 0) {
+          sm.c_blkmin[c >> 3] = e.mn;
+          sm.c_blkmax_iv[c >> 3] = e.mx;
+          sm.c_blkmax_fg[c >> 3] = e.mf;
+        }
       }
-      for (int r = t; r < kSlab; r += kThreads) {
+      {
+        const int r = t;  // kSlab == kThreads
         const int64_t i0 = rbase[0] + r, i1 = rbase[1] + r;
         const bool ok0 = i0 < rend[0], ok1 = i1 < rend[1];
         float4 f;
@@ -578,55 +675,68 @@ join_mixed_1nn_kernel(JoinParams P) {
         sm.r_fg[r] = f;
         sm.r_iv[r] = iv;
         sm.r_best[r] = rbv;
+        TableEntry e = table_entry(f, iv, rbv);
+        reduce8(e);
+        if ((lane & 7) == 0) {
+          sm.r_stepmin[r >> 3] = e.mn;
+          sm.r_stepmax_iv[r >> 3] = e.mx;
+          sm.r_stepmax_fg[r >> 3] = e.mf;
+        }
       }
       __syncthreads();
-      for (int b = t; b < kBlocks; b += kThreads) {
-        float2 mn = make_float2(kNoTarget, kNoTarget), mx = make_float2(0.f, 0.f);
-        float4 mf = make_float4(0.f, 0.f, 0.f, 0.f);
+      // Column tables over 16 columns: a step of thread t reads the 15
+      // columns from 8(s + t), entry s + t = blocks s + t and s + t + 1.
+      {
+        TableEntry e[2];
 #pragma unroll
-        for (int x = 0; x < 8; ++x) {
-          const int c = 8 * b + x;
-          const float4 f = sm.u.s.c_fg[padc(c)];
-          const float2 iv = sm.u.s.c_iv[padc(c)];
-          const float2 cbv = sm.c_best[c];
-          mn.x = fminf(mn.x, cbv.x); mn.y = fminf(mn.y, cbv.y);
-          mx.x = fmaxf(mx.x, iv.x); mx.y = fmaxf(mx.y, iv.y);
-          mf.x = fmaxf(mf.x, fabsf(f.x)); mf.y = fmaxf(mf.y, fabsf(f.y));
-          mf.z = fmaxf(mf.z, fabsf(f.z)); mf.w = fmaxf(mf.w, fabsf(f.w));
+        for (int h = 0; h < 2; ++h) {
+          const int b = t + h * kThreads;
+          if (b < kBlocks) {
+            e[h].mn = sm.c_blkmin[b];
+            e[h].mx = sm.c_blkmax_iv[b];
+            e[h].mf = sm.c_blkmax_fg[b];
+            if (b + 1 < kBlocks) {
+              TableEntry o;
+              o.mn = sm.c_blkmin[b + 1];
+              o.mx = sm.c_blkmax_iv[b + 1];
+              o.mf = sm.c_blkmax_fg[b + 1];
+              combine(e[h], o);
+            }
+          }
         }
-        sm.c_blkmin[b] = mn;
-        sm.c_blkmax_iv[b] = mx;
-        sm.c_blkmax_fg[b] = mf;
-      }
-      if (t < kSteps) {
-        float2 mn = make_float2(kNoTarget, kNoTarget), mx = make_float2(0.f, 0.f);
-        float4 mf = make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
 #pragma unroll
-        for (int x = 0; x < kRows; ++x) {
-          const int r = t * kRows + x;
-          const float4 f = sm.r_fg[r];
-          const float2 iv = sm.r_iv[r];
-          const float2 rbv = sm.r_best[r];
-          mn.x = fminf(mn.x, rbv.x); mn.y = fminf(mn.y, rbv.y);
-          mx.x = fmaxf(mx.x, iv.x); mx.y = fmaxf(mx.y, iv.y);
-          mf.x = fmaxf(mf.x, fabsf(f.x)); mf.y = fmaxf(mf.y, fabsf(f.y));
-          mf.z = fmaxf(mf.z, fabsf(f.z)); mf.w = fmaxf(mf.w, fabsf(f.w));
+        for (int h = 0; h < 2; ++h) {
+          const int b = t + h * kThreads;
+          if (b < kBlocks) {
+            sm.c_blkmin[b] = e[h].mn;
+            sm.c_blkmax_iv[b] = e[h].mx;
+            sm.c_blkmax_fg[b] = e[h].mf;
+          }
         }
-        sm.r_stepmin[t] = mn;
-        sm.r_stepmax_iv[t] = mx;
-        sm.r_stepmax_fg[t] = mf;
       }
       __syncthreads();
 
       // ---------------- steps ----------------
-#pragma unroll 1
-      for (int s = 0; s < kSteps; ++s) {
+      // Steps run in pairs.  The thread's column window is carried from the
+      // first step of a pair to the second (the last 7 columns of step s are
+      // the first 7 of step s + 1): column x of step s sits in slot
+      // (8 * (s & 1) + x) & 15, so every slot index is a constant.  The exact
+      // path runs only between pairs: a step whose trigger finds the warp's
+      // queue full is recorded in `pend` and queued after the pair as a
+      // two-step (or one-step) block.
+      float4 cfw[16];
+      float2 ciw[16];
+      int pend = -1;
+      float2 vlast = make_float2(0.f, 0.f);
+      auto step = [&](const int s, auto parity) {
+        constexpr int P = decltype(parity)::value;
         const int r0 = s * kRows;
         const int base = 9 * (s + t);  // padded slot of staged column 8(s+t)
         // filter threshold and margin
-        const float2 bm0 = sm.c_blkmin[s + t], bm1 = sm.c_blkmin[s + t + 1];
+        const float2 bm = sm.c_blkmin[s + t];
         const float2 rsm = sm.r_stepmin[s];
-        const float2 ic0 = sm.c_blkmax_iv[s + t], ic1 = sm.c_blkmax_iv[s + t + 1];
+        const float2 icm = sm.c_blkmax_iv[s + t];
         const float2 irm = sm.r_stepmax_iv[s];
         {
           const float2 cm = absmax8(cov);
@@ -634,49 +744,39 @@ join_mixed_1nn_kernel(JoinParams P) {
         }
         {
           // bound of |df_c dg_r| + |df_r dg_c| over the step's cells
-          const float4 cf0 = sm.c_blkmax_fg[s + t], cf1 = sm.c_blkmax_fg[s + t + 1];
+          const float4 cfm = sm.c_blkmax_fg[s + t];
           const float4 rfm = sm.r_stepmax_fg[s];
-          const float2 cdf = make_float2(fmaxf(cf0.x, cf1.x), fmaxf(cf0.y, cf1.y));
-          const float2 cdg = make_float2(fmaxf(cf0.z, cf1.z), fmaxf(cf0.w, cf1.w));
-          const float2 inc = fma2(make_float2(rfm.x, rfm.y), cdg,
-                                  mul2(make_float2(rfm.z, rfm.w), cdf));
+          const float2 inc = fma2(make_float2(rfm.x, rfm.y), make_float2(cfm.z, cfm.w),
+                                  mul2(make_float2(rfm.z, rfm.w), make_float2(cfm.x, cfm.y)));
           W = fma2(inc, inc, W);
         }
         const float vx = Vt.x + W.x, vy = Vt.y + W.y;
-        const float tx = fminf(fminf(bm0.x, bm1.x), rsm.x) -
-                         kBoundC * kEps * sqrtf(kRows * vx) * fmaxf(ic0.x, ic1.x) * irm.x;
-        const float ty = fminf(fminf(bm0.y, bm1.y), rsm.y) -
-                         kBoundC * kEps * sqrtf(kRows * vy) * fmaxf(ic0.y, ic1.y) * irm.y;
+        const float tx = fminf(bm.x, rsm.x) - kBoundC * kEps * sqrtf(kRows * vx) * icm.x * irm.x;
+        const float ty = fminf(bm.y, rsm.y) - kBoundC * kEps * sqrtf(kRows * vy) * icm.y * irm.y;
 
         // fast path: recurrence + block maximum
         float bx = -3.f, by = -3.f;
         float2 rprev;
-        float4 cf[kDiags + kRows - 1];
-        float2 ci[kDiags + kRows - 1];
-#pragma unroll
-        for (int x = 0; x < kDiags; ++x) {
-          cf[x] = sm.u.s.c_fg[base + x + (x >> 3)];
-          ci[x] = sm.u.s.c_iv[base + x + (x >> 3)];
-        }
 #pragma unroll
         for (int rr = 0; rr < kRows; ++rr) {
-          if (rr > 0) {
+          {
             const int x = rr + kDiags - 1;
-            cf[x] = sm.u.s.c_fg[base + x + (x >> 3)];
-            ci[x] = sm.u.s.c_iv[base + x + (x >> 3)];
+            cfw[(8 * P + x) & 15] = col_fg(sm, base + x + (x >> 3));
+            ciw[(8 * P + x) & 15] = sm.u.s.c_iv[base + x + (x >> 3)];
           }
           const float4 rf = sm.r_fg[r0 + rr];
           const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
           const float2 ivr = sm.r_iv[r0 + rr];
           // the row's largest cov * inv_c, times inv_r (> 0): the largest r
           // of the row, rounded exactly as (cov * inv_c) * inv_r per cell
-          float2 p[kDiags];
+          float mx = -3.f, my = -3.f;
 #pragma unroll
-          for (int k = 0; k < kDiags; ++k) p[k] = mul2(cov[k], ci[rr + k]);
-          float mx = max3(p[0].x, p[1].x, p[2].x), my = max3(p[0].y, p[1].y, p[2].y);
-          mx = max3(mx, p[3].x, p[4].x); my = max3(my, p[3].y, p[4].y);
-          mx = max3(mx, p[5].x, p[6].x); my = max3(my, p[5].y, p[6].y);
-          mx = fmaxf(mx, p[7].x); my = fmaxf(my, p[7].y);
+          for (int k = 0; k < kDiags; k += 2) {
+            const float2 pa = mul2(cov[k], ciw[(8 * P + rr + k) & 15]);
+            const float2 pb = mul2(cov[k + 1], ciw[(8 * P + rr + k + 1) & 15]);
+            mx = max3(mx, pa.x, pb.x);
+            my = max3(my, pa.y, pb.y);
+          }
           const float2 rm = mul2(make_float2(mx, my), ivr);
           if (rr & 1) {
             bx = max3(bx, rprev.x, rm.x);
@@ -686,43 +786,69 @@ join_mixed_1nn_kernel(JoinParams P) {
           }
 #pragma unroll
           for (int k = 0; k < kDiags; ++k) {
-            const int x = rr + k;
-            cov[k] = fma2(make_float2(cf[x].x, cf[x].y), dgr, cov[k]);
-            cov[k] = fma2(dfr, make_float2(cf[x].z, cf[x].w), cov[k]);
+            const float4 c4 = cfw[(8 * P + rr + k) & 15];
+            cov[k] = fma2(make_float2(c4.x, c4.y), dgr, cov[k]);
+            cov[k] = fma2(dfr, make_float2(c4.z, c4.w), cov[k]);
           }
         }
-        ++n_steps;
         const bool trig = bx > tx || by > ty;
         const unsigned tmask = __ballot_sync(0xffffffffu, trig);
         if (tmask) {
-          // enqueue the triggered lanes in rank order, draining whenever the
-          // queue is full (warp-uniform loop)
-          const int nt = __popc(tmask);
+          // queue the triggered lanes in rank order while there is room
           const int rank = __popc(tmask & ((1u << lane) - 1u));
-          for (int done = 0; done < nt;) {
-            if (qn == kQueue) {
-              n_verify += drain_queue(sm, cx, warp, qn, lane);
-              qn = 0;
-            }
-            const int take = (nt - done) < (kQueue - qn) ? (nt - done) : (kQueue - qn);
-            if (trig && rank >= done && rank < done + take) {
-              SlowItem& it = sm.queue[warp][qn + rank - done];
+          if (trig) {
+            if (qn + rank < kQueue) {
+              SlowItem& it = sm.queue[warp][qn + rank];
 #pragma unroll
               for (int k = 0; k < kDiags; ++k) it.cov[k] = cov[k];
               it.vw = make_float2(vx, vy);
-              it.s = s;
+              it.s = s | (1 << 8);
+              it.owner = t;
+            } else if (pend < 0) {
+              pend = s;
+            }
+          }
+          const int nq = qn + __popc(tmask);
+          qn = nq < kQueue ? nq : kQueue;
+          n_slow += trig ? 1u : 0u;
+        }
+        vlast = make_float2(vx, vy);
+      };
+#pragma unroll 1
+      for (int s = 0; s < kSteps; s += 2) {
+#pragma unroll
+        for (int x = 0; x < kDiags - 1; ++x) {
+          cfw[x] = col_fg(sm, 9 * (s + t) + x);  // padc(8(s + t) + x), x < 8
+          ciw[x] = sm.u.s.c_iv[9 * (s + t) + x];
+        }
+        step(s, Parity<0>());
+        step(s + 1, Parity<1>());
+        // between pairs: drain a half-full queue (every queue at the slab's
+        // end), then queue and drain the steps that found it full
+        const unsigned pmask = __ballot_sync(0xffffffffu, pend >= 0);
+        if (pmask || qn >= kQueue / 2 || (qn && s + 2 == kSteps)) {
+          if (qn) {
+            n_verify += drain_queue(sm, warp, qn, lane);
+            qn = 0;
+          }
+          const int np = __popc(pmask);
+          const int rank = __popc(pmask & ((1u << lane) - 1u));
+          for (int done = 0; done < np; done += kQueue) {
+            if (pend >= 0 && rank >= done && rank < done + kQueue) {
+              SlowItem& it = sm.queue[warp][rank - done];
+#pragma unroll
+              for (int k = 0; k < kDiags; ++k) it.cov[k] = cov[k];
+              it.vw = vlast;
+              it.s = pend | ((s + 2 - pend) << 8);
               it.owner = t;
             }
-            qn += take;
-            done += take;
+            const int take = (np - done) < kQueue ? (np - done) : kQueue;
+            n_verify += drain_queue(sm, warp, take, lane);
           }
-          n_slow += trig ? 1 : 0;
+          pend = -1;
         }
       }
-      if (qn) {
-        n_verify += drain_queue(sm, cx, warp, qn, lane);
-        qn = 0;
-      }
+      n_steps += kSteps;
       __syncthreads();
     }
   }
@@ -731,11 +857,45 @@ join_mixed_1nn_kernel(JoinParams P) {
   for (int o = 16; o > 0; o >>= 1) {
     n_steps += __shfl_xor_sync(0xffffffffu, n_steps, o);
     n_slow += __shfl_xor_sync(0xffffffffu, n_slow, o);
+    n_verify += __shfl_xor_sync(0xffffffffu, n_verify, o);
   }
   if (lane == 0 && P.counters) {
     atomicAdd(P.counters + 0, n_steps);
     atomicAdd(P.counters + 1, n_slow);
     atomicAdd(P.counters + 2, n_verify);
+  }
+}
+
+// Settles the verification requests of join_mixed_1nn_kernel, one warp per
+// cell.  A request whose upper bound rv + margin no longer exceeds the
+// current best of its row or column cannot change the profile and is
+// skipped; otherwise the cell's covariance is computed directly from the
+// FP32 series copies (each factor centred per window) and its r merged into
+// both profiles.  Runs after the join on the same stream; the request count
+// is read on the device.
+__global__ void __launch_bounds__(256)
+verify_requests_kernel(JoinParams P) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long total = P.counters[3];
+  const int64_t n = total < static_cast<unsigned long long>(P.vreq_cap)
+                        ? static_cast<int64_t>(total) : P.vreq_cap;
+  const int64_t nwarps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t w = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+       w < n; w += nwarps) {
+    const VerifyReq rq = P.vreq[w];
+    const Problem& pr = P.prob[rq.i >> 62];
+    const int64_t i = static_cast<int64_t>(rq.i & ((uint64_t{1} << 62) - 1));
+    const int64_t j = i + rq.d;
+    const bool row_open = pr.key_row && rq.ub > key_corr_floor(pr.key_row[i], P.kl);
+    const bool col_open = pr.key_col && rq.ub > key_corr_floor(pr.key_col[j], P.kl);
+    if (!row_open && !col_open) continue;
+    const float cv = verify_cov_warp(pr.R, pr.C, i, j, P.m, lane);
+    if (lane == 0) {
+      const float rv = (cv * pr.C.inv32[j]) * pr.R.inv32[i];
+      const uint64_t q = q_from_float_bits(__float_as_uint(rv), P.kl.frac_bits);
+      if (row_open) atomicMax(reinterpret_cast<u64*>(pr.key_row + i), make_key(q, j, P.kl));
+      if (col_open) atomicMax(reinterpret_cast<u64*>(pr.key_col + j), make_key(q, i, P.kl));
+    }
   }
 }
 

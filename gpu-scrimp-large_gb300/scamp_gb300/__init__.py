@@ -179,7 +179,8 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
     out["comparisons"] = int(res.comparisons)
     out["gpu_launches"] = int(res.gpu_launches)
     out["counters"] = {"steps": int(res.steps), "slow_steps": int(res.slow_steps),
-                       "verifications": int(res.verifications)}
+                       "verifications": int(res.verifications),
+                       "verify_kernel_ms": float(res.verify_kernel_ms)}
     return out
 
 
@@ -211,7 +212,8 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
     _check(rc, err)
     return {"elapsed_ms": res.elapsed_ms, "join_kernel_ms": res.join_kernel_ms,
             "counters": {"steps": int(res.steps), "slow_steps": int(res.slow_steps),
-                         "verifications": int(res.verifications)},
+                         "verifications": int(res.verifications),
+                         "verify_kernel_ms": float(res.verify_kernel_ms)},
             "comparisons": int(res.comparisons),
             "gpu_launches": int(res.gpu_launches)}
 

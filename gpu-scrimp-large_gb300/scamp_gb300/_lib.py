@@ -86,7 +86,7 @@ class CResult(ctypes.Structure):
         ("steps", ctypes.c_uint64),
         ("slow_steps", ctypes.c_uint64),
         ("verifications", ctypes.c_uint64),
-        ("reserved", ctypes.c_uint32 * 2),
+        ("verify_kernel_ms", ctypes.c_double),
     ]
 
 

@@ -91,17 +91,19 @@ typedef struct scamp_c_result {
   double *corr_b;       /* optional */
   /* Filled by the engine. */
   double elapsed_ms;    /* device time of the join (stats .. final profile) */
-  double join_kernel_ms;/* device time of the join kernel alone */
+  double join_kernel_ms;/* device time of the join kernels (the band kernel,
+                         * then, in the mixed 1NN form, the verification of
+                         * deferred candidates) */
   uint64_t comparisons; /* distance-matrix cells evaluated */
   uint32_t gpu_launches;/* kernels launched by this call */
   uint32_t reserved0;
   /* Work counters of the mixed 1NN_INDEX form (0 otherwise): 8-row steps
    * of one thread, steps recomputed on the exact path, and candidate cells
-   * verified by a direct dot product. */
+   * sent to verification by a direct dot product. */
   uint64_t steps;
   uint64_t slow_steps;
   uint64_t verifications;
-  uint32_t reserved[2];
+  double verify_kernel_ms; /* part of join_kernel_ms: deferred verification */
 } scamp_c_result;
 
 /* Runs one join.  Inputs and results are HOST memory; the engine copies them
