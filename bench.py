@@ -42,7 +42,14 @@ WORKLOAD = ("AB-join: A = random walk 2^20, B = random walk 2^19, 64 planted sin
 NA, NB, M = 1 << 20, 1 << 19, 256
 # CPU sample: the same distributions, A[:2^17] x B[:2^16], both directions.
 CPU_NA, CPU_NB = 1 << 17, 1 << 16
-OPS_PER_CELL = 4  # FMA-pipe operations per comparison: 2 FMA + 2 MUL
+# Algorithmic work per comparison: 2 FMA (covariance update) + 2 MUL
+# (r = cov * inv_c * inv_r), counted on the FMA pipe.
+OPS_PER_CELL = 4
+# DRAM bytes (read + write) of one launch of the mixed join kernel on this
+# workload: one single-pass ncu capture of the full-size launch
+# (profiles/join_mixed_1nn_cfg2.txt).  Mostly the verification requests and
+# profile atomics: the series, statistics and profiles stay in the 129 MB L2.
+DRAM_BYTES_PER_LAUNCH = 55.54e6 + 127.96e6
 
 
 def dist_env():
@@ -234,12 +241,13 @@ def main():
         one("mixed")
     barrier()
     torch.cuda.synchronize()
-    times, kernel_ms, launches = [], [], 0
+    times, kernel_ms, verify_ms, launches = [], [], [], 0
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             ms, r = one("mixed")
             times.append(ms)
-            kernel_ms.append(r["join_kernel_ms"])
+            kernel_ms.append(r["join_kernel_ms"] - r["counters"]["verify_kernel_ms"])
+            verify_ms.append(r["counters"]["verify_kernel_ms"])
             launches += r["gpu_launches"]
     torch.cuda.synchronize()
     barrier()
@@ -340,9 +348,13 @@ def main():
                               "frac": achieved64 / peak64, "peak_source": "measured DFMA probe"}},
         "speedup_mixed_vs_fp64": (sum(fp64_ms) / len(fp64_ms)) / ms_step,
         "roofline": {"bound": "fp32_fma_pipe", "achieved": achieved / 1e12, "peak": peak32 / 1e12,
-                     "unit": "Tops/s", "frac": achieved / peak32, "traffic": None,
-                     "kernel": "join_mixed_kernel", "kernel_ms": k_ms,
+                     "unit": "Tops/s", "frac": achieved / peak32,
+                     "traffic": DRAM_BYTES_PER_LAUNCH if NA == 1 << 20 else None,
+                     "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
+                     "kernel": "join_mixed_1nn_kernel", "kernel_ms": k_ms,
                      "ops_per_comparison": OPS_PER_CELL,
+                     "verify_kernel_ms": sum(verify_ms) / len(verify_ms),
+                     "work_counters": r["counters"],
                      "peak_source": "measured packed-FP32 FMA probe (scamp_gb300_pipe_peak)"},
         "e2e": {"value": cells * world / e2e_s, "unit": "comparisons/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

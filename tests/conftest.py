@@ -9,6 +9,7 @@ for p in (os.path.join(REPO, "gpu-scrimp-large_gb300"), os.path.join(REPO, "orac
     if p not in sys.path:
         sys.path.insert(0, p)
 
+PKG_DIR = os.path.join(REPO, "gpu-scrimp-large_gb300", "scamp_gb300")
 REFERENCE_TREE = "/root/reference"
 
 
