@@ -701,3 +701,283 @@ extern "C" int scamp_gb300_join(const scamp_c_args* args, scamp_c_result* res,
   return SCAMP_OK;
 #undef HOST_CUDA
 }
+
+// ---------------------------------------------------------------------------
+// Join without allocation (scamp_gb300_join_dev_noalloc).
+//
+// Some callers cannot let the engine allocate device memory at join time: a
+// host whose device memory is all handed to its own pool before any work
+// starts, or a loop that must never wait on the allocator (cudaMalloc and
+// cudaFree can synchronise the whole device and stall every other stream).
+// For them this entry runs the FP64 join with every intermediate buffer
+// (statistics, merge keys, the work-queue prefix and counters) carved from
+// one static device array, so that nothing is allocated per call.  The array
+// bounds each series to kNoAllocMaxSamples samples.
+// ---------------------------------------------------------------------------
+namespace scamp_gb300 {
+namespace {
+
+constexpr int64_t kNoAllocMaxSamples = int64_t{1} << 16;
+constexpr int64_t kNoAllocPrefixCap = 1024;   // band prefix entries
+constexpr size_t kNoAllocAlign = 256;
+
+constexpr size_t noalloc_round(size_t b) { return (b + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
+// One series: T (8n), mean/inv/df/dg (4 x 8n), inv32/df32/dg32 (3 x 4n),
+// T32 (4n), bhi/blo (2 x 4 x (n/32 + 1)), mu_rel (4n); windows <= samples.
+constexpr size_t noalloc_series_bytes(int64_t n) {
+  return noalloc_round(8 * n) + 4 * noalloc_round(8 * n) + 3 * noalloc_round(4 * n) +
+         noalloc_round(4 * n) + 2 * noalloc_round(4 * (n / 32 + 1)) + noalloc_round(4 * n);
+}
+// counters (64 B, zeroed per call) | band prefix | two merge-key arrays | series A | series B
+constexpr size_t kNoAllocScratchBytes =
+    noalloc_round(64) + noalloc_round(8 * kNoAllocPrefixCap) +
+    2 * noalloc_round(8 * kNoAllocMaxSamples) + 2 * noalloc_series_bytes(kNoAllocMaxSamples);
+
+// About 8.6 MB per device, reserved when the module is loaded on it.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+struct NoAllocDevice {
+  unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch
+  int sms = 0;
+};
+NoAllocDevice g_noalloc_dev[64];
+std::mutex g_noalloc_mu;
+
+// Once per device, with that device current: the scratch's device address
+// and the SM count.  The first call on a device therefore makes runtime
+// calls (module load, symbol lookup) that should happen before any stream
+// capture is started.
+int noalloc_setup(int device, NoAllocDevice** out, std::string* msg) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    *msg = "Error: no CUDA device available (this engine has no CPU fallback)";
+    return SCAMP_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= ndev || device >= 64) {
+    *msg = "Error: invalid CUDA device ordinal";
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  CUDA_TRY(cudaSetDevice(device));
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  NoAllocDevice& d = g_noalloc_dev[device];
+  if (!d.scratch) {
+    void* p = nullptr;
+    CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    CUDA_TRY(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, device));
+    d.scratch = static_cast<unsigned char*>(p);
+  }
+  *out = &d;
+  return SCAMP_OK;
+}
+
+// Hands out consecutive 256-byte-aligned pieces of the scratch.
+struct Carver {
+  unsigned char* p;
+  template <typename T>
+  T* take(size_t bytes) {
+    T* r = reinterpret_cast<T*>(p);
+    p += noalloc_round(bytes);
+    return r;
+  }
+};
+
+SeriesBufs carve_series(Carver& c, int64_t n, int bshift) {
+  SeriesBufs s{};
+  s.bshift = bshift;
+  s.T = c.take<double>(8 * n);
+  s.mean = c.take<double>(8 * n);
+  s.inv = c.take<double>(8 * n);
+  s.df = c.take<double>(8 * n);
+  s.dg = c.take<double>(8 * n);
+  s.inv32 = c.take<float>(4 * n);
+  s.df32 = c.take<float>(4 * n);
+  s.dg32 = c.take<float>(4 * n);
+  s.T32 = c.take<float>(4 * n);
+  s.bhi = c.take<float>(4 * (n / 32 + 1));
+  s.blo = c.take<float>(4 * (n / 32 + 1));
+  s.mu_rel = c.take<float>(4 * n);
+  return s;
+}
+
+// The FP64 join of run_device() on the static scratch: the same kernels,
+// launch shapes and segment length, so the results equal
+// scamp_gb300_join_dev's.  Ordered on `st`; nothing is synchronised.
+int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_result* res,
+                       cudaStream_t st, std::string* msg) {
+  const int64_t na = static_cast<int64_t>(a->len_a);
+  const int64_t nb = a->has_b ? static_cast<int64_t>(a->len_b) : na;
+  if (na > kNoAllocMaxSamples || nb > kNoAllocMaxSamples) {
+    *msg = "Error: the no-allocation join takes series of at most 65536 samples "
+           "(use scamp_gb300_join_dev for longer series)";
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  if (a->precision_type != SCAMP_PRECISION_DOUBLE && a->precision_type != SCAMP_PRECISION_ULTRA) {
+    *msg = "Error: the no-allocation join runs the FP64 form only (precision double or ultra)";
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  const Plan plan = make_plan(a);
+  const bool is_1nn = a->profile_type == SCAMP_PROFILE_1NN_INDEX;
+  const bool ultra = a->precision_type == SCAMP_PRECISION_ULTRA;
+  const int64_t m = plan.m;
+  const int W = fp64_band_width();
+  const int slab = fp64_slab_rows();
+  const int nthreads = fp64_threads();
+
+  Carver cv{dv.scratch};
+  unsigned long long* counters = cv.take<unsigned long long>(64);
+  int64_t* dprefix = cv.take<int64_t>(8 * kNoAllocPrefixCap);
+  uint64_t* keys_mem[2] = {cv.take<uint64_t>(8 * kNoAllocMaxSamples),
+                           cv.take<uint64_t>(8 * kNoAllocMaxSamples)};
+  const int bshift = block_shift(m);
+  SeriesBufs sa = carve_series(cv, kNoAllocMaxSamples, bshift);
+  SeriesBufs sb = carve_series(cv, kNoAllocMaxSamples, bshift);
+
+  uint32_t launches = 0;
+  const int chunk = 64;
+  const double* dA = a->timeseries_a;
+  const double* dB = a->has_b ? a->timeseries_b : a->timeseries_a;
+  {
+    const int64_t threads = (plan.ns_a + chunk - 1) / chunk;
+    stats_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, st>>>(
+        dA, na, m, ultra ? 1 : 0, chunk, sa.bshift, sa.T, sa.T32, sa.bhi, sa.blo, sa.mu_rel,
+        sa.mean, sa.inv, sa.df, sa.dg, sa.inv32, sa.df32, sa.dg32);
+    ++launches;
+  }
+  if (a->has_b) {
+    const int64_t threads = (plan.ns_b + chunk - 1) / chunk;
+    stats_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, st>>>(
+        dB, nb, m, ultra ? 1 : 0, chunk, sb.bshift, sb.T, sb.T32, sb.bhi, sb.blo, sb.mu_rel,
+        sb.mean, sb.inv, sb.df, sb.dg, sb.inv32, sb.df32, sb.dg32);
+    ++launches;
+  } else {
+    sb = sa;
+  }
+  CUDA_TRY(cudaGetLastError());
+  const SeriesDev devA = to_dev(sa, na, plan.ns_a);
+  const SeriesDev devB = to_dev(sb, nb, plan.ns_b);
+
+  const KeyLayout kl = make_key_layout(std::max(plan.ns_a, plan.ns_b));
+  uint64_t* profs[2] = {res->profile_a, res->profile_b};
+  double* sums[2] = {res->sum_a, res->sum_b};
+  uint64_t* keys[2] = {nullptr, nullptr};
+  const int64_t nsz[2] = {plan.ns_a, plan.ns_b};
+  bool used[2] = {false, false};
+  for (const auto& q : plan.probs) {
+    if (q.col_target >= 0) used[q.col_target] = true;
+    if (q.row_target >= 0) used[q.row_target] = true;
+  }
+  for (int s = 0; s < 2; ++s) {
+    // the profiles run_device() converts: every target, and profile A
+    const bool conv = used[s] || (s == 0 && profs[0]);
+    if (is_1nn && conv && !profs[s]) { *msg = "Error: profile buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
+    if (!is_1nn && used[s] && !sums[s]) { *msg = "Error: sum buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
+  }
+  if (is_1nn) {
+    for (int s = 0; s < 2; ++s) {
+      if (!used[s] && !(s == 0 && profs[0])) continue;
+      keys[s] = keys_mem[s];
+      profile_to_keys_kernel<<<static_cast<unsigned>((nsz[s] + 255) / 256), 256, 0, st>>>(
+          profs[s], keys[s], nsz[s], kl);
+      ++launches;
+    }
+  }
+
+  int occ = 1;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &occ, reinterpret_cast<const void*>(join_fp64_kernel), nthreads, 0));
+  occ = std::max(occ, 1);
+  const int64_t resident = static_cast<int64_t>(dv.sms) * occ;
+  // segment length: the FP64 rule of run_device()
+  const double cells_d = static_cast<double>(plan.cells);
+  const int64_t k_lb = static_cast<int64_t>(cells_d / (8.0 * resident * 2.0 * W));
+  int64_t K = std::max<int64_t>(8 * m, 2048);
+  K = std::min(K, std::max<int64_t>(k_lb, slab));
+  K = std::max<int64_t>(slab, (K / slab) * slab);
+  {
+    const int64_t blk = 1ll << block_shift(m);
+    if (K % blk) K = std::max<int64_t>(blk, (K / blk) * blk);
+  }
+
+  JoinParams P{};
+  int64_t prefix[kNoAllocPrefixCap];
+  int64_t np = 0;
+  prefix[np++] = 0;
+  int64_t band_total = 0;
+  for (const auto& q : plan.probs) {
+    Problem& pr = P.prob[P.nprob++];
+    pr.R = q.rows_series == 0 ? devA : devB;
+    pr.C = q.cols_series == 0 ? devA : devB;
+    pr.d_lo = q.d_lo; pr.d_hi = q.d_hi; pr.x_lo = q.x_lo; pr.x_hi = q.x_hi;
+    pr.key_col = is_1nn && q.col_target >= 0 ? keys[q.col_target] : nullptr;
+    pr.key_row = is_1nn && q.row_target >= 0 ? keys[q.row_target] : nullptr;
+    pr.sum_col = !is_1nn && q.col_target >= 0 ? sums[q.col_target] : nullptr;
+    pr.sum_row = !is_1nn && q.row_target >= 0 ? sums[q.row_target] : nullptr;
+    pr.band_begin = band_total;
+    pr.nbands = (q.d_hi - q.d_lo + W - 1) / W;
+    if (np + pr.nbands > kNoAllocPrefixCap) {
+      *msg = "Error: join too large for the no-allocation work queue";
+      return SCAMP_ERR_INVALID_ARGS;
+    }
+    for (int64_t b = 0; b < pr.nbands; ++b) {
+      const int64_t D0 = q.d_lo + b * W;
+      const int64_t rows = band_rows(q.n_r, q.n_c, D0);
+      const int64_t units = (rows + 2 * K - 1) / (2 * K);
+      prefix[np] = prefix[np - 1] + units;
+      ++np;
+    }
+    band_total += pr.nbands;
+  }
+  P.total_bands = band_total;
+  P.total_units = prefix[np - 1];
+  P.m = m;
+  P.seg_len = K;
+  P.band_width = W;
+  P.profile_type = a->profile_type;
+  P.threshold = a->distance_threshold;
+  P.kl = kl;
+
+  if (P.total_units > 0) {
+    CUDA_TRY(cudaMemcpyAsync(dprefix, prefix, np * 8, cudaMemcpyHostToDevice, st));
+    // the unit queue head and the work counters must start at zero
+    CUDA_TRY(cudaMemsetAsync(counters, 0, 64, st));
+    P.band_unit_prefix = dprefix;
+    P.unit_counter = counters;
+    P.counters = counters + 1;
+    P.error_flag = reinterpret_cast<int*>(counters + 6);
+    const int64_t grid = std::min<int64_t>(resident, P.total_units);
+    join_fp64_kernel<<<static_cast<unsigned>(grid), nthreads, 0, st>>>(P);
+    ++launches;
+    CUDA_TRY(cudaGetLastError());
+  }
+  if (is_1nn) {
+    double* corr[2] = {res->corr_a, res->corr_b};
+    for (int s = 0; s < 2; ++s) {
+      if (!keys[s]) continue;
+      keys_to_profile_kernel<<<static_cast<unsigned>((nsz[s] + 255) / 256), 256, 0, st>>>(
+          keys[s], profs[s], corr[s], nsz[s], kl);
+      ++launches;
+    }
+  }
+  CUDA_TRY(cudaGetLastError());
+  res->comparisons = plan.cells;
+  res->gpu_launches = launches;
+  res->elapsed_ms = res->join_kernel_ms = 0;
+  res->steps = res->slow_steps = res->verifications = 0;
+  return SCAMP_OK;
+}
+
+}  // namespace
+}  // namespace scamp_gb300
+
+extern "C" int scamp_gb300_join_dev_noalloc(const scamp_c_args* args, scamp_c_result* res,
+                                            void* stream, char* errbuf, size_t errlen) {
+  std::string msg;
+  int rc = validate(args, &msg);
+  if (rc == SCAMP_OK && !res) { msg = "Error: result struct missing"; rc = SCAMP_ERR_INVALID_ARGS; }
+  NoAllocDevice* dv = nullptr;
+  if (rc == SCAMP_OK) rc = noalloc_setup(args->device, &dv, &msg);
+  if (rc == SCAMP_OK) rc = run_device_noalloc(*dv, args, res, static_cast<cudaStream_t>(stream), &msg);
+  if (rc) set_err(errbuf, errlen, msg);
+  return rc;
+}

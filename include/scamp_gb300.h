@@ -120,6 +120,28 @@ int scamp_gb300_join(const scamp_c_args *args, scamp_c_result *res,
 int scamp_gb300_join_dev(const scamp_c_args *args, scamp_c_result *res,
                          void *stream, char *errbuf, size_t errlen);
 
+/* The FP64 form of scamp_gb300_join_dev without any allocation: every
+ * intermediate buffer lives in one static device array of the library
+ * (about 8.6 MB per device), so the join calls no allocator.  For callers
+ * that must not allocate device memory at join time (a host that gives all
+ * device memory to its own pool up front, or a loop that cannot wait on the
+ * allocator).  Has no counterpart in the reference.
+ *   - series of at most 65536 samples each; precision DOUBLE or ULTRA;
+ *     1NN_INDEX or SUM_THRESH; larger or other requests return
+ *     SCAMP_ERR_INVALID_ARGS with a message.
+ *   - all pointers are device memory of args->device; the work is ordered on
+ *     `stream` and not synchronised: results are ready when the stream
+ *     reaches the end of this call.  Timing fields and work counters of
+ *     `res` are left 0.
+ *   - the first call on a device looks up the static array and the SM
+ *     count; make it before starting any stream capture.
+ *   - calls that overlap on one device (other streams, other threads) race
+ *     on the shared array: serialise them on one stream.
+ *   - the entry zeroes the array's work counters itself on `stream`; every
+ *     other part of the array is written before it is read. */
+int scamp_gb300_join_dev_noalloc(const scamp_c_args *args, scamp_c_result *res,
+                                 void *stream, char *errbuf, size_t errlen);
+
 /* Checks arguments the way SCAMPArgs::validate does (src/common.cpp:417-436).
  * Pure host logic, needs no GPU. */
 int scamp_gb300_validate(const scamp_c_args *args, char *errbuf, size_t errlen);
