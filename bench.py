@@ -179,6 +179,8 @@ def main():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--na-log2", type=int, default=20,
                    help="log2 length of A (B is half); smaller only for profiling captures")
+    p.add_argument("--profile-form", default="mixed", choices=["mixed", "double"],
+                   help="form run by --profile-only")
     p.add_argument("--profile-only", action="store_true",
                    help="run only the timed mixed joins (for ncu captures); prints no JSON")
     args = p.parse_args()
@@ -235,6 +237,11 @@ def main():
         ev1.record(stream)
         ev1.synchronize()
         return ev0.elapsed_time(ev1), r
+
+    if args.profile_only and args.profile_form == "double":
+        for _ in range(args.warmup + args.steps):
+            one("double")
+        return
 
     # ---- mixed form (headline) ----
     for _ in range(max(args.warmup, 3)):
