@@ -237,7 +237,7 @@ enum Slot {
   S_T_B, S_MEAN_B, S_INV_B, S_DF_B, S_DG_B, S_INV32_B, S_DF32_B, S_DG32_B,
   S_KEY_A, S_KEY_B, S_SUM_A, S_SUM_B, S_PROF_A, S_PROF_B, S_CORR_A, S_CORR_B,
   S_PREFIX, S_COUNTER, S_T32_A, S_T32_B, S_BHI_A, S_BLO_A, S_MUREL_A,
-  S_BHI_B, S_BLO_B, S_MUREL_B, S_VREQ,
+  S_BHI_B, S_BLO_B, S_MUREL_B, S_VREQ, S_PAA_A, S_PAA_B, S_SEED_A, S_SEED_B,
 };
 
 #define CUDA_TRY(expr)                                                     \
@@ -296,11 +296,97 @@ SeriesDev to_dev(const SeriesBufs& s, int64_t n, int64_t ns) {
 
 // Runs a join whose inputs are device pointers; profile_a/b (packed entries)
 // and sum_a/b are device pointers too and are merged in place.
+// Seeding pre-pass of the mixed 1NN join: when and how.  The block-averaged
+// join costs ~1/64 of the join's cells; below a few 1e9 cells it does not pay.
+constexpr float kSeedFloor = 0.8f;  // partners below it are not worth a seed
+constexpr int64_t kSeedMinWindow = 64;
+
+// Block size of the pre-pass: the largest power of two <= m / 16 within
+// [4, 64] (window m / f of about 16 samples).  On the AB-join of 2^20 x 2^19
+// random walks at m = 256: no seeds 138.6 ms, f = 8: 127.1, f = 16: 126.2.
+int seed_factor(int64_t m) {
+  int f = 4;
+  while (f < 64 && 2 * f * 16 <= m) f *= 2;
+  return f;
+}
+constexpr uint64_t kSeedMinCells = uint64_t{4} << 30;
+
+// Seedable configurations: a self-join into one profile, or an AB join
+// (columns, and rows when kept separately), without alignment offsets.
+bool seedable(const scamp_c_args* a, const Plan& plan) {
+  if (a->is_aligned || a->distributed_start_row >= 0 || a->distributed_start_col >= 0) return false;
+  if (plan.m < kSeedMinWindow || plan.cells < kSeedMinCells) return false;
+  if (!a->computing_columns) return false;
+  if (plan.self_join) return a->computing_rows && !a->keep_rows_separate;
+  return !a->computing_rows || a->keep_rows_separate;
+}
+
 int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
                const double* dA, const double* dB, uint64_t* dprof_a,
                uint64_t* dprof_b, double* dsum_a, double* dsum_b,
                double* dcorr_a, double* dcorr_b, cudaStream_t st,
-               std::string* msg) {
+               std::string* msg, bool nested = false);
+
+// Block-averaged join of the inputs (window m / 8) into the seed profiles
+// S_SEED_A/B; returns their device pointers (seed_b null when not kept).
+int seed_prepass(Workspace& ws, const scamp_c_args* a, const Plan& plan, const double* dA,
+                 const double* dB, cudaStream_t st, uint64_t** seed_a, uint64_t** seed_b,
+                 int64_t* ns_a, int64_t* ns_b, uint32_t* launches, std::string* msg) {
+  const int f = seed_factor(plan.m);
+  const int64_t na = static_cast<int64_t>(a->len_a) / f;
+  const int64_t nb = a->has_b ? static_cast<int64_t>(a->len_b) / f : 0;
+  const int64_t m2 = plan.m / f;
+  const bool want_b = a->has_b && a->keep_rows_separate && a->computing_rows;
+  void *pa, *pb = nullptr, *qa, *qb = nullptr;
+  int rc;
+  if ((rc = ensure(ws, S_PAA_A, na * 8, &pa, msg))) return rc;
+  paa_kernel<<<static_cast<unsigned>((na + 255) / 256), 256, 0, st>>>(dA, na, f, static_cast<double*>(pa));
+  ++*launches;
+  if (a->has_b) {
+    if ((rc = ensure(ws, S_PAA_B, nb * 8, &pb, msg))) return rc;
+    paa_kernel<<<static_cast<unsigned>((nb + 255) / 256), 256, 0, st>>>(dB, nb, f, static_cast<double*>(pb));
+    ++*launches;
+  }
+  *ns_a = na - m2 + 1;
+  *ns_b = a->has_b ? nb - m2 + 1 : *ns_a;
+  if ((rc = ensure(ws, S_SEED_A, *ns_a * 8, &qa, msg))) return rc;
+  fill_floor_kernel<<<static_cast<unsigned>((*ns_a + 255) / 256), 256, 0, st>>>(
+      static_cast<uint64_t*>(qa), *ns_a, kSeedFloor);
+  ++*launches;
+  if (want_b) {
+    if ((rc = ensure(ws, S_SEED_B, *ns_b * 8, &qb, msg))) return rc;
+    fill_floor_kernel<<<static_cast<unsigned>((*ns_b + 255) / 256), 256, 0, st>>>(
+        static_cast<uint64_t*>(qb), *ns_b, kSeedFloor);
+    ++*launches;
+  }
+  CUDA_TRY(cudaGetLastError());
+  scamp_c_args a2 = *a;
+  a2.timeseries_a = static_cast<double*>(pa);
+  a2.len_a = static_cast<uint64_t>(na);
+  a2.timeseries_b = a->has_b ? static_cast<double*>(pb) : nullptr;
+  a2.len_b = static_cast<uint64_t>(nb);
+  a2.window = static_cast<uint64_t>(m2);
+  a2.precision_type = SCAMP_PRECISION_MIXED;
+  a2.profile_type = SCAMP_PROFILE_1NN_INDEX;
+  a2.anchor_interval = 0;
+  a2.silent_mode = 1;
+  scamp_c_result r2{};
+  rc = run_device(ws, &a2, &r2, static_cast<double*>(pa),
+                  a->has_b ? static_cast<double*>(pb) : static_cast<double*>(pa),
+                  static_cast<uint64_t*>(qa), static_cast<uint64_t*>(qb), nullptr, nullptr,
+                  nullptr, nullptr, st, msg, true);
+  if (rc) return rc;
+  *launches += r2.gpu_launches;
+  *seed_a = static_cast<uint64_t*>(qa);
+  *seed_b = static_cast<uint64_t*>(qb);
+  return SCAMP_OK;
+}
+
+int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
+               const double* dA, const double* dB, uint64_t* dprof_a,
+               uint64_t* dprof_b, double* dsum_a, double* dsum_b,
+               double* dcorr_a, double* dcorr_b, cudaStream_t st,
+               std::string* msg, bool nested) {
   Plan plan = make_plan(a);
   const bool is_1nn = a->profile_type == SCAMP_PROFILE_1NN_INDEX;
   const bool mixed = a->precision_type == SCAMP_PRECISION_MIXED ||
@@ -312,9 +398,20 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   uint32_t launches = 0;
   int rc;
 
-  ws.timed_kernel = false;
-  ws.timed_verify = false;
-  CUDA_TRY(cudaEventRecord(ws.ev0, st));
+  if (!nested) {
+    ws.timed_kernel = false;
+    ws.timed_verify = false;
+    CUDA_TRY(cudaEventRecord(ws.ev0, st));
+  }
+
+  // ---- seeds: block-averaged pre-pass (mixed 1NN joins that pay for it) ----
+  uint64_t *seed_a = nullptr, *seed_b = nullptr;
+  int64_t seed_ns_a = 0, seed_ns_b = 0;
+  if (!nested && mixed && is_1nn && seedable(a, plan)) {
+    if ((rc = seed_prepass(ws, a, plan, dA, dB, st, &seed_a, &seed_b, &seed_ns_a, &seed_ns_b,
+                           &launches, msg)))
+      return rc;
+  }
 
   // ---- statistics ----
   SeriesBufs sa{}, sb{};
@@ -367,6 +464,25 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   } else {
     for (int s = 0; s < 2; ++s)
       if (used[s] && !sums[s]) { *msg = "Error: sum buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
+  }
+
+  // ---- seeds merged into the keys ----
+  if (seed_a) {
+    const int64_t excl = plan.self_join ? plan.m / 4 : -1;
+    auto launch_seed = [&](const SeriesDev& X, const SeriesDev& Y, const uint64_t* paa,
+                           int64_t ns_paa, uint64_t* kx, uint64_t* ky) {
+      const SeedArgs S{X, Y, paa, ns_paa, kx, ky, excl, m, kl, kSeedFloor, seed_factor(m)};
+      const int64_t blocks = std::min<int64_t>((X.ns + 7) / 8, static_cast<int64_t>(ws.sms) * 16);
+      seed_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(S);
+      ++launches;
+    };
+    if (plan.self_join) {
+      launch_seed(devA, devA, seed_a, seed_ns_a, keys[0], keys[0]);
+    } else {
+      launch_seed(devA, devB, seed_a, seed_ns_a, keys[0], seed_b ? keys[1] : nullptr);
+      if (seed_b) launch_seed(devB, devA, seed_b, seed_ns_b, keys[1], keys[0]);
+    }
+    CUDA_TRY(cudaGetLastError());
   }
 
   // ---- work plan ----
@@ -484,13 +600,17 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
       P.vreq_cap = want;
     }
     const int64_t grid = std::min<int64_t>(resident, P.total_units);
-    CUDA_TRY(cudaEventRecord(ws.evk0, st));
-    ws.timed_kernel = true;
+    if (!nested) {
+      CUDA_TRY(cudaEventRecord(ws.evk0, st));
+      ws.timed_kernel = true;
+    }
     if (kind == K_MIXED_1NN) {
       join_mixed_1nn_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
       ++launches;
-      CUDA_TRY(cudaEventRecord(ws.evkv, st));
-      ws.timed_verify = true;
+      if (!nested) {
+        CUDA_TRY(cudaEventRecord(ws.evkv, st));
+        ws.timed_verify = true;
+      }
       verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
     } else if (kind == K_MIXED_SUM)
       join_mixed_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
@@ -498,7 +618,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
       join_fp64_kernel<<<static_cast<unsigned>(grid), nthreads, 0, st>>>(P);
     ++launches;
     CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaEventRecord(ws.evk1, st));
+    if (!nested) CUDA_TRY(cudaEventRecord(ws.evk1, st));
   }
 
   // ---- keys -> packed entries (+ optional double correlations) ----
@@ -512,7 +632,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     }
   }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaEventRecord(ws.ev1, st));
+  if (!nested) CUDA_TRY(cudaEventRecord(ws.ev1, st));
   if (res) {
     res->comparisons = plan.cells;
     res->gpu_launches = launches;

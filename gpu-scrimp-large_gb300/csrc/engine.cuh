@@ -190,6 +190,25 @@ __global__ void join_mixed_kernel(JoinParams P);      // SUM_THRESH
 __global__ void join_mixed_1nn_kernel(JoinParams P);  // 1NN_INDEX
 __global__ void verify_requests_kernel(JoinParams P);
 
+// Seeds of the mixed 1NN join from a block-averaged pre-pass.
+struct SeedArgs {
+  SeriesDev X;            // windows seeded
+  SeriesDev Y;            // their partners' series
+  const uint64_t* paa;    // packed profile of X's block-averaged windows
+  int64_t ns_paa;
+  uint64_t* key_x;        // X's profile keys
+  uint64_t* key_y;        // Y's profile keys, or null
+  int64_t excl;           // self-join: |i - j| >= excl; -1 for AB joins
+  int64_t m;
+  KeyLayout kl;
+  float floor;            // pre-pass entries not above it found no partner
+  int factor;             // samples per block-averaged sample
+};
+__global__ void paa_kernel(const double* __restrict__ T, int64_t n_out, int f,
+                           double* __restrict__ out);
+__global__ void fill_floor_kernel(uint64_t* __restrict__ p, int64_t n, float floor);
+__global__ void seed_kernel(SeedArgs S);
+
 __global__ void profile_to_keys_kernel(const uint64_t* __restrict__ in,
                                        uint64_t* __restrict__ keys, int64_t n,
                                        KeyLayout kl);

@@ -899,6 +899,64 @@ verify_requests_kernel(JoinParams P) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Seeds of the mixed 1NN join (an approximate pre-pass in the manner of
+// SCRIMP++'s PreSCRIMP).  A join of the series averaged over blocks of f
+// samples (window m / f) gives every block-averaged window a likely partner;
+// each full-resolution window i = f i' + o then gets the exact correlation of
+// the cell on the same diagonal, (i, f idx(i') + o), merged into the profile
+// keys before the band kernel runs.  Every seed is a real cell's r, so the
+// join's result is unchanged; its filters simply start high, which spares
+// most of the exact-path work of the first bands.
+// ---------------------------------------------------------------------------
+
+// out[k] = mean of T[f k .. f k + f), NaN when any of them is not finite.
+__global__ void paa_kernel(const double* __restrict__ T, int64_t n_out, int f,
+                           double* __restrict__ out) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n_out) return;
+  double sum = 0.0;
+  bool finite = true;
+  for (int u = 0; u < f; ++u) {
+    const double v = T[static_cast<int64_t>(f) * k + u];
+    finite = finite && isfinite(v);
+    sum += v;
+  }
+  out[k] = finite ? sum / f : __longlong_as_double(0x7FF8000000000000ll);
+}
+
+// Packed entries {r = floor, index 0}: the pre-pass only looks for partners
+// above `floor`, which spares it the cold start of a join from "no match".
+__global__ void fill_floor_kernel(uint64_t* __restrict__ p, int64_t n, float floor) {
+  const int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) p[k] = __float_as_uint(floor);
+}
+
+// One warp per window i of X: its seed partner from the block-averaged
+// profile, the exact r of that cell, merged into X's keys (and Y's).
+__global__ void __launch_bounds__(256) seed_kernel(SeedArgs S) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t i = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+       i < S.X.ns; i += nwarps) {
+    const int64_t ib = i / S.factor;
+    const int64_t ip = ib < S.ns_paa ? ib : S.ns_paa - 1;
+    const uint64_t packed = S.paa[ip];
+    if (!(__uint_as_float(static_cast<uint32_t>(packed)) > S.floor)) continue;  // no partner found
+    const int64_t j = S.factor * static_cast<int64_t>(packed >> 32) + (i - S.factor * ip);
+    if (j >= S.Y.ns) continue;
+    if (S.excl >= 0 && (j - i < S.excl && i - j < S.excl)) continue;  // trivial match
+    const float ivx = S.X.inv32[i], ivy = S.Y.inv32[j];
+    if (isnan(ivx) || isnan(ivy)) continue;
+    const float cv = verify_cov_warp(S.X, S.Y, i, j, S.m, lane);
+    if (lane == 0) {
+      const uint64_t q = q_from_float_bits(__float_as_uint((cv * ivy) * ivx), S.kl.frac_bits);
+      atomicMax(reinterpret_cast<u64*>(S.key_x + i), make_key(q, j, S.kl));
+      if (S.key_y) atomicMax(reinterpret_cast<u64*>(S.key_y + j), make_key(q, i, S.kl));
+    }
+  }
+}
+
 int mixed_1nn_band_width() { return kBand; }
 int mixed_1nn_slab_rows() { return kSlab; }
 int mixed_1nn_threads() { return kThreads; }

@@ -230,3 +230,23 @@ def test_against_reference_golden_fixtures(gpu_engine, precision, tol):
             if "sum_" + side in z.files:
                 rt = 1e-9 if precision == "double" else 2e-5
                 check_sum(f, got["sum_" + side], z["sum_" + side], thr, rt)
+
+
+# Joins of >= 4e9 cells at m >= 64 run the block-averaged seeding pre-pass
+# before the mixed band kernel; the result must be the unseeded join's.
+@pytest.mark.parametrize("keep_rows", [True, False])
+def test_seeded_abjoin(gpu_engine, oracle_mod, keep_rows):
+    from scamp_gb300 import workloads
+
+    a, b, m = workloads.cfg2_abjoin(na=1 << 17, nb=1 << 16, motifs=16)
+    assert gpu_engine.count_cells(len(a), m, len_b=len(b)) >= 4 << 30
+    got, _ = run_1nn(gpu_engine, oracle_mod, a, b, m, "mixed", TOL_MIXED, keep_rows=keep_rows,
+                     rows=keep_rows, name="seeded_ab")
+    assert got["gpu_launches"] > 12  # pre-pass launches included
+
+
+def test_seeded_selfjoin(gpu_engine, oracle_mod):
+    rng = np.random.default_rng(123)
+    a = rw(rng, 1 << 17)
+    got, _ = run_1nn(gpu_engine, oracle_mod, a, None, 128, "mixed", TOL_MIXED, name="seeded_self")
+    assert got["gpu_launches"] > 8
