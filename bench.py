@@ -112,9 +112,22 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+# Second workload (--workload self): the precision study's large self-join,
+# random walk + 0.5 N(0,1) noise, n = 2^24, m = 1024.  Its FP64 leg and the
+# error check run on the first 2^22 samples (FP64 on the whole join takes
+# ~20 minutes); comparisons/s are per-cell rates, so they carry over.
+SELF_WORKLOAD = "self-join: random walk + 0.5 N(0,1) noise, n=2^24, m=1024, 1NN_INDEX"
+SELF_M = 1024
+SELF_FP64_PREFIX = 1 << 22
+WORKLOAD_KIND = "ab"
+
+
 def make_workload(na=None, nb=None):
     from scamp_gb300 import workloads
 
+    if WORKLOAD_KIND == "self":
+        a, m = workloads.cfg3_large(n=na or NA, m=SELF_M)
+        return a, None, m
     return workloads.cfg2_abjoin(na=na or NA, nb=nb or NB, m=M)
 
 
@@ -126,24 +139,23 @@ def run_reference(args, world, rank):
     import oracle
 
     oracle.load()
-    a, b, m = make_workload(1 << 20, 1 << 19)
-    a, b = a[:CPU_NA], b[:CPU_NB]
-    cells = (len(a) - m + 1) * (len(b) - m + 1)
+    a, b, cells, sample = cpu_sample()
+    m = M if WORKLOAD_KIND == "ab" else SELF_M
     threads = oracle.max_threads()
     for _ in range(args.warmup):
-        oracle.join(a, b, m, keep_rows=True, threads=threads)
+        oracle.join(a, b, m, keep_rows=b is not None, threads=threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        oracle.join(a, b, m, keep_rows=True, threads=threads)
+        oracle.join(a, b, m, keep_rows=b is not None, threads=threads)
     dt = (time.perf_counter() - t0) / args.steps
     value = cells / dt
-    sample = "A[:2^17] x B[:2^16] of the workload, both directions, DOUBLE"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "comparisons/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": sample},
+        "config": {"workload": WORKLOAD if WORKLOAD_KIND == "ab" else SELF_WORKLOAD,
+                   "sample": sample},
         "cpu_baseline": {"value": value, "unit": "comparisons/s", "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "comparisons/s", "h2d_bytes_per_step": 0,
@@ -152,21 +164,34 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def cpu_sample():
+    """Bounded CPU sample of the workload: (a, b, cells, description)."""
+    if WORKLOAD_KIND == "self":
+        a, _, m = make_workload(1 << 24)
+        a = a[:CPU_NA]
+        ns = len(a) - m + 1
+        e = m // 4
+        cells = (ns - e) * (ns - e + 1) // 2
+        return a, None, cells, "first 2^17 samples of the workload, self-join, DOUBLE"
+    a, b, m = make_workload(1 << 20, 1 << 19)
+    a, b = a[:CPU_NA], b[:CPU_NB]
+    cells = (len(a) - m + 1) * (len(b) - m + 1)
+    return a, b, cells, "A[:2^17] x B[:2^16] of the workload, both directions, DOUBLE"
+
+
 def cpu_baseline_leg():
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
 
     oracle.load()
-    a, b, m = make_workload(1 << 20, 1 << 19)
-    a, b = a[:CPU_NA], b[:CPU_NB]
-    cells = (len(a) - m + 1) * (len(b) - m + 1)
+    a, b, cells, sample = cpu_sample()
+    m = M if WORKLOAD_KIND == "ab" else SELF_M
     threads = oracle.max_threads()
     t0 = time.perf_counter()
-    oracle.join(a, b, m, keep_rows=True, threads=threads)
+    oracle.join(a, b, m, keep_rows=b is not None, threads=threads)
     dt = time.perf_counter() - t0
     return {"value": cells / dt, "unit": "comparisons/s", "cores": threads, "kind": "port",
-            "sample": "A[:2^17] x B[:2^16] of the workload, both directions, DOUBLE, "
-                      "%.1f s" % dt}
+            "sample": sample + ", %.1f s" % dt}
 
 
 def main():
@@ -177,15 +202,25 @@ def main():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--fp64-steps", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--na-log2", type=int, default=20,
+    p.add_argument("--workload", default="ab", choices=["ab", "self"],
+                   help="ab: the headline AB-join (default); self: the 2^24-point m=1024 "
+                        "self-join of the precision study")
+    p.add_argument("--na-log2", type=int, default=None,
                    help="log2 length of A (B is half); smaller only for profiling captures")
     p.add_argument("--profile-form", default="mixed", choices=["mixed", "double"],
                    help="form run by --profile-only")
     p.add_argument("--profile-only", action="store_true",
                    help="run only the timed mixed joins (for ncu captures); prints no JSON")
     args = p.parse_args()
-    global NA, NB
-    NA, NB = 1 << args.na_log2, 1 << (args.na_log2 - 1)
+    global NA, NB, WORKLOAD_KIND
+    WORKLOAD_KIND = args.workload
+    if args.workload == "self":
+        NA = 1 << (args.na_log2 or 24)
+        NB = NA
+    else:
+        na_log2 = args.na_log2 or 20
+        NA, NB = 1 << na_log2, 1 << (na_log2 - 1)
+    self_join = args.workload == "self"
     world, rank, local = dist_env()
 
     if args.impl == "reference":
@@ -208,20 +243,22 @@ def main():
             dist.barrier()
 
     a_np, b_np, m = make_workload()
-    nsa, nsb = NA - m + 1, NB - m + 1
+    nsa = NA - m + 1
+    nsb = nsa if self_join else NB - m + 1
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     a_d = torch.from_numpy(a_np).to(dev)
-    b_d = torch.from_numpy(b_np).to(dev)
+    b_d = a_d if self_join else torch.from_numpy(b_np).to(dev)
     no_match = int(scamp_gb300.NO_MATCH)
     prof_a = torch.empty(nsa, dtype=torch.int64, device=dev)
-    prof_b = torch.empty(nsb, dtype=torch.int64, device=dev)
+    prof_b = torch.empty(1 if self_join else nsb, dtype=torch.int64, device=dev)
     corr_a = torch.empty(nsa, dtype=torch.float64, device=dev)
-    corr_b = torch.empty(nsb, dtype=torch.float64, device=dev)
+    corr_b = torch.empty(1 if self_join else nsb, dtype=torch.float64, device=dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     nm = no_match - (1 << 64) if no_match >= (1 << 63) else no_match
 
-    def one(precision):
+    def one(precision, n_a=None):
+        """One join (the whole workload, or the self-join's first n_a samples)."""
         with torch.cuda.stream(stream):
             prof_a.fill_(nm)
             prof_b.fill_(nm)
@@ -230,10 +267,12 @@ def main():
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
         r = scamp_gb300.join_device(
-            a_d.data_ptr(), NA, m, b_d.data_ptr(), NB, "1NN_INDEX", precision,
-            computing_rows=True, keep_rows=True, profile_a_ptr=prof_a.data_ptr(),
-            profile_b_ptr=prof_b.data_ptr(), corr_a_ptr=corr_a.data_ptr(),
-            corr_b_ptr=corr_b.data_ptr(), stream=stream.cuda_stream, device=local)
+            a_d.data_ptr(), n_a or NA, m, None if self_join else b_d.data_ptr(),
+            0 if self_join else NB, "1NN_INDEX", precision,
+            computing_rows=True, keep_rows=not self_join, profile_a_ptr=prof_a.data_ptr(),
+            profile_b_ptr=None if self_join else prof_b.data_ptr(), corr_a_ptr=corr_a.data_ptr(),
+            corr_b_ptr=None if self_join else corr_b.data_ptr(), stream=stream.cuda_stream,
+            device=local)
         ev1.record(stream)
         ev1.synchronize()
         return ev0.elapsed_time(ev1), r
@@ -244,7 +283,7 @@ def main():
         return
 
     # ---- mixed form (headline) ----
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(args.warmup, 1 if self_join else 3)):
         one("mixed")
     barrier()
     torch.cuda.synchronize()
@@ -273,17 +312,28 @@ def main():
                  prof_b.cpu().numpy().view(np.uint64) >> np.uint64(32))
 
     # ---- FP64 form: throughput and the accuracy reference ----
-    one("double")
+    n_fp64 = None
+    if self_join and NA > SELF_FP64_PREFIX:
+        # the study's FP64 leg and error check: the first 2^22 samples
+        n_fp64 = SELF_FP64_PREFIX
+        one("mixed", n_fp64)
+        one("mixed", n_fp64)
+        mixed_corr = (corr_a.cpu().numpy()[: n_fp64 - m + 1].copy(), mixed_corr[1])
+        mixed_idx = ((prof_a.cpu().numpy().view(np.uint64) >> np.uint64(32))[: n_fp64 - m + 1],
+                     mixed_idx[1])
+    one("double", n_fp64)
     fp64_ms, fp64_kernel = [], []
     for _ in range(max(1, args.fp64_steps)):
-        ms, r64 = one("double")
+        ms, r64 = one("double", n_fp64)
         fp64_ms.append(ms)
         fp64_kernel.append(r64["join_kernel_ms"])
-    f_corr = (corr_a.cpu().numpy(), corr_b.cpu().numpy())
-    f_idx = (prof_a.cpu().numpy().view(np.uint64) >> np.uint64(32),
+    cells64 = r64["comparisons"]
+    n_f = (n_fp64 or NA) - m + 1
+    f_corr = (corr_a.cpu().numpy()[:n_f], corr_b.cpu().numpy())
+    f_idx = ((prof_a.cpu().numpy().view(np.uint64) >> np.uint64(32))[:n_f],
              prof_b.cpu().numpy().view(np.uint64) >> np.uint64(32))
     max_err, idx_agree, n_valid = 0.0, 0, 0
-    for k in range(2):
+    for k in range(1 if self_join else 2):
         ok = f_corr[k] >= -1
         if ok.any():
             max_err = max(max_err, float(np.max(np.abs(mixed_corr[k][ok] - f_corr[k][ok]))))
@@ -292,7 +342,7 @@ def main():
 
     # ---- e2e through the host-buffer C ABI ----
     a_pin = torch.from_numpy(a_np).pin_memory().numpy()
-    b_pin = torch.from_numpy(b_np).pin_memory().numpy()
+    b_pin = None if self_join else torch.from_numpy(b_np).pin_memory().numpy()
     pa_pin = torch.empty(nsa, dtype=torch.int64).pin_memory().numpy().view(np.uint64)
     pb_pin = torch.empty(nsb, dtype=torch.int64).pin_memory().numpy().view(np.uint64)
     pa_pin[:] = scamp_gb300.NO_MATCH
@@ -306,8 +356,9 @@ def main():
             flush.fill_(2)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = scamp_gb300.join(a_pin, b_pin, m, "1NN_INDEX", "mixed", keep_rows=True,
-                             profile_a=pa_pin, profile_b=pb_pin, device=local, inplace=True)
+        r = scamp_gb300.join(a_pin, b_pin, m, "1NN_INDEX", "mixed", keep_rows=not self_join,
+                             profile_a=pa_pin, profile_b=None if self_join else pb_pin,
+                             device=local, inplace=True)
         dt = time.perf_counter() - t0
         if it >= args.warmup:
             e2e_t.append(dt)
@@ -317,8 +368,11 @@ def main():
         t = torch.tensor([e2e_s], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = t.item()
-    h2d = (NA + NB) * 8 + (nsa + nsb) * 8
-    d2h = (nsa + nsb) * 8
+    if self_join:
+        h2d, d2h = NA * 8 + nsa * 8, nsa * 8
+    else:
+        h2d = (NA + NB) * 8 + (nsa + nsb) * 8
+        d2h = (nsa + nsb) * 8
 
     # ---- roofline: the join kernel against the measured FMA-pipe peaks ----
     peak32 = scamp_gb300.pipe_peak("fp32", local)
@@ -326,7 +380,7 @@ def main():
     k_ms = sum(kernel_ms) / len(kernel_ms)
     achieved = cells * OPS_PER_CELL / (k_ms * 1e-3)
     k64 = sum(fp64_kernel) / len(fp64_kernel)
-    achieved64 = cells * OPS_PER_CELL / (k64 * 1e-3)
+    achieved64 = cells64 * OPS_PER_CELL / (k64 * 1e-3)
 
     if rank != 0:
         return
@@ -343,20 +397,22 @@ def main():
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded random walks with planted motifs and NaNs)",
-        "config": {"workload": WORKLOAD, "form": "mixed (FP32 recurrence, FP64-centred anchors)",
+        "config": {"workload": SELF_WORKLOAD if self_join else WORKLOAD,
+                   "form": "mixed (FP32 recurrence, FP64-centred anchors)",
                    "comparisons_per_step": cells, "l2": "flushed (512 MB write) before each step",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "max_abs_r_err_vs_fp64": max_err,
         "index_agreement_vs_fp64": idx_agree / max(n_valid, 1),
-        "fp64": {"value": cells / (sum(fp64_ms) / len(fp64_ms) * 1e-3), "unit": "comparisons/s",
+        "fp64": {"value": cells64 / (sum(fp64_ms) / len(fp64_ms) * 1e-3), "unit": "comparisons/s",
+                 "comparisons_per_step": cells64,
                  "ms_per_step": sum(fp64_ms) / len(fp64_ms),
                  "roofline": {"bound": "fp64_fma_pipe", "achieved": achieved64 / 1e12,
                               "peak": peak64 / 1e12, "unit": "Tops/s",
                               "frac": achieved64 / peak64, "peak_source": "measured DFMA probe"}},
-        "speedup_mixed_vs_fp64": (sum(fp64_ms) / len(fp64_ms)) / ms_step,
+        "speedup_mixed_vs_fp64": value / world / (cells64 / (sum(fp64_ms) / len(fp64_ms) * 1e-3)),
         "roofline": {"bound": "fp32_fma_pipe", "achieved": achieved / 1e12, "peak": peak32 / 1e12,
                      "unit": "Tops/s", "frac": achieved / peak32,
-                     "traffic": DRAM_BYTES_PER_LAUNCH if NA == 1 << 20 else None,
+                     "traffic": DRAM_BYTES_PER_LAUNCH if (NA == 1 << 20 and not self_join) else None,
                      "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
                      "kernel": "join_mixed_1nn_kernel", "kernel_ms": k_ms,
                      "ops_per_comparison": OPS_PER_CELL,

@@ -40,10 +40,14 @@ int measure_pipe_peak(int device, int kind, double* ops_per_s);
 
 namespace {
 
-// Rows between re-anchors of the mixed form: measured best on the AB-join
-// of 2^20 x 2^19 random walks, m = 256 (512: 149 ms, 768: 141, 1024: 137.5,
-// 1536: 139; the max |r| error stays 5.7e-6).
-constexpr int kDefaultAnchorInterval = 1024;
+// Rows between re-anchors of the mixed form: 4 m within [1024, 4096], the
+// measured best.  AB-join of 2^20 x 2^19 random walks, m = 256: K = 512
+// 149 ms, 768 141, 1024 137.5, 1536 139.  Self-join of 2^22 noisy random walk,
+// m = 1024: K = 1024 2.45 s, 2048 2.08, 4096 1.89.  The max |r| error stays
+// below 5e-6 (6e-6) throughout.
+int64_t default_anchor_interval(int64_t m) {
+  return std::min<int64_t>(4096, std::max<int64_t>(1024, 4 * m));
+}
 
 struct Error {
   int code;
@@ -208,7 +212,7 @@ struct Workspace {
 };
 
 constexpr int64_t kMinVerifyReqs = int64_t{1} << 22;
-constexpr int64_t kMaxVerifyReqs = int64_t{1} << 27;  // 2 GiB of requests
+constexpr int64_t kMaxVerifyReqs = int64_t{1} << 28;  // 4 GiB of requests
 
 Workspace g_ws[64];
 
@@ -515,7 +519,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   const double cells_d = static_cast<double>(plan.cells);
   const int64_t k_lb = static_cast<int64_t>(cells_d / (8.0 * resident * 2.0 * W));
   if (mixed) {
-    K = a->anchor_interval > 0 ? a->anchor_interval : kDefaultAnchorInterval;
+    K = a->anchor_interval > 0 ? a->anchor_interval : default_anchor_interval(m);
   } else {
     K = std::max<int64_t>(8 * m, 2048);
   }
