@@ -242,6 +242,7 @@ enum Slot {
   S_KEY_A, S_KEY_B, S_SUM_A, S_SUM_B, S_PROF_A, S_PROF_B, S_CORR_A, S_CORR_B,
   S_PREFIX, S_COUNTER, S_T32_A, S_T32_B, S_BHI_A, S_BLO_A, S_MUREL_A,
   S_BHI_B, S_BLO_B, S_MUREL_B, S_VREQ, S_PAA_A, S_PAA_B, S_SEED_A, S_SEED_B,
+  S_BATCH,
 };
 
 #define CUDA_TRY(expr)                                                     \
@@ -548,6 +549,8 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     pr.sum_row = !is_1nn && q.row_target >= 0 ? sums[q.row_target] : nullptr;
     pr.band_begin = band_total;
     pr.nbands = (q.d_hi - q.d_lo + W - 1) / W;
+    pr.m = m;
+    pr.seg_len = K;
     for (int64_t b = 0; b < pr.nbands; ++b) {
       const int64_t D0 = q.d_lo + b * W;
       const int64_t rows = band_rows(q.n_r, q.n_c, D0);
@@ -569,6 +572,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     const double blk = static_cast<double>(1 << sa.bshift);
     const double e = std::sqrt(std::min<double>(m, blk)) + std::sqrt(std::ceil(m / blk) + 1.0);
     P.anchor_vcoef = static_cast<float>(e * e / 8.0);  // per 8-row step units
+    for (int p = 0; p < P.nprob; ++p) P.prob[p].anchor_vcoef = P.anchor_vcoef;
   }
 
   if (!a->silent_mode) {
@@ -1106,6 +1110,307 @@ extern "C" int scamp_gb300_join_dev_noalloc(const scamp_c_args* args, scamp_c_re
   NoAllocDevice* dv = nullptr;
   if (rc == SCAMP_OK) rc = noalloc_setup(args->device, &dv, &msg);
   if (rc == SCAMP_OK) rc = run_device_noalloc(*dv, args, res, static_cast<cudaStream_t>(stream), &msg);
+  if (rc) set_err(errbuf, errlen, msg);
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Batched self-joins (scamp_gb300_join_batch): many independent series, each
+// its own band problem, all in one persistent launch of the mixed 1NN band
+// kernel.  Series, statistics, keys and profiles of the whole batch are
+// concatenated in one workspace arena; one batched statistics launch, one
+// key conversion each way and one verification launch serve every series.
+// ---------------------------------------------------------------------------
+namespace scamp_gb300 {
+namespace {
+
+struct BatchSeries {
+  int64_t n, m, ns, excl, K;
+  int bshift;
+  int64_t off_n, off_ns, off_blk;
+  uint64_t cells;
+};
+
+// Segment length of one series of a batch: the anchor interval, reduced for
+// short series so that a band's rows split into at least two segments.
+int64_t batch_segment(int64_t m, int64_t ns, int slab) {
+  int64_t K = default_anchor_interval(m);
+  const int64_t half = std::max<int64_t>(slab, (ns / 2 / slab) * slab);
+  K = std::min(K, half);
+  const int64_t blk = int64_t{1} << block_shift(m);
+  if (K % blk) K = std::max<int64_t>(blk, (K / blk) * blk);
+  return K;
+}
+
+int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int count,
+              cudaStream_t st, std::string* msg) {
+  int rc;
+  ws.timed_kernel = false;
+  ws.timed_verify = false;
+  std::vector<BatchSeries> ser(count);
+  int64_t Nn = 0, Nns = 0, Nblk = 0, ns_max = 1;
+  bool want_corr = false;
+  for (int k = 0; k < count; ++k) {
+    const scamp_c_args* a = &args[k];
+    BatchSeries& b = ser[k];
+    b.n = static_cast<int64_t>(a->len_a);
+    b.m = static_cast<int64_t>(a->window);
+    b.ns = b.n - b.m + 1;
+    b.excl = b.m / 4;  // src/tile.cpp:14
+    b.bshift = block_shift(b.m);
+    b.K = batch_segment(b.m, b.ns, mixed_1nn_slab_rows());
+    b.off_n = Nn;
+    b.off_ns = Nns;
+    b.off_blk = Nblk;
+    b.cells = b.ns > b.excl ? diag_cells(b.ns, b.ns, b.excl, b.ns) : 0;
+    Nn += b.n;
+    Nns += b.ns;
+    Nblk += (b.n >> b.bshift) + 1;
+    ns_max = std::max(ns_max, b.ns);
+    want_corr = want_corr || res[k].corr_a != nullptr;
+  }
+  // ---- arena ----
+  size_t total = 0;
+  auto sz = [&](size_t b) { const size_t r = (b + 255) / 256 * 256; total += r; return r; };
+  const size_t b_raw = sz(8 * Nn), b_T = sz(8 * Nn), b_mean = sz(8 * Nns), b_inv = sz(8 * Nns),
+               b_df = sz(8 * Nns), b_dg = sz(8 * Nns), b_inv32 = sz(4 * Nns), b_df32 = sz(4 * Nns),
+               b_dg32 = sz(4 * Nns), b_T32 = sz(4 * Nn), b_bhi = sz(4 * Nblk), b_blo = sz(4 * Nblk),
+               b_murel = sz(4 * Nns), b_keys = sz(8 * Nns), b_prof = sz(8 * Nns),
+               b_corr = sz(want_corr ? 8 * Nns : 8), b_jobs = sz(sizeof(StatsJob) * count),
+               b_jpre = sz(8 * (count + 1)), b_probs = sz(sizeof(Problem) * count),
+               b_counter = sz(64);
+  // band prefix: sized after the problems are known
+  int64_t bands_max = 0;
+  for (const auto& b : ser) bands_max += (b.ns + mixed_1nn_band_width() - 1) / mixed_1nn_band_width();
+  const size_t b_bpre = sz(8 * (bands_max + 1));
+  void* arena;
+  if ((rc = ensure(ws, S_BATCH, total, &arena, msg))) return rc;
+  unsigned char* cur = static_cast<unsigned char*>(arena);
+  auto take = [&](size_t bytes) { unsigned char* r = cur; cur += bytes; return r; };
+  double* d_raw = reinterpret_cast<double*>(take(b_raw));
+  double* d_T = reinterpret_cast<double*>(take(b_T));
+  double* d_mean = reinterpret_cast<double*>(take(b_mean));
+  double* d_inv = reinterpret_cast<double*>(take(b_inv));
+  double* d_df = reinterpret_cast<double*>(take(b_df));
+  double* d_dg = reinterpret_cast<double*>(take(b_dg));
+  float* d_inv32 = reinterpret_cast<float*>(take(b_inv32));
+  float* d_df32 = reinterpret_cast<float*>(take(b_df32));
+  float* d_dg32 = reinterpret_cast<float*>(take(b_dg32));
+  float* d_T32 = reinterpret_cast<float*>(take(b_T32));
+  float* d_bhi = reinterpret_cast<float*>(take(b_bhi));
+  float* d_blo = reinterpret_cast<float*>(take(b_blo));
+  float* d_murel = reinterpret_cast<float*>(take(b_murel));
+  uint64_t* d_keys = reinterpret_cast<uint64_t*>(take(b_keys));
+  uint64_t* d_prof = reinterpret_cast<uint64_t*>(take(b_prof));
+  double* d_corr = reinterpret_cast<double*>(take(b_corr));
+  StatsJob* d_jobs = reinterpret_cast<StatsJob*>(take(b_jobs));
+  int64_t* d_jpre = reinterpret_cast<int64_t*>(take(b_jpre));
+  Problem* d_probs = reinterpret_cast<Problem*>(take(b_probs));
+  unsigned long long* d_counter = reinterpret_cast<unsigned long long*>(take(b_counter));
+  int64_t* d_bpre = reinterpret_cast<int64_t*>(take(b_bpre));
+
+  CUDA_TRY(cudaEventRecord(ws.ev0, st));
+  uint32_t launches = 0;
+  // ---- inputs: gathered on the host, one copy each way ----
+  std::vector<double> h_raw(static_cast<size_t>(Nn));
+  std::vector<uint64_t> h_prof(static_cast<size_t>(Nns));
+  for (int k = 0; k < count; ++k) {
+    std::memcpy(h_raw.data() + ser[k].off_n, args[k].timeseries_a, ser[k].n * 8);
+    std::memcpy(h_prof.data() + ser[k].off_ns, res[k].profile_a, ser[k].ns * 8);
+  }
+  CUDA_TRY(cudaMemcpyAsync(d_raw, h_raw.data(), Nn * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d_prof, h_prof.data(), Nns * 8, cudaMemcpyHostToDevice, st));
+
+  // ---- statistics: one launch for the batch ----
+  const int chunk = 64;
+  std::vector<StatsJob> jobs(count);
+  std::vector<int64_t> jpre(count + 1, 0);
+  for (int k = 0; k < count; ++k) {
+    const BatchSeries& b = ser[k];
+    StatsJob& j = jobs[k];
+    j.T_raw = d_raw + b.off_n;
+    j.n = b.n;
+    j.m = b.m;
+    j.bshift = b.bshift;
+    j.T_clean = d_T + b.off_n;
+    j.mean = d_mean + b.off_ns;
+    j.inv = d_inv + b.off_ns;
+    j.df = d_df + b.off_ns;
+    j.dg = d_dg + b.off_ns;
+    j.T32 = d_T32 + b.off_n;
+    j.bhi = d_bhi + b.off_blk;
+    j.blo = d_blo + b.off_blk;
+    j.mu_rel = d_murel + b.off_ns;
+    j.inv32 = d_inv32 + b.off_ns;
+    j.df32 = d_df32 + b.off_ns;
+    j.dg32 = d_dg32 + b.off_ns;
+    const int64_t threads = (b.ns + chunk - 1) / chunk;
+    jpre[k + 1] = jpre[k] + (threads + 127) / 128;
+  }
+  CUDA_TRY(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(StatsJob) * count, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d_jpre, jpre.data(), 8 * (count + 1), cudaMemcpyHostToDevice, st));
+  stats_batch_kernel<<<static_cast<unsigned>(jpre[count]), 128, 0, st>>>(d_jobs, d_jpre, count, 0, chunk);
+  ++launches;
+
+  // ---- keys ----
+  const KeyLayout kl = make_key_layout(ns_max);
+  profile_to_keys_kernel<<<static_cast<unsigned>((Nns + 255) / 256), 256, 0, st>>>(d_prof, d_keys, Nns, kl);
+  ++launches;
+  CUDA_TRY(cudaGetLastError());
+
+  // ---- problems and the work queue ----
+  const int W = mixed_1nn_band_width();
+  std::vector<Problem> probs;
+  probs.reserve(count);
+  std::vector<int64_t> bpre;
+  bpre.push_back(0);
+  int64_t band_total = 0;
+  uint64_t cells_total = 0;
+  for (int k = 0; k < count; ++k) {
+    const BatchSeries& b = ser[k];
+    if (b.cells == 0) continue;
+    SeriesDev sd;
+    sd.T = d_T + b.off_n; sd.mean = d_mean + b.off_ns; sd.inv = d_inv + b.off_ns;
+    sd.df = d_df + b.off_ns; sd.dg = d_dg + b.off_ns;
+    sd.inv32 = d_inv32 + b.off_ns; sd.df32 = d_df32 + b.off_ns; sd.dg32 = d_dg32 + b.off_ns;
+    sd.T32 = d_T32 + b.off_n; sd.bhi = d_bhi + b.off_blk; sd.blo = d_blo + b.off_blk;
+    sd.mu_rel = d_murel + b.off_ns; sd.bshift = b.bshift; sd.n = b.n; sd.ns = b.ns;
+    Problem pr{};
+    pr.R = sd;
+    pr.C = sd;
+    pr.d_lo = b.excl;
+    pr.d_hi = b.ns;
+    pr.x_lo = pr.x_hi = 0;
+    pr.key_col = pr.key_row = d_keys + b.off_ns;  // self-join: rows and columns into profile A
+    pr.band_begin = band_total;
+    pr.nbands = (pr.d_hi - pr.d_lo + W - 1) / W;
+    pr.m = b.m;
+    pr.seg_len = b.K;
+    {
+      const double blk = static_cast<double>(1 << b.bshift);
+      const double e = std::sqrt(std::min<double>(b.m, blk)) + std::sqrt(std::ceil(b.m / blk) + 1.0);
+      pr.anchor_vcoef = static_cast<float>(e * e / 8.0);
+    }
+    for (int64_t g = 0; g < pr.nbands; ++g) {
+      const int64_t D0 = pr.d_lo + g * W;
+      const int64_t rows = band_rows(b.ns, b.ns, D0);
+      bpre.push_back(bpre.back() + (rows + 2 * b.K - 1) / (2 * b.K));
+    }
+    band_total += pr.nbands;
+    cells_total += b.cells;
+    probs.push_back(pr);
+  }
+  if (!probs.empty()) {
+    CUDA_TRY(cudaMemcpyAsync(d_probs, probs.data(), sizeof(Problem) * probs.size(),
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_bpre, bpre.data(), 8 * bpre.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(d_counter, 0, 64, st));
+    JoinParams P{};
+    P.nprob = 0;
+    P.batch = d_probs;
+    P.nbatch = static_cast<int64_t>(probs.size());
+    P.band_unit_prefix = d_bpre;
+    P.total_bands = band_total;
+    P.total_units = bpre.back();
+    P.unit_counter = d_counter;
+    P.counters = d_counter + 1;
+    P.error_flag = reinterpret_cast<int*>(d_counter + 6);
+    P.profile_type = SCAMP_PROFILE_1NN_INDEX;
+    P.kl = kl;
+    int64_t want = std::max<int64_t>(kMinVerifyReqs, 32 * Nns);
+    want = std::max<int64_t>(want, ws.vreq_seen + ws.vreq_seen / 4);
+    want = std::max<int64_t>(std::min<int64_t>(want, kMaxVerifyReqs), ws.vreq_cap);
+    void* q;
+    if ((rc = ensure(ws, S_VREQ, static_cast<size_t>(want) * sizeof(VerifyReq), &q, msg))) return rc;
+    ws.vreq_cap = want;
+    P.vreq = static_cast<VerifyReq*>(q);
+    P.vreq_cap = want;
+    const size_t smem = mixed_1nn_smem_bytes();
+    const void* kfn = reinterpret_cast<const void*>(join_mixed_1nn_kernel);
+    CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int occ = 1;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, mixed_1nn_threads(), smem));
+    const int64_t grid = std::min<int64_t>(static_cast<int64_t>(ws.sms) * std::max(occ, 1), P.total_units);
+    CUDA_TRY(cudaEventRecord(ws.evk0, st));
+    ws.timed_kernel = true;
+    join_mixed_1nn_kernel<<<static_cast<unsigned>(grid), mixed_1nn_threads(), smem, st>>>(P);
+    ++launches;
+    CUDA_TRY(cudaEventRecord(ws.evkv, st));
+    ws.timed_verify = true;
+    verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
+    ++launches;
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaEventRecord(ws.evk1, st));
+  }
+  keys_to_profile_kernel<<<static_cast<unsigned>((Nns + 255) / 256), 256, 0, st>>>(
+      d_keys, d_prof, want_corr ? d_corr : nullptr, Nns, kl);
+  ++launches;
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(h_prof.data(), d_prof, Nns * 8, cudaMemcpyDeviceToHost, st));
+  std::vector<double> h_corr;
+  if (want_corr) {
+    h_corr.resize(static_cast<size_t>(Nns));
+    CUDA_TRY(cudaMemcpyAsync(h_corr.data(), d_corr, Nns * 8, cudaMemcpyDeviceToHost, st));
+  }
+  CUDA_TRY(cudaEventRecord(ws.ev1, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  for (int k = 0; k < count; ++k) {
+    std::memcpy(res[k].profile_a, h_prof.data() + ser[k].off_ns, ser[k].ns * 8);
+    if (res[k].corr_a) std::memcpy(res[k].corr_a, h_corr.data() + ser[k].off_ns, ser[k].ns * 8);
+  }
+  scamp_c_result tot{};
+  read_times(ws, &tot);
+  for (int k = 0; k < count; ++k) {
+    res[k].elapsed_ms = tot.elapsed_ms;
+    res[k].join_kernel_ms = tot.join_kernel_ms;
+    res[k].verify_kernel_ms = tot.verify_kernel_ms;
+    res[k].comparisons = ser[k].cells;
+    res[k].gpu_launches = launches;
+    res[k].steps = tot.steps;
+    res[k].slow_steps = tot.slow_steps;
+    res[k].verifications = tot.verifications;
+  }
+  (void)cells_total;
+  return SCAMP_OK;
+}
+
+}  // namespace
+}  // namespace scamp_gb300
+
+extern "C" int scamp_gb300_join_batch(const scamp_c_args* args, scamp_c_result* res, int count,
+                                      char* errbuf, size_t errlen) {
+  std::string msg;
+  if (!args || !res || count <= 0) {
+    set_err(errbuf, errlen, "Error: empty batch");
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  for (int k = 0; k < count; ++k) {
+    const scamp_c_args* a = &args[k];
+    int rc = validate(a, &msg);
+    if (rc == SCAMP_OK) {
+      if (a->has_b || a->is_aligned || a->keep_rows_separate || !a->computing_rows ||
+          !a->computing_columns || a->distributed_start_row >= 0 || a->distributed_start_col >= 0)
+        msg = "Error: batched joins are plain self-joins (rows and columns into profile A)";
+      else if (a->profile_type != SCAMP_PROFILE_1NN_INDEX)
+        msg = "Error: batched joins compute 1NN_INDEX profiles";
+      else if (a->precision_type != SCAMP_PRECISION_MIXED && a->precision_type != SCAMP_PRECISION_SINGLE)
+        msg = "Error: batched joins run the mixed form (precision single or mixed)";
+      else if (a->device != args[0].device)
+        msg = "Error: a batch runs on one device";
+      else if (!res[k].profile_a)
+        msg = "Error: profile buffer missing";
+      if (!msg.empty()) rc = SCAMP_ERR_INVALID_ARGS;
+    }
+    if (rc) {
+      set_err(errbuf, errlen, "series " + std::to_string(k) + ": " + msg);
+      return rc;
+    }
+  }
+  Workspace* ws;
+  int rc = init_workspace(args[0].device, &ws, &msg);
+  if (rc) { set_err(errbuf, errlen, msg); return rc; }
+  std::lock_guard<std::mutex> lock(ws->mu);
+  rc = run_batch(*ws, args, res, count, ws->stream, &msg);
   if (rc) set_err(errbuf, errlen, msg);
   return rc;
 }

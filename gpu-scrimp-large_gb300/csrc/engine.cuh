@@ -115,6 +115,9 @@ struct Problem {
   double* sum_row;
   int64_t band_begin;   // first global band of this problem
   int64_t nbands;
+  int64_t m;            // window length
+  int64_t seg_len;      // K: rows per segment (mixed 1NN kernel)
+  float anchor_vcoef;   // initial drift estimate of an anchor / cov^2 (mixed 1NN)
 };
 
 constexpr int kMaxProblems = 2;
@@ -122,7 +125,7 @@ constexpr int kMaxProblems = 2;
 // A cell of the mixed 1NN join whose FP32 value is not trusted, settled after
 // the join by verify_requests_kernel.
 struct VerifyReq {
-  uint64_t i;   // row window | problem index << 62
+  uint64_t i;   // row window (low 40 bits) | problem index << 40
   uint32_t d;   // diagonal: column window = i + d
   float ub;     // upper bound of the cell's r (FP32 value + margin)
 };
@@ -131,6 +134,10 @@ struct VerifyReq {
 struct JoinParams {
   Problem prob[kMaxProblems];
   int nprob;
+  // Batched joins (mixed 1NN kernel): when nbatch > 0 the problems are the
+  // device array batch[0 .. nbatch) instead of prob[].
+  const Problem* batch;
+  int64_t nbatch;
   const int64_t* band_unit_prefix;  // [total_bands + 1] unit offsets
   int64_t total_bands;
   int64_t total_units;
@@ -159,10 +166,25 @@ __device__ __forceinline__ void decode_unit(const JoinParams& P, int64_t u,
     if (P.band_unit_prefix[mid] <= u) lo = mid; else hi = mid;
   }
   int p = 0;
-  while (p + 1 < P.nprob && lo >= P.prob[p + 1].band_begin) ++p;
+  if (P.nbatch > 0) {
+    // largest problem whose first band is <= lo
+    int64_t a = 0, b = P.nbatch;
+    while (b - a > 1) {
+      const int64_t mid = (a + b) >> 1;
+      if (P.batch[mid].band_begin <= lo) a = mid; else b = mid;
+    }
+    p = static_cast<int>(a);
+    *band = lo - P.batch[p].band_begin;
+  } else {
+    while (p + 1 < P.nprob && lo >= P.prob[p + 1].band_begin) ++p;
+    *band = lo - P.prob[p].band_begin;
+  }
   *prob = p;
-  *band = lo - P.prob[p].band_begin;
   *unit_in_band = u - P.band_unit_prefix[lo];
+}
+
+__device__ __forceinline__ const Problem& problem_of(const JoinParams& P, int p) {
+  return P.nbatch > 0 ? P.batch[p] : P.prob[p];
 }
 
 // Rows of band b (first diagonal D0): every row whose cell on D0 is inside.
@@ -175,6 +197,19 @@ __host__ __device__ __forceinline__ int64_t band_rows(int64_t n_r, int64_t n_c,
 // ---------------------------------------------------------------------------
 // Kernels (launch wrappers live in engine.cu).
 // ---------------------------------------------------------------------------
+// One series of a batched statistics launch.
+struct StatsJob {
+  const double* T_raw;
+  int64_t n, m;
+  int bshift;
+  double *T_clean, *mean, *inv, *df, *dg;
+  float *T32, *bhi, *blo, *mu_rel, *inv32, *df32, *dg32;
+};
+// Block b of the launch works for job j with block_prefix[j] <= b < block_prefix[j + 1].
+__global__ void stats_batch_kernel(const StatsJob* __restrict__ jobs,
+                                   const int64_t* __restrict__ block_prefix, int njobs,
+                                   int ultra, int chunk);
+
 __global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
                              int64_t m, int ultra, int chunk, int bshift,
                              double* __restrict__ T_clean, float* __restrict__ T32,

@@ -388,7 +388,7 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
           if (slot < static_cast<unsigned long long>(cx.vcap)) {
             publish(sm, cx, rv - mk, i, j, r0 + rr, cs, g);
             VerifyReq q;
-            q.i = static_cast<uint64_t>(i) | (static_cast<uint64_t>(cx.prob) << 62);
+            q.i = static_cast<uint64_t>(i) | (static_cast<uint64_t>(cx.prob) << 40);
             q.d = static_cast<uint32_t>(j - i);
             q.ub = rv + mk;
             cx.vreq[slot] = q;
@@ -420,8 +420,6 @@ join_mixed_1nn_kernel(JoinParams P) {
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   const int t = threadIdx.x;
   const int lane = t & 31, warp = t >> 5;
-  const int64_t K = P.seg_len;
-  const int64_t m = P.m;
   unsigned long long n_steps = 0, n_slow = 0, n_verify = 0;
   int qn = 0;  // queued blocks of this warp (warp-uniform)
 
@@ -433,7 +431,7 @@ join_mixed_1nn_kernel(JoinParams P) {
         int pi;
         int64_t bb, ubb;
         decode_unit(P, uu, &pi, &bb, &ubb);
-        sm.prob = P.prob[pi];
+        sm.prob = problem_of(P, pi);
         sm.prob_index = pi;
         sm.band = bb;
         sm.unit_in_band = ubb;
@@ -443,6 +441,8 @@ join_mixed_1nn_kernel(JoinParams P) {
     const int64_t u = sm.unit;
     if (u >= P.total_units) break;
     const Problem& pr = sm.prob;
+    const int64_t K = pr.seg_len;  // per problem: batched joins mix windows
+    const int64_t m = pr.m;
     const int64_t band = sm.band, ub = sm.unit_in_band;
     const int64_t D0 = pr.d_lo + band * kBand;
     const int64_t rows_b = band_rows(pr.R.ns, pr.C.ns, D0);
@@ -598,7 +598,7 @@ join_mixed_1nn_kernel(JoinParams P) {
     float2 Vt;
     {
       const float2 cm = absmax8(cov);
-      Vt = make_float2(P.anchor_vcoef * cm.x * cm.x, P.anchor_vcoef * cm.y * cm.y);
+      Vt = make_float2(pr.anchor_vcoef * cm.x * cm.x, pr.anchor_vcoef * cm.y * cm.y);
     }
     float2 W = make_float2(0.f, 0.f);
 
@@ -883,13 +883,13 @@ verify_requests_kernel(JoinParams P) {
   for (int64_t w = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
        w < n; w += nwarps) {
     const VerifyReq rq = P.vreq[w];
-    const Problem& pr = P.prob[rq.i >> 62];
-    const int64_t i = static_cast<int64_t>(rq.i & ((uint64_t{1} << 62) - 1));
+    const Problem& pr = problem_of(P, static_cast<int>(rq.i >> 40));
+    const int64_t i = static_cast<int64_t>(rq.i & ((uint64_t{1} << 40) - 1));
     const int64_t j = i + rq.d;
     const bool row_open = pr.key_row && rq.ub > key_corr_floor(pr.key_row[i], P.kl);
     const bool col_open = pr.key_col && rq.ub > key_corr_floor(pr.key_col[j], P.kl);
     if (!row_open && !col_open) continue;
-    const float cv = verify_cov_warp(pr.R, pr.C, i, j, P.m, lane);
+    const float cv = verify_cov_warp(pr.R, pr.C, i, j, pr.m, lane);
     if (lane == 0) {
       const float rv = (cv * pr.C.inv32[j]) * pr.R.inv32[i];
       const uint64_t q = q_from_float_bits(__float_as_uint(rv), P.kl.frac_bits);

@@ -39,7 +39,8 @@ __device__ __forceinline__ void acc2(double& s, double& c, double x) {
 
 }  // namespace
 
-__global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
+// Statistics of windows [tid * chunk, (tid + 1) * chunk) of one series.
+__device__ __forceinline__ void stats_body(int64_t tid, const double* __restrict__ T_raw, int64_t n,
                              int64_t m, int ultra, int chunk, int bshift,
                              double* __restrict__ T_clean, float* __restrict__ T32,
                              float* __restrict__ bhi, float* __restrict__ blo,
@@ -49,7 +50,6 @@ __global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
                              float* __restrict__ inv32, float* __restrict__ df32,
                              float* __restrict__ dg32) {
   const int64_t ns = n - m + 1;
-  const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   const int64_t w0 = tid * chunk;
   if (w0 >= ns) return;
   const int64_t w1 = (w0 + chunk < ns) ? w0 + chunk : ns;
@@ -177,6 +177,36 @@ __global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
     mu_lo = mu_next_lo;
     last_bad = last_bad_next;
   }
+}
+
+
+__global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
+                             int64_t m, int ultra, int chunk, int bshift,
+                             double* __restrict__ T_clean, float* __restrict__ T32,
+                             float* __restrict__ bhi, float* __restrict__ blo,
+                             float* __restrict__ mu_rel,
+                             double* __restrict__ mean, double* __restrict__ inv,
+                             double* __restrict__ df, double* __restrict__ dg,
+                             float* __restrict__ inv32, float* __restrict__ df32,
+                             float* __restrict__ dg32) {
+  const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  stats_body(tid, T_raw, n, m, ultra, chunk, bshift, T_clean, T32, bhi, blo, mu_rel, mean, inv,
+             df, dg, inv32, df32, dg32);
+}
+
+__global__ void stats_batch_kernel(const StatsJob* __restrict__ jobs,
+                                   const int64_t* __restrict__ block_prefix, int njobs,
+                                   int ultra, int chunk) {
+  const int64_t b = blockIdx.x;
+  int lo = 0, hi = njobs;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (block_prefix[mid] <= b) lo = mid; else hi = mid;
+  }
+  const StatsJob& j = jobs[lo];
+  const int64_t tid = (b - block_prefix[lo]) * blockDim.x + threadIdx.x;
+  stats_body(tid, j.T_raw, j.n, j.m, ultra, chunk, j.bshift, j.T_clean, j.T32, j.bhi, j.blo,
+             j.mu_rel, j.mean, j.inv, j.df, j.dg, j.inv32, j.df32, j.dg32);
 }
 
 }  // namespace scamp_gb300

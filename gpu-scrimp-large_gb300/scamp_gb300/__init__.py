@@ -218,6 +218,50 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
             "gpu_launches": int(res.gpu_launches)}
 
 
+def join_batch(series, windows, precision="mixed", return_corr=False, device=0):
+    """scamp_gb300_join_batch: independent 1NN_INDEX self-joins of every
+    series in ``series`` (window ``windows[k]``, or one int for all) in one
+    batched call.  Returns a list of dicts with ``profile_a`` (packed
+    entries), ``corr_a`` (with ``return_corr``) and the batch's timings."""
+    lib = _lib.load()
+    n = len(series)
+    if isinstance(windows, (int, np.integer)):
+        windows = [int(windows)] * n
+    if len(windows) != n:
+        raise ValueError("one window per series")
+    arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in series]
+    cargs = (_lib.CArgs * n)()
+    cres = (_lib.CResult * n)()
+    profs, corrs = [], []
+    for k, (x, m) in enumerate(zip(arrs, windows)):
+        ca = _args(x, None, m, "1NN_INDEX", precision, True, True, False, False, 0.0,
+                   -1, -1, max(128000, 2 * int(m)), 0, device, True)
+        ctypes.memmove(ctypes.byref(cargs[k]), ctypes.byref(ca), ctypes.sizeof(ca))
+        ns = len(x) - int(m) + 1
+        p = np.full(max(ns, 0), NO_MATCH, dtype=np.uint64)
+        profs.append(p)
+        cres[k].profile_a = p.ctypes.data if ns > 0 else None
+        if return_corr:
+            c = np.empty(max(ns, 0), dtype=np.float64)
+            corrs.append(c)
+            cres[k].corr_a = c.ctypes.data if ns > 0 else None
+    err = ctypes.create_string_buffer(1024)
+    rc = lib.scamp_gb300_join_batch(cargs, cres, n, err, 1024)
+    _check(rc, err)
+    out = []
+    for k in range(n):
+        d = {"profile_a": profs[k], "comparisons": int(cres[k].comparisons),
+             "elapsed_ms": cres[k].elapsed_ms, "join_kernel_ms": cres[k].join_kernel_ms,
+             "gpu_launches": int(cres[k].gpu_launches),
+             "counters": {"steps": int(cres[k].steps), "slow_steps": int(cres[k].slow_steps),
+                          "verifications": int(cres[k].verifications),
+                          "verify_kernel_ms": float(cres[k].verify_kernel_ms)}}
+        if return_corr:
+            d["corr_a"] = corrs[k]
+        out.append(d)
+    return out
+
+
 def unpack_profile(packed):
     """(float32 correlation, int64 index) from packed 1NN_INDEX entries;
     index -1 where there was no match."""

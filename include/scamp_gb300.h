@@ -120,6 +120,17 @@ int scamp_gb300_join(const scamp_c_args *args, scamp_c_result *res,
 int scamp_gb300_join_dev(const scamp_c_args *args, scamp_c_result *res,
                          void *stream, char *errbuf, size_t errlen);
 
+/* Many independent self-joins in one call: count series (args[k], host
+ * buffers, has_b = 0, computing rows and columns, no keep_rows, 1NN_INDEX,
+ * precision SINGLE or MIXED, one device), each merged into res[k].profile_a
+ * (and res[k].corr_a when set).  All series run in one persistent launch of
+ * the mixed band kernel, with one statistics, key-conversion and
+ * verification launch for the whole batch.  Timing fields and work counters
+ * of every res[k] describe the whole batch; comparisons are per series.
+ * Extends do_SCAMP (src/SCAMP.cpp:261-334), which takes one join per call. */
+int scamp_gb300_join_batch(const scamp_c_args *args, scamp_c_result *res, int count,
+                           char *errbuf, size_t errlen);
+
 /* The FP64 form of scamp_gb300_join_dev without any allocation: every
  * intermediate buffer lives in one static device array of the library
  * (about 8.6 MB per device), so the join calls no allocator.  For callers
