@@ -194,6 +194,103 @@ def cpu_baseline_leg():
             "sample": sample + ", %.1f s" % dt}
 
 
+BATCH_WORKLOAD = ("4096 independent self-joins: lengths round(2^U[10,16]), random walks scaled by "
+                  "LogU(1e-3,1e3) and offset by U(-1e4,1e4), windows from {32,64,128}, 1NN_INDEX")
+
+
+def run_batch_workload(args, world, rank, local):
+    """--workload batch: every series of the batch in one scamp_gb300_join_batch
+    call (host buffers in and out, so value and e2e are both whole calls);
+    beside it the same series joined one call at a time, a sample checked
+    against FP64 single joins, and the CPU port on a sample of series."""
+    import torch
+
+    import scamp_gb300
+    from scamp_gb300 import workloads
+
+    torch.cuda.set_device(local)
+    batch = workloads.cfg4_batch()
+    series = [x for x, _ in batch]
+    windows = [m for _, m in batch]
+    for _ in range(max(args.warmup, 3)):
+        out = scamp_gb300.join_batch(series, windows, "mixed", device=local)
+    cells = sum(r["comparisons"] for r in out)
+    dev_ms, wall = [], []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            out = scamp_gb300.join_batch(series, windows, "mixed", return_corr=True, device=local)
+            wall.append(time.perf_counter() - t0)
+            dev_ms.append(out[0]["elapsed_ms"])
+    clocks = clk.summary()
+    ms_step = sum(dev_ms) / len(dev_ms)
+    wall_s = sum(wall) / len(wall)
+    # the same series one join per call
+    t0 = time.perf_counter()
+    for x, m in batch:
+        scamp_gb300.join(x, None, m, "1NN_INDEX", "mixed", device=local)
+    loop_s = time.perf_counter() - t0
+    # accuracy: FP64 single joins of a sample of the series
+    max_err, agree, nv = 0.0, 0, 0
+    for k in range(0, len(batch), 128):
+        x, m = batch[k]
+        f = scamp_gb300.join(x, None, m, "1NN_INDEX", "double", return_corr=True, device=local)
+        ok = f["corr_a"] >= -1
+        if ok.any():
+            max_err = max(max_err, float(np.max(np.abs(out[k]["corr_a"][ok] - f["corr_a"][ok]))))
+            _, i1 = scamp_gb300.unpack_profile(out[k]["profile_a"])
+            _, i2 = scamp_gb300.unpack_profile(f["profile_a"])
+            agree += int(np.sum(i1[ok] == i2[ok]))
+            nv += int(ok.sum())
+    peak32 = scamp_gb300.pipe_peak("fp32", local)
+    k_ms = out[0]["join_kernel_ms"] - out[0]["counters"]["verify_kernel_ms"]
+    achieved = cells * OPS_PER_CELL / (k_ms * 1e-3)
+    if rank != 0:
+        return
+    h2d = sum(len(x) * 8 + (len(x) - m + 1) * 8 for x, m in batch)
+    d2h = sum((len(x) - m + 1) * 16 for x, m in batch)
+    line = {
+        "metric": METRIC, "value": cells / (ms_step * 1e-3), "unit": "comparisons/s",
+        "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": BATCH_WORKLOAD, "form": "mixed, one scamp_gb300_join_batch call",
+                   "comparisons_per_step": cells, "series": len(batch),
+                   "timing": "device events from the first H2D copy to the last D2H copy"},
+        "max_abs_r_err_vs_fp64_sample": max_err,
+        "index_agreement_vs_fp64_sample": agree / max(nv, 1),
+        "one_call_per_series_s": loop_s,
+        "batched_speedup_vs_one_call_per_series": loop_s / wall_s,
+        "roofline": {"bound": "fp32_fma_pipe", "achieved": achieved / 1e12, "peak": peak32 / 1e12,
+                     "unit": "Tops/s", "frac": achieved / peak32, "traffic": None,
+                     "kernel": "join_mixed_1nn_kernel", "kernel_ms": k_ms,
+                     "ops_per_comparison": OPS_PER_CELL},
+        "e2e": {"value": cells / wall_s, "unit": "comparisons/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": out[0]["gpu_launches"] * args.steps,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle
+
+        oracle.load()
+        threads = oracle.max_threads()
+        sample = batch[:256]
+        c_cells = 0
+        t0 = time.perf_counter()
+        for x, m in sample:
+            oracle.join(x, None, m, threads=threads)
+            ns = len(x) - m + 1
+            e = m // 4
+            c_cells += max(ns - e, 0) * max(ns - e + 1, 0) // 2
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": c_cells / dt, "unit": "comparisons/s", "cores": threads,
+                                "kind": "port", "sample": "first 256 series of the batch, DOUBLE, "
+                                                          "%.1f s" % dt}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -202,7 +299,7 @@ def main():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--fp64-steps", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="ab", choices=["ab", "self"],
+    p.add_argument("--workload", default="ab", choices=["ab", "self", "batch"],
                    help="ab: the headline AB-join (default); self: the 2^24-point m=1024 "
                         "self-join of the precision study")
     p.add_argument("--na-log2", type=int, default=None,
@@ -225,6 +322,9 @@ def main():
 
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload == "batch":
+        run_batch_workload(args, world, rank, local)
         return
 
     import torch
