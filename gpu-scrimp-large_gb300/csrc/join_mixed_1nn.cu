@@ -47,6 +47,13 @@ constexpr int kSteps = kSlab / kRows;
 constexpr int kCols = kSlab + kBand;      // staged columns per slab
 constexpr int kBlocks = kCols / 8;        // 8-column blocks
 constexpr int kPad = kCols + kBlocks;     // padded slot c + c/8
+// The staged columns form a ring over the unit's rows: slab q holds unit
+// columns 128 q .. 128 q + kCols - 1 at ring columns (128 q + c) mod kCols, so
+// a slab stages only the kSlab columns entering it.  Ring columns
+// 0 .. kGhost - 1 are repeated after the end, so that a step's 15-column
+// window never wraps.
+constexpr int kGhost = 16;
+constexpr int kPadG = kCols + kGhost + (kCols + kGhost) / 8;
 constexpr int kAnchorChunk = 512;         // row-window samples per anchor pass
 constexpr int kYSpan = kBand + kAnchorChunk + 16;     // staged column samples
 constexpr int kYPad = (kYSpan / 8) * 10;              // padded: 10 pairs per 8
@@ -123,6 +130,7 @@ struct SlowCtx {
   const Problem* pr;
   int64_t rbase[2];
   int64_t D0;  // first diagonal of the unit; thread t owns D0 + t*kDiags ..
+  int ring0;   // ring column of the slab's first staged column
   int64_t m;
   KeyLayout kl;
   int prob;                        // index of the problem in JoinParams
@@ -137,9 +145,9 @@ struct Smem {
       // {df.x, df.y} and {dg.x, dg.y} per staged column pair: separate
       // 8-byte arrays, so that 64-bit loads at a stride of 9 slots meet no
       // bank conflict
-      float2 c_df[kPad];
-      float2 c_dg[kPad];
-      float2 c_iv[kPad];  // {inv.x, inv.y}
+      float2 c_df[kPadG];
+      float2 c_dg[kPadG];
+      float2 c_iv[kPadG];  // {inv.x, inv.y}
     } s;
     struct {
       float2 xr[kAnchorChunk];    // centred row windows of both segments (chunk)
@@ -148,9 +156,11 @@ struct Smem {
     } a;
   } u;
   float2 c_best[kCols];
-  float2 c_blkmin[kBlocks];
-  float2 c_blkmax_iv[kBlocks];
-  float4 c_blkmax_fg[kBlocks];  // max |df|, |dg| per 8-column block
+  // per 8-column ring block (entry kBlocks repeats block 0): smallest best,
+  // largest inverse norm, largest |df|, |dg|
+  float2 c_blkmin[kBlocks + 1];
+  float2 c_blkmax_iv[kBlocks + 1];
+  float4 c_blkmax_fg[kBlocks + 1];
   float4 r_fg[kSlab];
   float2 r_iv[kSlab];
   float2 r_best[kSlab];
@@ -217,6 +227,11 @@ static_assert(kCols % kThreads == 0, "whole warps stage the columns");
 static_assert(sizeof(Smem) + 1024 <= 228 * 1024 / 4, "shared memory exceeds 4 CTAs/SM");
 
 __device__ __forceinline__ int padc(int c) { return c + (c >> 3); }
+// Ring column of slab-relative column c (0 <= c < kCols).
+__device__ __forceinline__ int ringc(int ring0, int c) {
+  const int r = ring0 + c;
+  return r >= kCols ? r - kCols : r;
+}
 
 // {df.x, df.y, dg.x, dg.y} of the staged column in padded slot `slot`.
 __device__ __forceinline__ float4 col_fg(const Smem& sm, int slot) {
@@ -350,7 +365,7 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
 #pragma unroll 8
     for (int rr = nrows - 1; rr >= 0; --rr) {
       const float4 rf = sm.r_fg[r0 + rr];
-      const float4 cf = col_fg(sm, padc(cb0 + rr));
+      const float4 cf = col_fg(sm, padc(ringc(cx.ring0, cb0 + rr)));
       const float dfr = g ? rf.y : rf.x, dgr = g ? rf.w : rf.z;
       const float dfc = g ? cf.y : cf.x, dgc = g ? cf.w : cf.z;
       c = fmaf(-dfr, dgc, c);
@@ -362,15 +377,16 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
       const bool live = rw < nrows;
       const int rr = live ? rw : 0;  // rows past the block's end read row 0
       const int cs = cb0 + rr;
+      const int rcs = ringc(cx.ring0, cs);  // its ring column
       const float4 rf = sm.r_fg[r0 + rr];
-      const float4 cf = col_fg(sm, padc(cs));
+      const float4 cf = col_fg(sm, padc(rcs));
       const float2 ivr2 = sm.r_iv[r0 + rr];
-      const float2 ivc2 = sm.u.s.c_iv[padc(cs)];
+      const float2 ivc2 = sm.u.s.c_iv[padc(rcs)];
       const float ivr = g ? ivr2.y : ivr2.x, ivc = g ? ivc2.y : ivc2.x;
       const float rv = (c * ivc) * ivr;  // the fast path's rounding
       const float mk = vk * ivc * ivr;
       const float rb = g ? sm.r_best[r0 + rr].y : sm.r_best[r0 + rr].x;
-      const float cbv = g ? sm.c_best[cs].y : sm.c_best[cs].x;
+      const float cbv = g ? sm.c_best[rcs].y : sm.c_best[rcs].x;
       const bool cand = live && rv + mk > fminf(rb, cbv);
       const bool req = cand && mk > kTrust;
       const unsigned rmask = __ballot_sync(0xffffffffu, req);
@@ -386,7 +402,7 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
         if (req) {
           ++nreq;
           if (slot < static_cast<unsigned long long>(cx.vcap)) {
-            publish(sm, cx, rv - mk, i, j, r0 + rr, cs, g);
+            publish(sm, cx, rv - mk, i, j, r0 + rr, rcs, g);
             VerifyReq q;
             q.i = static_cast<uint64_t>(i) | (static_cast<uint64_t>(cx.prob) << 40);
             q.d = static_cast<uint32_t>(j - i);
@@ -394,10 +410,10 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
             cx.vreq[slot] = q;
           } else {
             publish(sm, cx, verify_cov_lane(pr.R, pr.C, i, j, cx.m) * ivc * ivr, i, j,
-                    r0 + rr, cs, g);
+                    r0 + rr, rcs, g);
           }
         } else {
-          publish(sm, cx, rv, i, j, r0 + rr, cs, g);
+          publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
         }
       }
       const float dfr = g ? rf.y : rf.x, dgr = g ? rf.w : rf.z;
@@ -626,13 +642,17 @@ join_mixed_1nn_kernel(JoinParams P) {
         cbase_g[g] = rbase[g] + D0;
         if (t == 0) sm.cx.rbase[g] = rbase[g];
       }
+      const int ring0 = static_cast<int>((q * kSlab) % kCols);
+      const int rq = ring0 >> 3;  // ring block of the slab's first column
+      if (t == 0) sm.cx.ring0 = ring0;
       // Staging, coalesced: thread t stages columns t, t + kThreads, ... and
       // row t.  The filter tables are reduced on the way, 8 lanes (8
       // consecutive columns or rows) at a time: per 8-column block and per
       // 8-row step the smallest best, the largest inverse norm and the
       // largest |df|, |dg|.
 #pragma unroll 3
-      for (int c = t; c < kCols; c += kThreads) {
+      for (int c = (q == 0 ? 0 : kCols - kSlab) + t; c < kCols; c += kThreads) {
+        const int rc = ringc(ring0, c);
         const int64_t j0 = cbase_g[0] + c, j1 = cbase_g[1] + c;
         const bool ok0 = seg_len[0] > 0 && j0 < pr.C.ns;
         const bool ok1 = seg_len[1] > 0 && j1 < pr.C.ns;
@@ -647,16 +667,27 @@ join_mixed_1nn_kernel(JoinParams P) {
         float2 cbv;
         cbv.x = (pr.key_col && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_col[j0], P.kl) : kNoTarget;
         cbv.y = (pr.key_col && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_col[j1], P.kl) : kNoTarget;
-        sm.u.s.c_df[padc(c)] = make_float2(f.x, f.y);
-        sm.u.s.c_dg[padc(c)] = make_float2(f.z, f.w);
-        sm.u.s.c_iv[padc(c)] = iv;
-        sm.c_best[c] = cbv;
+        sm.u.s.c_df[padc(rc)] = make_float2(f.x, f.y);
+        sm.u.s.c_dg[padc(rc)] = make_float2(f.z, f.w);
+        sm.u.s.c_iv[padc(rc)] = iv;
+        if (rc < kGhost) {
+          sm.u.s.c_df[padc(rc + kCols)] = make_float2(f.x, f.y);
+          sm.u.s.c_dg[padc(rc + kCols)] = make_float2(f.z, f.w);
+          sm.u.s.c_iv[padc(rc + kCols)] = iv;
+        }
+        sm.c_best[rc] = cbv;
         TableEntry e = table_entry(f, iv, cbv);
-        reduce8(e);
+        reduce8(e);  // 8 lanes = one aligned ring block
         if ((lane & 7) == 0) {
-          sm.c_blkmin[c >> 3] = e.mn;
-          sm.c_blkmax_iv[c >> 3] = e.mx;
-          sm.c_blkmax_fg[c >> 3] = e.mf;
+          const int b = rc >> 3;
+          sm.c_blkmin[b] = e.mn;
+          sm.c_blkmax_iv[b] = e.mx;
+          sm.c_blkmax_fg[b] = e.mf;
+          if (b == 0) {
+            sm.c_blkmin[kBlocks] = e.mn;
+            sm.c_blkmax_iv[kBlocks] = e.mx;
+            sm.c_blkmax_fg[kBlocks] = e.mf;
+          }
         }
       }
       {
@@ -684,39 +715,6 @@ join_mixed_1nn_kernel(JoinParams P) {
         }
       }
       __syncthreads();
-      // Column tables over 16 columns: a step of thread t reads the 15
-      // columns from 8(s + t), entry s + t = blocks s + t and s + t + 1.
-      {
-        TableEntry e[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int b = t + h * kThreads;
-          if (b < kBlocks) {
-            e[h].mn = sm.c_blkmin[b];
-            e[h].mx = sm.c_blkmax_iv[b];
-            e[h].mf = sm.c_blkmax_fg[b];
-            if (b + 1 < kBlocks) {
-              TableEntry o;
-              o.mn = sm.c_blkmin[b + 1];
-              o.mx = sm.c_blkmax_iv[b + 1];
-              o.mf = sm.c_blkmax_fg[b + 1];
-              combine(e[h], o);
-            }
-          }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int b = t + h * kThreads;
-          if (b < kBlocks) {
-            sm.c_blkmin[b] = e[h].mn;
-            sm.c_blkmax_iv[b] = e[h].mx;
-            sm.c_blkmax_fg[b] = e[h].mf;
-          }
-        }
-      }
-      __syncthreads();
-
       // ---------------- steps ----------------
       // Steps run in pairs.  The thread's column window is carried from the
       // first step of a pair to the second (the last 7 columns of step s are
@@ -732,11 +730,16 @@ join_mixed_1nn_kernel(JoinParams P) {
       auto step = [&](const int s, auto parity) {
         constexpr int P = decltype(parity)::value;
         const int r0 = s * kRows;
-        const int base = 9 * (s + t);  // padded slot of staged column 8(s+t)
-        // filter threshold and margin
-        const float2 bm = sm.c_blkmin[s + t];
+        // ring block of the step's first column 8(s + t)
+        const int rb = (rq + s + t) < kBlocks ? (rq + s + t) : (rq + s + t - kBlocks);
+        const int base = 9 * rb;  // its padded slot
+        // filter threshold and margin: the step's 15 columns lie in ring
+        // blocks rb and rb + 1
+        const float2 bm0 = sm.c_blkmin[rb], bm1 = sm.c_blkmin[rb + 1];
+        const float2 bm = make_float2(fminf(bm0.x, bm1.x), fminf(bm0.y, bm1.y));
         const float2 rsm = sm.r_stepmin[s];
-        const float2 icm = sm.c_blkmax_iv[s + t];
+        const float2 ic0 = sm.c_blkmax_iv[rb], ic1 = sm.c_blkmax_iv[rb + 1];
+        const float2 icm = make_float2(fmaxf(ic0.x, ic1.x), fmaxf(ic0.y, ic1.y));
         const float2 irm = sm.r_stepmax_iv[s];
         {
           const float2 cm = absmax8(cov);
@@ -744,7 +747,9 @@ join_mixed_1nn_kernel(JoinParams P) {
         }
         {
           // bound of |df_c dg_r| + |df_r dg_c| over the step's cells
-          const float4 cfm = sm.c_blkmax_fg[s + t];
+          const float4 cf0 = sm.c_blkmax_fg[rb], cf1 = sm.c_blkmax_fg[rb + 1];
+          const float4 cfm = make_float4(fmaxf(cf0.x, cf1.x), fmaxf(cf0.y, cf1.y),
+                                         fmaxf(cf0.z, cf1.z), fmaxf(cf0.w, cf1.w));
           const float4 rfm = sm.r_stepmax_fg[s];
           const float2 inc = fma2(make_float2(rfm.x, rfm.y), make_float2(cfm.z, cfm.w),
                                   mul2(make_float2(rfm.z, rfm.w), make_float2(cfm.x, cfm.y)));
@@ -816,10 +821,13 @@ join_mixed_1nn_kernel(JoinParams P) {
       };
 #pragma unroll 1
       for (int s = 0; s < kSteps; s += 2) {
+        {
+          const int rb = (rq + s + t) < kBlocks ? (rq + s + t) : (rq + s + t - kBlocks);
 #pragma unroll
-        for (int x = 0; x < kDiags - 1; ++x) {
-          cfw[x] = col_fg(sm, 9 * (s + t) + x);  // padc(8(s + t) + x), x < 8
-          ciw[x] = sm.u.s.c_iv[9 * (s + t) + x];
+          for (int x = 0; x < kDiags - 1; ++x) {
+            cfw[x] = col_fg(sm, 9 * rb + x);  // padc(ring column 8 rb + x), x < 8
+            ciw[x] = sm.u.s.c_iv[9 * rb + x];
+          }
         }
         step(s, Parity<0>());
         step(s + 1, Parity<1>());
