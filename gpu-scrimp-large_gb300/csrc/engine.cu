@@ -40,13 +40,13 @@ int measure_pipe_peak(int device, int kind, double* ops_per_s);
 
 namespace {
 
-// Rows between re-anchors of the mixed form: 4 m within [1024, 4096], the
-// measured best.  AB-join of 2^20 x 2^19 random walks, m = 256: K = 512
-// 149 ms, 768 141, 1024 137.5, 1536 139.  Self-join of 2^22 noisy random walk,
-// m = 1024: K = 1024 2.45 s, 2048 2.08, 4096 1.89.  The max |r| error stays
-// below 5e-6 (6e-6) throughout.
+// Rows between re-anchors of the mixed form: 8 m within [1024, 4096], the
+// measured best.  AB-join of 2^20 x 2^19 random walks, m = 256, with seeds and
+// kTrust = 5e-6: K = 1024 114.4 ms, 1536 109.6, 2048 107.4 (max |r| error
+// 5.7e-6, 5.7e-6, 6.6e-6).  Self-join of a 2^22 noisy random walk, m = 1024:
+// K = 1024 2.45 s, 2048 2.08, 4096 1.89 (max error 4.9e-6).
 int64_t default_anchor_interval(int64_t m) {
-  return std::min<int64_t>(4096, std::max<int64_t>(1024, 4 * m));
+  return std::min<int64_t>(4096, std::max<int64_t>(1024, 8 * m));
 }
 
 struct Error {
