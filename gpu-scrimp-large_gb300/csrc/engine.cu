@@ -49,6 +49,11 @@ int64_t default_anchor_interval(int64_t m) {
   return std::min<int64_t>(4096, std::max<int64_t>(1024, 8 * m));
 }
 
+// Rows between seeds of the FP64 form.  The FP64 recurrence drifts by
+// ~2^-53 per row, so seeds only bound the work lost to them: 32 m rows keep
+// the direct-dot seeds at 1/32 of the FP64 pipe's work.
+int64_t fp64_segment(int64_t m) { return std::max<int64_t>(32 * m, 8192); }
+
 struct Error {
   int code;
   std::string msg;
@@ -513,16 +518,16 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, nthreads, smem));
   occ = std::max(occ, 1);
   const int64_t resident = static_cast<int64_t>(ws.sms) * occ;
-  // Segment length K: the anchor interval for the mixed form; for FP64 long
-  // enough that seeds cost ~1/32 of the cells.  Both shrink (down to one
-  // slab) when the join is too small to give every resident CTA ~8 units.
+  // Segment length K: the anchor interval for the mixed form, the seed
+  // interval (fp64_segment) for FP64.  Both shrink (down to one slab) when
+  // the join is too small to give every resident CTA ~8 units.
   int64_t K;
   const double cells_d = static_cast<double>(plan.cells);
   const int64_t k_lb = static_cast<int64_t>(cells_d / (8.0 * resident * 2.0 * W));
   if (mixed) {
     K = a->anchor_interval > 0 ? a->anchor_interval : default_anchor_interval(m);
   } else {
-    K = std::max<int64_t>(8 * m, 2048);
+    K = fp64_segment(m);
   }
   K = std::min(K, std::max<int64_t>(k_lb, slab));
   K = std::max<int64_t>(slab, (K / slab) * slab);
@@ -1023,7 +1028,7 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
   // segment length: the FP64 rule of run_device()
   const double cells_d = static_cast<double>(plan.cells);
   const int64_t k_lb = static_cast<int64_t>(cells_d / (8.0 * resident * 2.0 * W));
-  int64_t K = std::max<int64_t>(8 * m, 2048);
+  int64_t K = fp64_segment(m);
   K = std::min(K, std::max<int64_t>(k_lb, slab));
   K = std::max<int64_t>(slab, (K / slab) * slab);
   {
