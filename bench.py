@@ -52,6 +52,24 @@ OPS_PER_CELL = 4
 DRAM_BYTES_PER_LAUNCH = 51.12e6 + 109.69e6
 
 
+def max_over_ranks(x, dist, device):
+    """The largest per-rank value (seconds or ms of a step): replicas are
+    timed by their slowest rank.  `dist` is torch.distributed or None."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.item()
+
+
+def replica_value(cells_per_rank, world, step_seconds):
+    """Whole-job comparisons/s of N replicas: all ranks' cells over the
+    slowest rank's step time (weak scaling)."""
+    return cells_per_rank * world / step_seconds
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -198,6 +216,55 @@ BATCH_WORKLOAD = ("4096 independent self-joins: lengths round(2^U[10,16]), rando
                   "LogU(1e-3,1e3) and offset by U(-1e4,1e4), windows from {32,64,128}, 1NN_INDEX")
 
 
+GAPS_WORKLOAD = ("self-join: random walk n=2^23 with 1% of samples in NaN gaps of length "
+                 "U[1,500], m=4096, 1NN_INDEX and SUM_THRESH (r > 0.9)")
+GAPS_FP64_PREFIX = 1 << 21
+
+
+def run_gaps_workload(args, world, rank, local):
+    """--workload gaps: the very large self-join's distribution at 2^23
+    samples (the 2^27-sample join takes ~30 minutes per form): mixed 1NN and
+    SUM_THRESH on the whole series; FP64 and the mixed-vs-FP64 errors on the
+    first 2^21 samples."""
+    import scamp_gb300
+    from scamp_gb300 import workloads
+
+    x, m = workloads.cfg5_gaps(n=1 << 23, m=4096)
+    res = {}
+    for prof in ("1NN_INDEX", "SUM_THRESH"):
+        r = None
+        for _ in range(max(args.warmup, 1) + 1):
+            r = scamp_gb300.join(x, None, m, prof, "mixed", threshold=0.9, device=local)
+        res[prof] = {"value": r["comparisons"] / (r["elapsed_ms"] * 1e-3), "ms": r["elapsed_ms"],
+                     "comparisons": r["comparisons"]}
+        xp = x[:GAPS_FP64_PREFIX]
+        mp = scamp_gb300.join(xp, None, m, prof, "mixed", threshold=0.9, return_corr=True,
+                              device=local)
+        fp = scamp_gb300.join(xp, None, m, prof, "double", threshold=0.9, return_corr=True,
+                              device=local)
+        res[prof]["fp64_value"] = fp["comparisons"] / (fp["elapsed_ms"] * 1e-3)
+        if prof == "1NN_INDEX":
+            ok = fp["corr_a"] >= -1
+            _, i1 = scamp_gb300.unpack_profile(mp["profile_a"])
+            _, i2 = scamp_gb300.unpack_profile(fp["profile_a"])
+            res[prof]["max_abs_r_err"] = float(np.max(np.abs(mp["corr_a"][ok] - fp["corr_a"][ok])))
+            res[prof]["index_agreement"] = float(np.mean(i1[ok] == i2[ok]))
+        else:
+            d = np.abs(mp["sum_a"] - fp["sum_a"])
+            res[prof]["max_abs_sum_diff"] = float(d.max())
+            res[prof]["mean_sum"] = float(np.mean(fp["sum_a"]))
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": res["1NN_INDEX"]["value"], "unit": "comparisons/s",
+            "n_gpus": 1, "steps": 1, "warmup": max(args.warmup, 1),
+            "ms_per_step": res["1NN_INDEX"]["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": GAPS_WORKLOAD,
+                       "fp64": "first 2^21 samples (FP64 and the error checks)"},
+            "forms": res}
+    print(json.dumps(line), flush=True)
+
+
 def run_batch_workload(args, world, rank, local):
     """--workload batch: every series of the batch in one scamp_gb300_join_batch
     call (host buffers in and out, so value and e2e are both whole calls);
@@ -299,7 +366,7 @@ def main():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--fp64-steps", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="ab", choices=["ab", "self", "batch"],
+    p.add_argument("--workload", default="ab", choices=["ab", "self", "batch", "gaps"],
                    help="ab: the headline AB-join (default); self: the 2^24-point m=1024 "
                         "self-join of the precision study")
     p.add_argument("--na-log2", type=int, default=None,
@@ -325,6 +392,12 @@ def main():
         return
     if args.workload == "batch":
         run_batch_workload(args, world, rank, local)
+        return
+    if args.workload == "gaps":
+        import torch
+
+        torch.cuda.set_device(local)
+        run_gaps_workload(args, world, rank, local)
         return
 
     import torch
@@ -401,12 +474,8 @@ def main():
     if args.profile_only:
         return
     cells = r["comparisons"]
-    ms_step = sum(times) / len(times)
-    if dist is not None:
-        t = torch.tensor([ms_step], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = t.item()
-    value = cells * world / (ms_step * 1e-3)
+    ms_step = max_over_ranks(sum(times) / len(times), dist, dev)
+    value = replica_value(cells, world, ms_step * 1e-3)
     mixed_corr = (corr_a.cpu().numpy().copy(), corr_b.cpu().numpy().copy())
     mixed_idx = (prof_a.cpu().numpy().view(np.uint64) >> np.uint64(32),
                  prof_b.cpu().numpy().view(np.uint64) >> np.uint64(32))
@@ -463,11 +532,7 @@ def main():
         if it >= args.warmup:
             e2e_t.append(dt)
             launches_e2e = r["gpu_launches"]
-    e2e_s = sum(e2e_t) / len(e2e_t)
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = t.item()
+    e2e_s = max_over_ranks(sum(e2e_t) / len(e2e_t), dist, dev)
     if self_join:
         h2d, d2h = NA * 8 + nsa * 8, nsa * 8
     else:
@@ -519,7 +584,7 @@ def main():
                      "verify_kernel_ms": sum(verify_ms) / len(verify_ms),
                      "work_counters": r["counters"],
                      "peak_source": "measured packed-FP32 FMA probe (scamp_gb300_pipe_peak)"},
-        "e2e": {"value": cells * world / e2e_s, "unit": "comparisons/s",
+        "e2e": {"value": replica_value(cells, world, e2e_s), "unit": "comparisons/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clocks,

@@ -45,8 +45,10 @@ namespace {
 // kTrust = 5e-6: K = 1024 114.4 ms, 1536 109.6, 2048 107.4 (max |r| error
 // 5.7e-6, 5.7e-6, 6.6e-6).  Self-join of a 2^22 noisy random walk, m = 1024:
 // K = 1024 2.45 s, 2048 2.08, 4096 1.89 (max error 4.9e-6).
+// Windows longer than 2048 allow 2 m rows (anchors then cost 1/8 of the
+// steps' FMA work, as at m = 256).
 int64_t default_anchor_interval(int64_t m) {
-  return std::min<int64_t>(4096, std::max<int64_t>(1024, 8 * m));
+  return std::min<int64_t>(std::max<int64_t>(4096, 2 * m), std::max<int64_t>(1024, 8 * m));
 }
 
 // Rows between seeds of the FP64 form.  The FP64 recurrence drifts by
