@@ -28,10 +28,6 @@ namespace scamp_gb300 {
 int fp64_band_width();
 int fp64_slab_rows();
 int fp64_threads();
-int mixed_band_width();
-int mixed_slab_rows();
-int mixed_threads();
-size_t mixed_smem_bytes();
 int mixed_1nn_band_width();
 int mixed_1nn_slab_rows();
 int mixed_1nn_threads();
@@ -498,21 +494,17 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   }
 
   // ---- work plan ----
-  // Kernel choice: FP64 form; mixed 1NN_INDEX (FP32 filter + verified
-  // candidates); mixed SUM_THRESH (FP32, every cell accumulated).
-  enum { K_FP64, K_MIXED_1NN, K_MIXED_SUM } kind =
-      !mixed ? K_FP64 : (is_1nn ? K_MIXED_1NN : K_MIXED_SUM);
+  // Kernel choice: FP64 form, or the mixed band kernel (FP32 filter; for
+  // 1NN_INDEX its candidates are verified, for SUM_THRESH the filter
+  // threshold is the sum threshold and every cell above it is accumulated).
+  enum { K_FP64, K_MIXED } kind = !mixed ? K_FP64 : K_MIXED;
   const void* kfn = kind == K_FP64 ? reinterpret_cast<const void*>(join_fp64_kernel)
-                  : kind == K_MIXED_1NN ? reinterpret_cast<const void*>(join_mixed_1nn_kernel)
-                                        : reinterpret_cast<const void*>(join_mixed_kernel);
-  const int W = kind == K_FP64 ? fp64_band_width()
-              : kind == K_MIXED_1NN ? mixed_1nn_band_width() : mixed_band_width();
-  const int slab = kind == K_FP64 ? fp64_slab_rows()
-                 : kind == K_MIXED_1NN ? mixed_1nn_slab_rows() : mixed_slab_rows();
-  const int nthreads = kind == K_FP64 ? fp64_threads()
-                     : kind == K_MIXED_1NN ? mixed_1nn_threads() : mixed_threads();
-  const size_t smem = kind == K_FP64 ? 0
-                    : kind == K_MIXED_1NN ? mixed_1nn_smem_bytes() : mixed_smem_bytes();
+                  : is_1nn ? reinterpret_cast<const void*>(join_mixed_1nn_kernel)
+                           : reinterpret_cast<const void*>(join_mixed_sum_kernel);
+  const int W = kind == K_FP64 ? fp64_band_width() : mixed_1nn_band_width();
+  const int slab = kind == K_FP64 ? fp64_slab_rows() : mixed_1nn_slab_rows();
+  const int nthreads = kind == K_FP64 ? fp64_threads() : mixed_1nn_threads();
+  const size_t smem = kind == K_FP64 ? 0 : mixed_1nn_smem_bytes();
   if (smem > 0)
     CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(smem)));
@@ -601,9 +593,9 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     P.unit_counter = static_cast<unsigned long long*>(p);
     P.counters = static_cast<unsigned long long*>(p) + 1;
     P.error_flag = reinterpret_cast<int*>(static_cast<char*>(p) + 48);
-    if (kind == K_MIXED_1NN) {
+    if (kind == K_MIXED) {
       // random-walk-like series ask for ~7 (K = 512) to ~18 (K = 1024)
-      // requests per window
+      // 1NN requests per window
       int64_t want = std::max<int64_t>(kMinVerifyReqs, 32 * (nsz[0] + nsz[1]));
       want = std::max<int64_t>(want, ws.vreq_seen + ws.vreq_seen / 4);
       want = std::max<int64_t>(std::min<int64_t>(want, kMaxVerifyReqs), ws.vreq_cap);
@@ -619,17 +611,18 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
       CUDA_TRY(cudaEventRecord(ws.evk0, st));
       ws.timed_kernel = true;
     }
-    if (kind == K_MIXED_1NN) {
-      join_mixed_1nn_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
+    if (kind == K_MIXED) {
+      if (is_1nn)
+        join_mixed_1nn_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
+      else
+        join_mixed_sum_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
       ++launches;
       if (!nested) {
         CUDA_TRY(cudaEventRecord(ws.evkv, st));
         ws.timed_verify = true;
       }
       verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
-    } else if (kind == K_MIXED_SUM)
-      join_mixed_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
-    else
+    } else
       join_fp64_kernel<<<static_cast<unsigned>(grid), nthreads, 0, st>>>(P);
     ++launches;
     CUDA_TRY(cudaGetLastError());

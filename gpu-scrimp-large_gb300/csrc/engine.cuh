@@ -221,8 +221,8 @@ __global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
                              float* __restrict__ dg32);
 
 __global__ void join_fp64_kernel(JoinParams P);
-__global__ void join_mixed_kernel(JoinParams P);      // SUM_THRESH
-__global__ void join_mixed_1nn_kernel(JoinParams P);  // 1NN_INDEX
+__global__ void join_mixed_1nn_kernel(JoinParams P);  // mixed 1NN_INDEX
+__global__ void join_mixed_sum_kernel(JoinParams P);  // mixed SUM_THRESH
 __global__ void verify_requests_kernel(JoinParams P);
 
 // Seeds of the mixed 1NN join from a block-averaged pre-pass.

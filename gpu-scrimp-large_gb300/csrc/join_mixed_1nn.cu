@@ -1,5 +1,6 @@
-// join_mixed_1nn.cu -- mixed-precision 1NN_INDEX join: FP32 filter, verified
-// candidates.
+// join_mixed_1nn.cu -- the mixed-precision band kernel: FP32 filter over an
+// FP32 recurrence, exact path for the blocks it flags.  Serves 1NN_INDEX
+// (verified candidates) and SUM_THRESH.
 //
 // Work decomposition as in join_fp64.cu (persistent kernel over a device
 // queue of units = band of kBand diagonals x two row segments of seg_len
@@ -15,16 +16,28 @@
 // maximum of the whole 8x8x2 block per thread (3-input max.f32, two cells per
 // instruction).
 //
-// A block whose maximum could beat the smallest best-so-far among its rows
-// and columns, less an error margin, is queued for the exact path.  The
-// margin bounds the FP32 drift since the diagonal's anchor: per diagonal the
-// kernel accumulates cov^2 and per thread the squared bound of the
+// 1NN_INDEX: a block whose maximum could beat the smallest best-so-far among
+// its rows and columns, less an error margin, is queued for the exact path.
+// The margin bounds the FP32 drift since the diagonal's anchor: per diagonal
+// the kernel accumulates cov^2 and per thread the squared bound of the
 // increments |df_c dg_r| + |df_r dg_c|, and uses
 //   margin = C * 2^-24 * sqrt(rows * (sum cov^2 + sum inc^2)) * inv_c * inv_r.
-// Each warp drains its queue cooperatively (one queued block per lane):
+// Each warp drains its queue cooperatively (16 lanes per queued block):
 // cells that may improve their row or column are published with their FP32
-// value when the margin is below kTrust, otherwise verified first by a
-// direct dot product of the two windows computed by the whole warp.
+// value when the margin is below kTrust; otherwise the lower bound r - margin
+// is published and the cell goes to a request buffer that
+// verify_requests_kernel settles after the join with a direct dot product of
+// the two centred windows.
+//
+// SUM_THRESH (the reference's sum of every r above the threshold,
+// src/kernels_compute.h:87-113 and 380-392), join_mixed_sum_kernel: the same
+// filter and exact path with the sum threshold as the value to beat.  A cell
+// above the threshold by more than its margin, or above it with a margin
+// within kTrust, adds its FP32 r to its row's and its column's slab sums in
+// shared memory (flushed to the FP64 profile by atomicAdd when the row's slab
+// ends or the column leaves the column ring).  A cell within a wider margin
+// of the threshold goes to the request buffer, and verify_requests_kernel
+// adds its directly computed r if that is above the threshold.
 //
 // Anchors and verifications read an FP32 copy of each series stored relative
 // to local block offsets (stats.cu), with every factor centred by its
@@ -46,7 +59,6 @@ constexpr int kSlab = 128;                // rows staged per slab
 constexpr int kSteps = kSlab / kRows;
 constexpr int kCols = kSlab + kBand;      // staged columns per slab
 constexpr int kBlocks = kCols / 8;        // 8-column blocks
-constexpr int kPad = kCols + kBlocks;     // padded slot c + c/8
 // The staged columns form a ring over the unit's rows: slab q holds unit
 // columns 128 q .. 128 q + kCols - 1 at ring columns (128 q + c) mod kCols, so
 // a slab stages only the kSlab columns entering it.  Ring columns
@@ -135,6 +147,10 @@ struct SlowCtx {
   int64_t rbase[2];
   int64_t D0;  // first diagonal of the unit; thread t owns D0 + t*kDiags ..
   int ring0;   // ring column of the slab's first staged column
+  // SUM_THRESH: cells with r > thr add r to their row's and column's sums
+  // (r_best / c_best hold the slab's float sums instead of bests)
+  bool sum_mode;
+  float thr;
   int64_t m;
   KeyLayout kl;
   int prob;                        // index of the problem in JoinParams
@@ -391,8 +407,11 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
       const float mk = vk * ivc * ivr;
       const float rb = g ? sm.r_best[r0 + rr].y : sm.r_best[r0 + rr].x;
       const float cbv = g ? sm.c_best[rcs].y : sm.c_best[rcs].x;
-      const bool cand = live && rv + mk > fminf(rb, cbv);
-      const bool req = cand && mk > kTrust;
+      // the value to beat: the row's and column's bests, or the threshold
+      const float tgt = cx.sum_mode ? cx.thr : fminf(rb, cbv);
+      const bool cand = live && rv + mk > tgt;
+      // SUM_THRESH: a cell surely above the threshold counts with its FP32 r
+      const bool req = cand && mk > kTrust && !(cx.sum_mode && rv - mk > tgt);
       const unsigned rmask = __ballot_sync(0xffffffffu, req);
       unsigned long long slot = 0;
       if (rmask) {
@@ -400,25 +419,39 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
         if (lane == leader) slot = atomicAdd(cx.vcount, static_cast<unsigned long long>(__popc(rmask)));
         slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(rmask & ((1u << lane) - 1u));
       }
+      float add = 0.f;  // SUM_THRESH: what the cell adds to its row and column
       if (cand) {
         const int64_t i = cx.rbase[g] + r0 + rr;
         const int64_t j = i + cx.D0 + it.owner * kDiags + k;
         if (req) {
           ++nreq;
           if (slot < static_cast<unsigned long long>(cx.vcap)) {
-            publish(sm, cx, rv - mk, i, j, r0 + rr, rcs, g);
+            if (!cx.sum_mode) publish(sm, cx, rv - mk, i, j, r0 + rr, rcs, g);
             VerifyReq q;
             q.i = static_cast<uint64_t>(i) | (static_cast<uint64_t>(cx.prob) << 40);
             q.d = static_cast<uint32_t>(j - i);
             q.ub = rv + mk;
             cx.vreq[slot] = q;
           } else {
-            publish(sm, cx, verify_cov_lane(pr.R, pr.C, i, j, cx.m) * ivc * ivr, i, j,
-                    r0 + rr, rcs, g);
+            const float ev = verify_cov_lane(pr.R, pr.C, i, j, cx.m) * ivc * ivr;
+            if (cx.sum_mode) add = ev > cx.thr ? ev : 0.f;
+            else publish(sm, cx, ev, i, j, r0 + rr, rcs, g);
           }
+        } else if (cx.sum_mode) {
+          add = rv > cx.thr ? rv : 0.f;
         } else {
           publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
         }
+      }
+      if (cx.sum_mode) {
+        // the 8 diagonals of a block meet in one row: reduce over lanes
+        // (k = lane bits 1-3) before the shared-memory atomic
+        if (add != 0.f) atomicAdd(g ? &sm.c_best[rcs].y : &sm.c_best[rcs].x, add);
+        float rs = add;
+        rs += __shfl_xor_sync(0xffffffffu, rs, 2);
+        rs += __shfl_xor_sync(0xffffffffu, rs, 4);
+        rs += __shfl_xor_sync(0xffffffffu, rs, 8);
+        if (k == 0 && rs != 0.f) atomicAdd(g ? &sm.r_best[r0 + rr].y : &sm.r_best[r0 + rr].x, rs);
       }
       const float dfr = g ? rf.y : rf.x, dgr = g ? rf.w : rf.z;
       const float dfc = g ? cf.y : cf.x, dgc = g ? cf.w : cf.z;
@@ -430,16 +463,16 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
   return nreq;
 }
 
-}  // namespace
-
-size_t mixed_1nn_smem_bytes() { return sizeof(Smem); }
-
-__global__ void __launch_bounds__(kThreads, 4)
-join_mixed_1nn_kernel(JoinParams P) {
+// The band kernel's body; kSum selects SUM_THRESH (two instantiations, so
+// the 1NN_INDEX form carries none of the sum bookkeeping).
+template <bool kSum>
+__device__ __forceinline__ void band_body(const JoinParams& P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   const int t = threadIdx.x;
   const int lane = t & 31, warp = t >> 5;
+  constexpr bool sum_mode = kSum;
+  const float thr = static_cast<float>(P.threshold);
   unsigned long long n_steps = 0, n_slow = 0, n_verify = 0;
   int qn = 0;  // queued blocks of this warp (warp-uniform)
 
@@ -633,6 +666,8 @@ join_mixed_1nn_kernel(JoinParams P) {
       cx.vreq = P.vreq;
       cx.vcount = P.counters + 3;
       cx.vcap = P.vreq_cap;
+      cx.sum_mode = kSum;
+      cx.thr = static_cast<float>(P.threshold);
     }
 
     // ---------------- slabs ----------------
@@ -669,8 +704,20 @@ join_mixed_1nn_kernel(JoinParams P) {
         // A window that cannot match (padding, NaN or flat) must not lower
         // the filter threshold: its best is "unreachable".
         float2 cbv;
-        cbv.x = (pr.key_col && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_col[j0], P.kl) : kNoTarget;
-        cbv.y = (pr.key_col && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_col[j1], P.kl) : kNoTarget;
+        if (sum_mode) {
+          // the ring column's previous occupant (kCols columns earlier)
+          // leaves: its sums go to the profile, the new one starts at 0
+          if (q > 0 && pr.sum_col) {
+            const float2 old = sm.c_best[rc];
+            const int64_t o0 = j0 - kCols, o1 = j1 - kCols;
+            if (old.x != 0.f && o0 >= 0 && o0 < pr.C.ns) atomicAdd(pr.sum_col + o0, static_cast<double>(old.x));
+            if (old.y != 0.f && o1 >= 0 && o1 < pr.C.ns) atomicAdd(pr.sum_col + o1, static_cast<double>(old.y));
+          }
+          cbv = make_float2(0.f, 0.f);
+        } else {
+          cbv.x = (pr.key_col && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_col[j0], P.kl) : kNoTarget;
+          cbv.y = (pr.key_col && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_col[j1], P.kl) : kNoTarget;
+        }
         sm.u.s.c_df[padc(rc)] = make_float2(f.x, f.y);
         sm.u.s.c_dg[padc(rc)] = make_float2(f.z, f.w);
         sm.u.s.c_iv[padc(rc)] = iv;
@@ -705,8 +752,12 @@ join_mixed_1nn_kernel(JoinParams P) {
         f.w = ok1 ? pr.R.dg32[i1] : 0.f;
         const float2 iv = make_float2(ok0 ? pr.R.inv32[i0] : qnan(), ok1 ? pr.R.inv32[i1] : qnan());
         float2 rbv;
-        rbv.x = (pr.key_row && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_row[i0], P.kl) : kNoTarget;
-        rbv.y = (pr.key_row && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_row[i1], P.kl) : kNoTarget;
+        if (sum_mode) {
+          rbv = make_float2(0.f, 0.f);
+        } else {
+          rbv.x = (pr.key_row && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_row[i0], P.kl) : kNoTarget;
+          rbv.y = (pr.key_row && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_row[i1], P.kl) : kNoTarget;
+        }
         sm.r_fg[r] = f;
         sm.r_iv[r] = iv;
         sm.r_best[r] = rbv;
@@ -760,8 +811,10 @@ join_mixed_1nn_kernel(JoinParams P) {
           W = fma2(inc, inc, W);
         }
         const float vx = Vt.x + W.x, vy = Vt.y + W.y;
-        const float tx = fminf(bm.x, rsm.x) - kBoundC * kEps * sqrtf(kRows * vx) * icm.x * irm.x;
-        const float ty = fminf(bm.y, rsm.y) - kBoundC * kEps * sqrtf(kRows * vy) * icm.y * irm.y;
+        const float tx = (sum_mode ? thr : fminf(bm.x, rsm.x))
+                         - kBoundC * kEps * sqrtf(kRows * vx) * icm.x * irm.x;
+        const float ty = (sum_mode ? thr : fminf(bm.y, rsm.y))
+                         - kBoundC * kEps * sqrtf(kRows * vy) * icm.y * irm.y;
 
         // fast path: recurrence + block maximum
         float bx = -3.f, by = -3.f;
@@ -862,6 +915,25 @@ join_mixed_1nn_kernel(JoinParams P) {
       }
       n_steps += kSteps;
       __syncthreads();
+      if (sum_mode && pr.sum_row) {
+        // the slab's row sums (thread t: row t; it restages row t next)
+        const float2 v = sm.r_best[t];
+        const int64_t i0 = rbase[0] + t, i1 = rbase[1] + t;
+        if (v.x != 0.f && i0 < rend[0]) atomicAdd(pr.sum_row + i0, static_cast<double>(v.x));
+        if (v.y != 0.f && i1 < rend[1]) atomicAdd(pr.sum_row + i1, static_cast<double>(v.y));
+      }
+      if (sum_mode && pr.sum_col && q + 1 == nslabs) {
+        // unit end: every column left in the ring
+        for (int c = t; c < kCols; c += kThreads) {
+          const float2 v = sm.c_best[ringc(ring0, c)];
+          const int64_t j0 = cbase_g[0] + c, j1 = cbase_g[1] + c;
+          if (v.x != 0.f && j0 < pr.C.ns) atomicAdd(pr.sum_col + j0, static_cast<double>(v.x));
+          if (v.y != 0.f && j1 < pr.C.ns) atomicAdd(pr.sum_col + j1, static_cast<double>(v.y));
+        }
+      }
+      // The flushes read the unit's Problem in shared memory, which thread 0
+      // overwrites when it fetches the next unit.
+      if (sum_mode && q + 1 == nslabs) __syncthreads();
     }
   }
   // per-CTA totals of the work counters
@@ -878,7 +950,19 @@ join_mixed_1nn_kernel(JoinParams P) {
   }
 }
 
-// Settles the verification requests of join_mixed_1nn_kernel, one warp per
+}  // namespace
+
+size_t mixed_1nn_smem_bytes() { return sizeof(Smem); }
+
+__global__ void __launch_bounds__(kThreads, 4) join_mixed_1nn_kernel(JoinParams P) {
+  band_body<false>(P);
+}
+
+__global__ void __launch_bounds__(kThreads, 4) join_mixed_sum_kernel(JoinParams P) {
+  band_body<true>(P);
+}
+
+// Settles the verification requests of the band kernels, one warp per
 // cell.  A request whose upper bound rv + margin no longer exceeds the
 // current best of its row or column cannot change the profile and is
 // skipped; otherwise the cell's covariance is computed directly from the
@@ -898,6 +982,15 @@ verify_requests_kernel(JoinParams P) {
     const Problem& pr = problem_of(P, static_cast<int>(rq.i >> 40));
     const int64_t i = static_cast<int64_t>(rq.i & ((uint64_t{1} << 40) - 1));
     const int64_t j = i + rq.d;
+    if (P.profile_type == 2) {  // SUM_THRESH: the cell counts if above it
+      const float cv = verify_cov_warp(pr.R, pr.C, i, j, pr.m, lane);
+      const float rv = (cv * pr.C.inv32[j]) * pr.R.inv32[i];
+      if (lane == 0 && rv > static_cast<float>(P.threshold)) {
+        if (pr.sum_row) atomicAdd(pr.sum_row + i, static_cast<double>(rv));
+        if (pr.sum_col) atomicAdd(pr.sum_col + j, static_cast<double>(rv));
+      }
+      continue;
+    }
     const bool row_open = pr.key_row && rq.ub > key_corr_floor(pr.key_row[i], P.kl);
     const bool col_open = pr.key_col && rq.ub > key_corr_floor(pr.key_col[j], P.kl);
     if (!row_open && !col_open) continue;

@@ -69,10 +69,17 @@ def check_1nn(name, got_corr, got_idx, want_corr, want_idx, tol, T_self, T_other
     return maxerr, int(mism.size)
 
 
-def check_sum(name, got, want, thr, rtol):
+def check_sum(name, got, want, thr, rtol, cell_tol=0.0):
     """SUM_THRESH: relative agreement, allowing whole multiples of the
     threshold where a correlation sits on the threshold edge (the reference's
-    compare_vectors_sum, test/test_common.py:27-51)."""
+    compare_vectors_sum, test/test_common.py:27-51).
+
+    That rule accepts a difference slightly above k * thr: a cell just above
+    the threshold that one side missed.  A form whose correlations carry
+    errors up to cell_tol (the mixed form: TOL_MIXED) may also count a cell
+    up to cell_tol below the threshold, a difference up to k * cell_tol below
+    k * thr; with cell_tol > 0 a difference within rtol * |sum| + k * cell_tol
+    of the nearest multiple k * thr passes."""
     got = np.asarray(got, dtype=np.float64)
     want = np.asarray(want, dtype=np.float64)
     diff = np.abs(got - want)
@@ -82,6 +89,9 @@ def check_sum(name, got, want, thr, rtol):
         q = np.round(diff[bad] / thr, 6)
         frac = q - np.floor(q)
         still = frac > 1e-3
+        if cell_tol > 0:
+            k = np.round(diff[bad] / thr)
+            still &= np.abs(diff[bad] - k * thr) > rtol * scale[bad] + k * cell_tol
         n_bad = int(np.sum(still))
     else:
         n_bad = int(np.sum(bad))

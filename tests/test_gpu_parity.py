@@ -113,13 +113,29 @@ def test_sum_thresh(gpu_engine, oracle_mod, precision, thr):
     a = rw(rng, 3000)
     b = rw(rng, 2000)
     rtol = 1e-9 if precision == "double" else 2e-5
+    ctol = 0.0 if precision == "double" else TOL_MIXED
     got = gpu_engine.join(a, None, 64, "SUM_THRESH", precision, threshold=thr)
     want = oracle_mod.join(a, None, 64, "SUM_THRESH", threshold=thr)
-    check_sum("selfsum", got["sum_a"], want["sum_a"], thr, rtol)
+    check_sum("selfsum", got["sum_a"], want["sum_a"], thr, rtol, ctol)
     got = gpu_engine.join(a, b, 64, "SUM_THRESH", precision, threshold=thr, keep_rows=True)
     want = oracle_mod.join(a, b, 64, "SUM_THRESH", threshold=thr, keep_rows=True)
-    check_sum("absum/A", got["sum_a"], want["sum_a"], thr, rtol)
-    check_sum("absum/B", got["sum_b"], want["sum_b"], thr, rtol)
+    check_sum("absum/A", got["sum_a"], want["sum_a"], thr, rtol, ctol)
+    check_sum("absum/B", got["sum_b"], want["sum_b"], thr, rtol, ctol)
+
+
+def test_sum_thresh_many_units(gpu_engine):
+    """Mixed SUM_THRESH over thousands of band units of both AB problems
+    (their column series differ in length), against the FP64 form, which the
+    other tests tie to the oracle."""
+    rng = np.random.default_rng(33)
+    a = rw(rng, 200_000)
+    b = rw(rng, 60_000)
+    for thr in (0.5, 0.9):
+        want = gpu_engine.join(a, b, 64, "SUM_THRESH", "double", threshold=thr, keep_rows=True)
+        for _ in range(2):
+            got = gpu_engine.join(a, b, 64, "SUM_THRESH", "mixed", threshold=thr, keep_rows=True)
+            check_sum("A", got["sum_a"], want["sum_a"], thr, 2e-5, TOL_MIXED)
+            check_sum("B", got["sum_b"], want["sum_b"], thr, 2e-5, TOL_MIXED)
 
 
 @pytest.mark.parametrize("precision,tol", PRECISIONS)
@@ -229,7 +245,8 @@ def test_against_reference_golden_fixtures(gpu_engine, precision, tol):
                     assert np.all(np.abs(r - wc[mism]) <= tol + 2.5e-7), f
             if "sum_" + side in z.files:
                 rt = 1e-9 if precision == "double" else 2e-5
-                check_sum(f, got["sum_" + side], z["sum_" + side], thr, rt)
+                check_sum(f, got["sum_" + side], z["sum_" + side], thr, rt,
+                          0.0 if precision == "double" else TOL_MIXED)
 
 
 # Joins of >= 4e9 cells at m >= 64 run the block-averaged seeding pre-pass
