@@ -74,6 +74,9 @@ constexpr int kSpanBlk = kYSpan / 32 + 3;
 constexpr int kQueue = 16;                // queued blocks per warp
 constexpr float kEps = 5.9604645e-8f;     // 2^-24
 constexpr float kBoundC = 4.0f;
+// kBoundC * kEps * sqrt(kRows), widened by 2^-16 (see the step's threshold)
+static_assert(kRows == 8, "kStepMarginC holds sqrt(8)");
+constexpr float kStepMarginC = kBoundC * kEps * 2.8284271f * 1.0000153f;
 // A candidate whose drift margin exceeds kTrust is verified by a direct dot
 // product.  The margin is a statistical bound; 5e-6 leaves room for it to be
 // exceeded (measured: max |r| error 6.6e-6 at 2048 rows per anchor, where
@@ -104,6 +107,12 @@ __device__ __forceinline__ float max3(float a, float b, float c) {
   float d;
   asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
   return d;
+}
+// PTX sqrt.approx.f32: an approximate square root (a few ulp); sqrt(0) = 0.
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
 __device__ __forceinline__ float qnan() { return __int_as_float(0x7FC00000); }
 
@@ -811,10 +820,15 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
           W = fma2(inc, inc, W);
         }
         const float vx = Vt.x + W.x, vy = Vt.y + W.y;
-        const float tx = (sum_mode ? thr : fminf(bm.x, rsm.x))
-                         - kBoundC * kEps * sqrtf(kRows * vx) * icm.x * irm.x;
-        const float ty = (sum_mode ? thr : fminf(bm.y, rsm.y))
-                         - kBoundC * kEps * sqrtf(kRows * vy) * icm.y * irm.y;
+        // threshold - margin, the margin as the exact path forms it per cell
+        // (C eps sqrt(rows v) inv_c inv_r) but with the block's largest
+        // inverse norms, an approximate square root and a 2^-16 allowance
+        // for both
+        const float2 mg = mul2(mul2(make_float2(sqrt_approx(vx), sqrt_approx(vy)), icm), irm);
+        const float2 tb = sum_mode ? make_float2(thr, thr)
+                                   : make_float2(fminf(bm.x, rsm.x), fminf(bm.y, rsm.y));
+        const float2 tt = fma2(make_float2(-kStepMarginC, -kStepMarginC), mg, tb);
+        const float tx = tt.x, ty = tt.y;
 
         // fast path: recurrence + block maximum
         float bx = -3.f, by = -3.f;
