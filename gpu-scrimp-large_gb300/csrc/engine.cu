@@ -96,8 +96,9 @@ int validate(const scamp_c_args* a, std::string* msg) {
     *msg = "Error: Input time series must be at least 'subesequence window size' in length";
     return SCAMP_ERR_INVALID_ARGS;
   }
-  if (a->profile_type != SCAMP_PROFILE_1NN_INDEX && a->profile_type != SCAMP_PROFILE_SUM_THRESH) {
-    *msg = "Error: profile type not supported by this engine (1NN_INDEX, SUM_THRESH)";
+  if (a->profile_type != SCAMP_PROFILE_1NN_INDEX && a->profile_type != SCAMP_PROFILE_SUM_THRESH &&
+      a->profile_type != SCAMP_PROFILE_1NN) {
+    *msg = "Error: profile type not supported by this engine (1NN_INDEX, SUM_THRESH, 1NN)";
     return SCAMP_ERR_UNIMPLEMENTED;
   }
   if (a->precision_type < SCAMP_PRECISION_SINGLE || a->precision_type > SCAMP_PRECISION_ULTRA) {
@@ -245,7 +246,7 @@ enum Slot {
   S_KEY_A, S_KEY_B, S_SUM_A, S_SUM_B, S_PROF_A, S_PROF_B, S_CORR_A, S_CORR_B,
   S_PREFIX, S_COUNTER, S_T32_A, S_T32_B, S_BHI_A, S_BLO_A, S_MUREL_A,
   S_BHI_B, S_BLO_B, S_MUREL_B, S_VREQ, S_PAA_A, S_PAA_B, S_SEED_A, S_SEED_B,
-  S_BATCH,
+  S_BATCH, S_MAX_A, S_MAX_B,
 };
 
 #define CUDA_TRY(expr)                                                     \
@@ -333,7 +334,8 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
                const double* dA, const double* dB, uint64_t* dprof_a,
                uint64_t* dprof_b, double* dsum_a, double* dsum_b,
                double* dcorr_a, double* dcorr_b, cudaStream_t st,
-               std::string* msg, bool nested = false);
+               std::string* msg, bool nested = false, float* dmax_a = nullptr,
+               float* dmax_b = nullptr);
 
 // Block-averaged join of the inputs (window m / 8) into the seed profiles
 // S_SEED_A/B; returns their device pointers (seed_b null when not kept).
@@ -394,9 +396,11 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
                const double* dA, const double* dB, uint64_t* dprof_a,
                uint64_t* dprof_b, double* dsum_a, double* dsum_b,
                double* dcorr_a, double* dcorr_b, cudaStream_t st,
-               std::string* msg, bool nested) {
+               std::string* msg, bool nested, float* dmax_a, float* dmax_b) {
   Plan plan = make_plan(a);
-  const bool is_1nn = a->profile_type == SCAMP_PROFILE_1NN_INDEX;
+  // 1NN (float best correlation, no index) runs as 1NN_INDEX on the keys
+  const bool max_only = a->profile_type == SCAMP_PROFILE_1NN;
+  const bool is_1nn = a->profile_type == SCAMP_PROFILE_1NN_INDEX || max_only;
   const bool mixed = a->precision_type == SCAMP_PRECISION_MIXED ||
                      a->precision_type == SCAMP_PRECISION_SINGLE;
   const bool ultra = a->precision_type == SCAMP_PRECISION_ULTRA;
@@ -443,9 +447,36 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   } else {
     sb = sa;
   }
+  // ULTRA: the reference's combined update terms (combined_stats_kernel):
+  // A's "A" terms, B's "B" terms; a self-join's rows take the "B" terms of A,
+  // held in series B's (otherwise unused) df/dg buffers.
+  double *ultra_row_df = nullptr, *ultra_row_dg = nullptr;
+  if (ultra) {
+    combined_stats_kernel<<<static_cast<unsigned>((plan.ns_a + 255) / 256), 256, 0, st>>>(
+        sa.T, na, m, sa.mean, 0, sa.df, sa.dg);
+    ++launches;
+    if (a->has_b) {
+      combined_stats_kernel<<<static_cast<unsigned>((plan.ns_b + 255) / 256), 256, 0, st>>>(
+          sb.T, nb, m, sb.mean, 1, sb.df, sb.dg);
+    } else {
+      void* p;
+      if ((rc = ensure(ws, S_DF_B, plan.ns_a * 8, &p, msg))) return rc;
+      ultra_row_df = static_cast<double*>(p);
+      if ((rc = ensure(ws, S_DG_B, plan.ns_a * 8, &p, msg))) return rc;
+      ultra_row_dg = static_cast<double*>(p);
+      combined_stats_kernel<<<static_cast<unsigned>((plan.ns_a + 255) / 256), 256, 0, st>>>(
+          sa.T, na, m, sa.mean, 1, ultra_row_df, ultra_row_dg);
+    }
+    ++launches;
+  }
   CUDA_TRY(cudaGetLastError());
   SeriesDev devA = to_dev(sa, na, plan.ns_a);
   SeriesDev devB = to_dev(sb, nb, plan.ns_b);
+  SeriesDev devArows = devA;  // series A in the row role
+  if (ultra_row_df) {
+    devArows.df = ultra_row_df;
+    devArows.dg = ultra_row_dg;
+  }
 
   // ---- profiles: packed entries -> merge keys ----
   const KeyLayout kl = make_key_layout(std::max(plan.ns_a, plan.ns_b));
@@ -458,15 +489,25 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     if (q.col_target >= 0) used[q.col_target] = true;
     if (q.row_target >= 0) used[q.row_target] = true;
   }
+  float* maxs[2] = {dmax_a, dmax_b};
   if (is_1nn) {
     for (int s = 0; s < 2; ++s) {
-      if (!used[s] && !(s == 0 && profs[0])) continue;
-      if (!profs[s]) { *msg = "Error: profile buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
+      if (max_only) {
+        if (!used[s] && !(s == 0 && maxs[0])) continue;
+        if (!maxs[s]) { *msg = "Error: profile buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
+      } else {
+        if (!used[s] && !(s == 0 && profs[0])) continue;
+        if (!profs[s]) { *msg = "Error: profile buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
+      }
       void* p;
       if ((rc = ensure(ws, s == 0 ? S_KEY_A : S_KEY_B, nsz[s] * 8, &p, msg))) return rc;
       keys[s] = static_cast<uint64_t*>(p);
-      profile_to_keys_kernel<<<static_cast<unsigned>((nsz[s] + 255) / 256), 256, 0, st>>>(
-          profs[s], keys[s], nsz[s], kl);
+      if (max_only)
+        floats_to_keys_kernel<<<static_cast<unsigned>((nsz[s] + 255) / 256), 256, 0, st>>>(
+            maxs[s], keys[s], nsz[s], kl);
+      else
+        profile_to_keys_kernel<<<static_cast<unsigned>((nsz[s] + 255) / 256), 256, 0, st>>>(
+            profs[s], keys[s], nsz[s], kl);
       ++launches;
     }
   } else {
@@ -539,7 +580,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   P.nprob = 0;
   for (const auto& q : plan.probs) {
     Problem& pr = P.prob[P.nprob++];
-    pr.R = q.rows_series == 0 ? devA : devB;
+    pr.R = q.rows_series == 0 ? devArows : devB;
     pr.C = q.cols_series == 0 ? devA : devB;
     pr.d_lo = q.d_lo; pr.d_hi = q.d_hi; pr.x_lo = q.x_lo; pr.x_hi = q.x_hi;
     pr.key_col = is_1nn && q.col_target >= 0 ? keys[q.col_target] : nullptr;
@@ -563,7 +604,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   P.m = m;
   P.seg_len = K;
   P.band_width = W;
-  P.profile_type = a->profile_type;
+  P.profile_type = is_1nn ? SCAMP_PROFILE_1NN_INDEX : a->profile_type;
   P.threshold = a->distance_threshold;
   P.kl = kl;
   {
@@ -634,8 +675,12 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     double* corr[2] = {dcorr_a, dcorr_b};
     for (int s = 0; s < 2; ++s) {
       if (!keys[s]) continue;
-      keys_to_profile_kernel<<<static_cast<unsigned>((nsz[s] + 255) / 256), 256, 0, st>>>(
-          keys[s], profs[s], corr[s], nsz[s], kl);
+      if (max_only)
+        keys_to_floats_kernel<<<static_cast<unsigned>((nsz[s] + 255) / 256), 256, 0, st>>>(
+            keys[s], maxs[s], corr[s], nsz[s], kl);
+      else
+        keys_to_profile_kernel<<<static_cast<unsigned>((nsz[s] + 255) / 256), 256, 0, st>>>(
+            keys[s], profs[s], corr[s], nsz[s], kl);
       ++launches;
     }
   }
@@ -746,7 +791,8 @@ extern "C" int scamp_gb300_join_dev(const scamp_c_args* args, scamp_c_result* re
   std::lock_guard<std::mutex> lock(ws->mu);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   rc = run_device(*ws, args, res, args->timeseries_a, args->has_b ? args->timeseries_b : args->timeseries_a,
-                  res->profile_a, res->profile_b, res->sum_a, res->sum_b, res->corr_a, res->corr_b, st, &msg);
+                  res->profile_a, res->profile_b, res->sum_a, res->sum_b, res->corr_a, res->corr_b, st, &msg,
+                  false, res->max_a, res->max_b);
   if (rc == SCAMP_OK) {
     cudaError_t e = cudaEventSynchronize(ws->ev1);
     if (e != cudaSuccess) { msg = std::string("CUDA error: ") + cudaGetErrorString(e); rc = SCAMP_ERR_CUDA; }
@@ -769,6 +815,7 @@ extern "C" int scamp_gb300_join(const scamp_c_args* args, scamp_c_result* res,
   std::lock_guard<std::mutex> lock(ws->mu);
   cudaStream_t st = ws->stream;
   const bool is_1nn = args->profile_type == SCAMP_PROFILE_1NN_INDEX;
+  const bool max_only = args->profile_type == SCAMP_PROFILE_1NN;
   const int64_t na = static_cast<int64_t>(args->len_a);
   const int64_t nb = args->has_b ? static_cast<int64_t>(args->len_b) : 0;
   const int64_t nsa = na - static_cast<int64_t>(args->window) + 1;
@@ -792,6 +839,8 @@ extern "C" int scamp_gb300_join(const scamp_c_args* args, scamp_c_result* res,
   const bool want_b = args->keep_rows_separate != 0;
   uint64_t *dprof[2] = {nullptr, nullptr};
   double *dsum[2] = {nullptr, nullptr}, *dcorr[2] = {nullptr, nullptr};
+  float* dmax[2] = {nullptr, nullptr};
+  float* hmax[2] = {res->max_a, res->max_b};
   uint64_t* hprof[2] = {res->profile_a, res->profile_b};
   double* hsum[2] = {res->sum_a, res->sum_b};
   double* hcorr[2] = {res->corr_a, res->corr_b};
@@ -799,7 +848,16 @@ extern "C" int scamp_gb300_join(const scamp_c_args* args, scamp_c_result* res,
   for (int s = 0; s < 2; ++s) {
     if (s == 1 && !want_b) continue;
     void* p;
-    if (is_1nn) {
+    if (max_only) {
+      if (!hmax[s]) { msg = "Error: profile buffer missing"; return fail(SCAMP_ERR_INVALID_ARGS); }
+      if ((rc = ensure(*ws, s ? S_MAX_B : S_MAX_A, nsz[s] * 4, &p, &msg))) return fail(rc);
+      dmax[s] = static_cast<float*>(p);
+      HOST_CUDA(cudaMemcpyAsync(p, hmax[s], nsz[s] * 4, cudaMemcpyHostToDevice, st));
+      if (hcorr[s]) {
+        if ((rc = ensure(*ws, s ? S_CORR_B : S_CORR_A, nsz[s] * 8, &p, &msg))) return fail(rc);
+        dcorr[s] = static_cast<double*>(p);
+      }
+    } else if (is_1nn) {
       if (!hprof[s]) { msg = "Error: profile buffer missing"; return fail(SCAMP_ERR_INVALID_ARGS); }
       if ((rc = ensure(*ws, s ? S_PROF_B : S_PROF_A, nsz[s] * 8, &p, &msg))) return fail(rc);
       dprof[s] = static_cast<uint64_t*>(p);
@@ -817,11 +875,15 @@ extern "C" int scamp_gb300_join(const scamp_c_args* args, scamp_c_result* res,
   }
   rc = run_device(*ws, args, res, static_cast<double*>(pa),
                   args->has_b ? static_cast<double*>(pb) : static_cast<double*>(pa),
-                  dprof[0], dprof[1], dsum[0], dsum[1], dcorr[0], dcorr[1], st, &msg);
+                  dprof[0], dprof[1], dsum[0], dsum[1], dcorr[0], dcorr[1], st, &msg,
+                  false, dmax[0], dmax[1]);
   if (rc) return fail(rc);
   for (int s = 0; s < 2; ++s) {
     if (s == 1 && !want_b) continue;
-    if (is_1nn) {
+    if (max_only) {
+      HOST_CUDA(cudaMemcpyAsync(hmax[s], dmax[s], nsz[s] * 4, cudaMemcpyDeviceToHost, st));
+      if (hcorr[s]) HOST_CUDA(cudaMemcpyAsync(hcorr[s], dcorr[s], nsz[s] * 8, cudaMemcpyDeviceToHost, st));
+    } else if (is_1nn) {
       HOST_CUDA(cudaMemcpyAsync(hprof[s], dprof[s], nsz[s] * 8, cudaMemcpyDeviceToHost, st));
       if (hcorr[s]) HOST_CUDA(cudaMemcpyAsync(hcorr[s], dcorr[s], nsz[s] * 8, cudaMemcpyDeviceToHost, st));
     } else {
@@ -948,6 +1010,10 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
     *msg = "Error: the no-allocation join runs the FP64 form only (precision double or ultra)";
     return SCAMP_ERR_INVALID_ARGS;
   }
+  if (a->profile_type == SCAMP_PROFILE_1NN) {
+    *msg = "Error: the no-allocation join serves 1NN_INDEX and SUM_THRESH";
+    return SCAMP_ERR_INVALID_ARGS;
+  }
   const Plan plan = make_plan(a);
   const bool is_1nn = a->profile_type == SCAMP_PROFILE_1NN_INDEX;
   const bool ultra = a->precision_type == SCAMP_PRECISION_ULTRA;
@@ -964,6 +1030,7 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
   const int bshift = block_shift(m);
   SeriesBufs sa = carve_series(cv, kNoAllocMaxSamples, bshift);
   SeriesBufs sb = carve_series(cv, kNoAllocMaxSamples, bshift);
+  const SeriesBufs sb_carved = sb;
 
   uint32_t launches = 0;
   const int chunk = 64;
@@ -985,9 +1052,31 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
   } else {
     sb = sa;
   }
+  // ULTRA update terms as in run_device; a self-join's row terms go to the
+  // second carved series' df/dg, unused by a self-join
+  bool ultra_rows = false;
+  if (ultra) {
+    combined_stats_kernel<<<static_cast<unsigned>((plan.ns_a + 255) / 256), 256, 0, st>>>(
+        sa.T, na, m, sa.mean, 0, sa.df, sa.dg);
+    ++launches;
+    if (a->has_b) {
+      combined_stats_kernel<<<static_cast<unsigned>((plan.ns_b + 255) / 256), 256, 0, st>>>(
+          sb.T, nb, m, sb.mean, 1, sb.df, sb.dg);
+    } else {
+      combined_stats_kernel<<<static_cast<unsigned>((plan.ns_a + 255) / 256), 256, 0, st>>>(
+          sa.T, na, m, sa.mean, 1, sb_carved.df, sb_carved.dg);
+      ultra_rows = true;
+    }
+    ++launches;
+  }
   CUDA_TRY(cudaGetLastError());
   const SeriesDev devA = to_dev(sa, na, plan.ns_a);
   const SeriesDev devB = to_dev(sb, nb, plan.ns_b);
+  SeriesDev devArows_nd = devA;  // series A in the row role
+  if (ultra_rows) {
+    devArows_nd.df = sb_carved.df;
+    devArows_nd.dg = sb_carved.dg;
+  }
 
   const KeyLayout kl = make_key_layout(std::max(plan.ns_a, plan.ns_b));
   uint64_t* profs[2] = {res->profile_a, res->profile_b};
@@ -1038,7 +1127,7 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
   int64_t band_total = 0;
   for (const auto& q : plan.probs) {
     Problem& pr = P.prob[P.nprob++];
-    pr.R = q.rows_series == 0 ? devA : devB;
+    pr.R = q.rows_series == 0 ? devArows_nd : devB;
     pr.C = q.cols_series == 0 ? devA : devB;
     pr.d_lo = q.d_lo; pr.d_hi = q.d_hi; pr.x_lo = q.x_lo; pr.x_hi = q.x_hi;
     pr.key_col = is_1nn && q.col_target >= 0 ? keys[q.col_target] : nullptr;

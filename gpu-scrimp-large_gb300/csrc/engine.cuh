@@ -220,6 +220,11 @@ __global__ void stats_kernel(const double* __restrict__ T_raw, int64_t n,
                              float* __restrict__ inv32, float* __restrict__ df32,
                              float* __restrict__ dg32);
 
+// ULTRA update terms of one series: role_b 0 gives the "A" terms, 1 the "B"
+// terms (stats.cu); T is the cleaned series, mean its window means.
+__global__ void combined_stats_kernel(const double* __restrict__ T, int64_t n, int64_t m,
+                                      const double* __restrict__ mean, int role_b,
+                                      double* __restrict__ df, double* __restrict__ dg);
 __global__ void join_fp64_kernel(JoinParams P);
 __global__ void join_mixed_1nn_kernel(JoinParams P);  // mixed 1NN_INDEX
 __global__ void join_mixed_sum_kernel(JoinParams P);  // mixed SUM_THRESH
@@ -244,6 +249,10 @@ __global__ void paa_kernel(const double* __restrict__ T, int64_t n_out, int f,
 __global__ void fill_floor_kernel(uint64_t* __restrict__ p, int64_t n, float floor);
 __global__ void seed_kernel(SeedArgs S);
 
+__global__ void floats_to_keys_kernel(const float* __restrict__ in, uint64_t* __restrict__ keys,
+                                      int64_t n, KeyLayout kl);
+__global__ void keys_to_floats_kernel(const uint64_t* __restrict__ keys, float* __restrict__ out,
+                                      double* __restrict__ corr, int64_t n, KeyLayout kl);
 __global__ void profile_to_keys_kernel(const uint64_t* __restrict__ in,
                                        uint64_t* __restrict__ keys, int64_t n,
                                        KeyLayout kl);

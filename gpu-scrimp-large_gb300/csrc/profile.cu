@@ -43,4 +43,26 @@ __global__ void keys_to_profile_kernel(const uint64_t* __restrict__ keys,
   if (corr) corr[i] = r;
 }
 
+// The reference's 1NN profile (PROFILE_TYPE_1NN, float per window, -2.0 =
+// none; src/common.cpp:290-292, merged by elementwise max, :388-391) to keys
+// and back.  A best-so-far value carries index 0.
+__global__ void floats_to_keys_kernel(const float* __restrict__ in, uint64_t* __restrict__ keys,
+                                      int64_t n, KeyLayout kl) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const float c = in[i];
+  keys[i] = (c >= -1.0f) ? make_key(q_from_float_bits(__float_as_uint(c), kl.frac_bits), 0, kl)
+                         : 0;
+}
+
+__global__ void keys_to_floats_kernel(const uint64_t* __restrict__ keys, float* __restrict__ out,
+                                      double* __restrict__ corr, int64_t n, KeyLayout kl) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t k = keys[i];
+  const double r = k == 0 ? -2.0 : key_to_corr(k, kl);
+  out[i] = static_cast<float>(r);
+  if (corr) corr[i] = r;
+}
+
 }  // namespace scamp_gb300

@@ -209,4 +209,40 @@ __global__ void stats_batch_kernel(const StatsJob* __restrict__ jobs,
              j.mu_rel, j.mean, j.inv, j.df, j.dg, j.inv32, j.df32, j.dg32);
 }
 
+// ULTRA's update terms (the reference's compute_combined_stats_cpu,
+// src/cpu_stats.cpp:162-196, used by src/tile.cpp:404-409).  With the
+// covariance written against a constant c for one window,
+//   cov(i+1, j+1) = cov(i, j) + (x[i+m] - mu[i+1]) (y[j+m] - c)
+//                             - (x[i] - mu[i]) (y[j] - c),
+// exact for c = mean(y[j+1 .. j+m-1]), the (m-1)-sample mean.  One side of a
+// band takes the "A" terms of its series,
+//   df = -(x[i] - mu[i]),  dg = x[i+m] - mu[i+1],
+// the other the "B" terms,
+//   df = y[j+m] - mu'[j+1],  dg = y[j] - mu'[j+1],
+// so that df_c dg_r + df_r dg_c is the update above.  mu' is summed directly
+// per window (TwoSum-compensated).  The last window's terms are 0 (the
+// recurrence never leaves it).
+__global__ void combined_stats_kernel(const double* __restrict__ T, int64_t n, int64_t m,
+                                      const double* __restrict__ mean, int role_b,
+                                      double* __restrict__ df, double* __restrict__ dg) {
+  const int64_t ns = n - m + 1;
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= ns) return;
+  if (i == ns - 1) {
+    df[i] = 0.0;
+    dg[i] = 0.0;
+    return;
+  }
+  if (!role_b) {
+    df[i] = -(T[i] - mean[i]);
+    dg[i] = T[i + m] - mean[i + 1];
+    return;
+  }
+  double s = 0.0, c = 0.0;
+  for (int64_t t = i + 1; t < i + m; ++t) acc2(s, c, T[t]);
+  const double mu1 = (s + c) / static_cast<double>(m - 1);
+  df[i] = T[i + m] - mu1;
+  dg[i] = T[i] - mu1;
+}
+
 }  // namespace scamp_gb300

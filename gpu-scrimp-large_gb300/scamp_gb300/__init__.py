@@ -29,7 +29,8 @@ _PRECISION = {
     "double": _lib.PRECISION_DOUBLE,
     "ultra": _lib.PRECISION_ULTRA,
 }
-_PROFILE = {"1NN_INDEX": _lib.PROFILE_1NN_INDEX, "SUM_THRESH": _lib.PROFILE_SUM_THRESH}
+_PROFILE = {"1NN_INDEX": _lib.PROFILE_1NN_INDEX, "SUM_THRESH": _lib.PROFILE_SUM_THRESH,
+            "1NN": _lib.PROFILE_1NN}
 
 # 1NN_INDEX "no match" entry {corr = -2.0f, index = 0xFFFFFFFF}
 # (src/common.cpp:294-299).
@@ -118,7 +119,9 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
     For 1NN_INDEX returns ``profile_a`` (and ``profile_b`` with keep_rows) as
     uint64 arrays in the reference's packed layout; ``profile_a`` /
     ``profile_b`` given on input are merged into, like a best-so-far profile
-    passed to do_SCAMP.  For SUM_THRESH returns ``sum_a`` / ``sum_b``.
+    passed to do_SCAMP.  For 1NN (the reference's PROFILE_TYPE_1NN) they are
+    float32 arrays of the best correlation, -2 where there is none.  For
+    SUM_THRESH returns ``sum_a`` / ``sum_b``.
     ``corr_a`` / ``corr_b`` (double correlations) when return_corr.
     With ``inplace`` the given profile arrays (contiguous uint64 / float64)
     are updated directly instead of copied (e.g. pinned host buffers).
@@ -140,6 +143,7 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
     res = _lib.CResult()
     out = {}
     is_1nn = ca.profile_type == _lib.PROFILE_1NN_INDEX
+    max_only = ca.profile_type == _lib.PROFILE_1NN
 
     def _buf(given, n, dtype, fill):
         if given is None:
@@ -150,14 +154,19 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
             return given
         return np.array(given, dtype=dtype, copy=True)
 
-    if is_1nn:
-        pa = _buf(profile_a, nsa, np.uint64, NO_MATCH)
+    if is_1nn or max_only:
+        dt, fill = (np.float32, np.float32(-2.0)) if max_only else (np.uint64, NO_MATCH)
+        pa = _buf(profile_a, nsa, dt, fill)
         out["profile_a"] = pa
-        res.profile_a = pa.ctypes.data
+        pb = _buf(profile_b, nsb, dt, fill) if keep_rows else None
         if keep_rows:
-            pb = _buf(profile_b, nsb, np.uint64, NO_MATCH)
             out["profile_b"] = pb
-            res.profile_b = pb.ctypes.data
+        if max_only:
+            res.max_a = pa.ctypes.data
+            res.max_b = pb.ctypes.data if keep_rows else None
+        else:
+            res.profile_a = pa.ctypes.data
+            res.profile_b = pb.ctypes.data if keep_rows else None
         if return_corr:
             out["corr_a"] = np.empty(nsa)
             res.corr_a = out["corr_a"].ctypes.data
@@ -189,9 +198,11 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
                 keep_rows=False, aligned=False, threshold=0.0,
                 profile_a_ptr=None, profile_b_ptr=None, sum_a_ptr=None,
                 sum_b_ptr=None, corr_a_ptr=None, corr_b_ptr=None, stream=0,
-                anchor_interval=0, device=0, max_tile_size=128000):
+                anchor_interval=0, device=0, max_tile_size=128000, max_a_ptr=None,
+                max_b_ptr=None):
     """scamp_gb300_join_dev: every pointer is device memory (integers, e.g.
-    ``tensor.data_ptr()``), results merged in place, ordered on ``stream``."""
+    ``tensor.data_ptr()``), results merged in place, ordered on ``stream``.
+    ``max_a_ptr`` / ``max_b_ptr``: float32 profiles of the 1NN type."""
     lib = _lib.load()
     ca = _args(None, None, m, profile, precision, computing_rows, computing_cols,
                keep_rows, aligned, threshold, -1, -1, max_tile_size,
@@ -206,6 +217,7 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
     res.profile_a, res.profile_b = profile_a_ptr, profile_b_ptr
     res.sum_a, res.sum_b = sum_a_ptr, sum_b_ptr
     res.corr_a, res.corr_b = corr_a_ptr, corr_b_ptr
+    res.max_a, res.max_b = max_a_ptr, max_b_ptr
     err = ctypes.create_string_buffer(1024)
     rc = lib.scamp_gb300_join_dev(ctypes.byref(ca), ctypes.byref(res),
                                   ctypes.c_void_p(stream), err, 1024)

@@ -12,6 +12,7 @@ LIB_PATH = os.path.join(PKG_DIR, "libscamp_gb300.so")
 
 PROFILE_1NN_INDEX = 1
 PROFILE_SUM_THRESH = 2
+PROFILE_1NN = 6
 PRECISION_SINGLE = 1
 PRECISION_MIXED = 2
 PRECISION_DOUBLE = 3
@@ -89,6 +90,8 @@ class CResult(ctypes.Structure):
         ("slow_steps", ctypes.c_uint64),
         ("verifications", ctypes.c_uint64),
         ("verify_kernel_ms", ctypes.c_double),
+        ("max_a", ctypes.c_void_p),
+        ("max_b", ctypes.c_void_p),
     ]
 
 

@@ -10,7 +10,8 @@ index to --output_a_index_file_name (mp_columns_out_index); with --keep_rows
 the row profile goes to --output_b_file_name / --output_b_index_file_name.
 Values are z-normalised Euclidean distances (or Pearson correlations with
 --output_pearson), 10 significant digits; unmatched entries are "nan" with
-index -1.  SUM_THRESH writes the per-window sums.  Exit status 1 with the
+index -1.  --profile_type=1NN writes the distances only (no index file),
+SUM_THRESH the per-window sums.  Exit status 1 with the
 reference's message for invalid arguments.
 
 Flags of the reference that select other machinery (distributed execution,
@@ -155,6 +156,20 @@ def write_profile(path_mp, path_mpi, packed, pearson, window):
         f.write("".join("%d\n" % i for i in idx.tolist()))
 
 
+def write_max_profile(path_mp, corr, pearson, window):
+    """WriteProfileToFile for 1NN profiles (src/scamp_utils.cpp:172-183):
+    distances (or correlations), no index file."""
+    corr = np.asarray(corr).astype(np.float64)
+    if pearson:
+        vals = np.where(corr < -1, np.nan, corr)
+    else:
+        with np.errstate(invalid="ignore"):
+            vals = np.sqrt(np.maximum(2.0 * window * (1.0 - corr), 0.0))
+        vals[corr < -1] = np.nan
+    with open(path_mp, "w") as f:
+        f.write("".join(_fmt(v) + "\n" for v in vals.tolist()))
+
+
 def write_sums(path, sums):
     with open(path, "w") as f:
         f.write("".join(_fmt(v) + "\n" for v in np.asarray(sums, dtype=np.float64).tolist()))
@@ -182,7 +197,7 @@ def run(argv):
                          "--input_a_file_name")
     if fl["no_gpu"]:
         raise UsageError("Error: this engine runs on the GPU only (--no_gpu is not supported)")
-    if fl["profile_type"] not in ("1NN_INDEX", "SUM_THRESH"):
+    if fl["profile_type"] not in ("1NN_INDEX", "SUM_THRESH", "1NN"):
         raise UsageError("Error: profile type %s is not supported by this engine"
                          % fl["profile_type"])
     self_join = not fl["input_b_file_name"]
@@ -205,6 +220,10 @@ def run(argv):
         if keep:
             write_profile(fl["output_b_file_name"], fl["output_b_index_file_name"],
                           r["profile_b"], fl["output_pearson"], m)
+    elif fl["profile_type"] == "1NN":
+        write_max_profile(fl["output_a_file_name"], r["profile_a"], fl["output_pearson"], m)
+        if keep:
+            write_max_profile(fl["output_b_file_name"], r["profile_b"], fl["output_pearson"], m)
     else:
         write_sums(fl["output_a_file_name"], r["sum_a"])
         if keep:

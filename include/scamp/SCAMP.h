@@ -5,7 +5,8 @@
 // fields and meaning (zpzim/GPU-SCRIMP-LARGE src/common.h:164-188), the
 // profile enums (src/common.h:34-58), Profile/ProfileData storage of the
 // results (src/common.h:96-150, 1NN_INDEX in data[0].uint64_value with the
-// mp_entry layout, SUM_THRESH in data[0].double_value), InitProfileMemory
+// mp_entry layout, SUM_THRESH in data[0].double_value, 1NN in
+// data[0].float_value), InitProfileMemory
 // (src/scamp_utils.cpp:226-245), do_SCAMP (src/SCAMP.h:15-18) and
 // SCAMPException for every failure (src/scamp_exception.h:7-22,
 // src/common.cpp:417-436).  Link with libscamp_gb300.so.
@@ -39,6 +40,7 @@ enum SCAMPProfileType {
   PROFILE_TYPE_INVALID = 0,
   PROFILE_TYPE_1NN_INDEX = SCAMP_PROFILE_1NN_INDEX,
   PROFILE_TYPE_SUM_THRESH = SCAMP_PROFILE_SUM_THRESH,
+  PROFILE_TYPE_1NN = SCAMP_PROFILE_1NN,
 };
 
 enum SCAMPPrecisionType {
@@ -52,6 +54,7 @@ enum SCAMPPrecisionType {
 struct ProfileData {
   std::vector<uint64_t> uint64_value;  // 1NN_INDEX: low word float r, high word index
   std::vector<double> double_value;    // SUM_THRESH
+  std::vector<float> float_value;      // 1NN: best correlation
 };
 
 struct Profile {
@@ -59,7 +62,7 @@ struct Profile {
   Profile(SCAMPProfileType t, size_t size) : type(t) { Alloc(size); }
 
   // Best-so-far initial values: {r = -2.0f, index = 0xFFFFFFFF} per 1NN_INDEX
-  // entry, 0 per SUM_THRESH entry.
+  // entry, -2.0f per 1NN entry, 0 per SUM_THRESH entry.
   void Alloc(size_t size) {
     data.assign(1, ProfileData());
     if (type == PROFILE_TYPE_1NN_INDEX) {
@@ -70,6 +73,8 @@ struct Profile {
       data[0].uint64_value.assign(size, (uint64_t{0xFFFFFFFFu} << 32) | bits);
     } else if (type == PROFILE_TYPE_SUM_THRESH) {
       data[0].double_value.assign(size, 0.0);
+    } else if (type == PROFILE_TYPE_1NN) {
+      data[0].float_value.assign(size, -2.0f);
     }
   }
 
@@ -152,11 +157,13 @@ inline void do_SCAMP(SCAMPArgs* args, const std::vector<int>& devices, int num_t
   c.device = devices.empty() ? 0 : devices[0];
   detail::check(scamp_gb300_validate(&c, msg, sizeof msg), msg);
   const bool nn = args->profile_type == PROFILE_TYPE_1NN_INDEX;
+  const bool nn_max = args->profile_type == PROFILE_TYPE_1NN;
   const size_t na = args->timeseries_a.size() - args->window + 1;
   const size_t nb = args->has_b ? args->timeseries_b.size() - args->window + 1 : na;
   auto sized = [&](Profile& p, size_t n) {
     if (p.type != args->profile_type || p.data.empty() ||
-        (nn ? p.data[0].uint64_value.size() : p.data[0].double_value.size()) != n)
+        (nn ? p.data[0].uint64_value.size()
+            : nn_max ? p.data[0].float_value.size() : p.data[0].double_value.size()) != n)
       throw SCAMPException("Error: profile memory not initialised (call InitProfileMemory)");
   };
   sized(args->profile_a, na);
@@ -165,6 +172,9 @@ inline void do_SCAMP(SCAMPArgs* args, const std::vector<int>& devices, int num_t
   if (nn) {
     r.profile_a = args->profile_a.data[0].uint64_value.data();
     if (args->keep_rows_separate) r.profile_b = args->profile_b.data[0].uint64_value.data();
+  } else if (nn_max) {
+    r.max_a = args->profile_a.data[0].float_value.data();
+    if (args->keep_rows_separate) r.max_b = args->profile_b.data[0].float_value.data();
   } else {
     r.sum_a = args->profile_a.data[0].double_value.data();
     if (args->keep_rows_separate) r.sum_b = args->profile_b.data[0].double_value.data();

@@ -29,6 +29,7 @@ extern "C" {
 enum {
   SCAMP_PROFILE_1NN_INDEX = 1,
   SCAMP_PROFILE_SUM_THRESH = 2,
+  SCAMP_PROFILE_1NN = 6, /* best correlation only, float32 (no index) */
 };
 enum {
   SCAMP_PRECISION_SINGLE = 1,
@@ -104,6 +105,11 @@ typedef struct scamp_c_result {
   uint64_t slow_steps;
   uint64_t verifications;
   double verify_kernel_ms; /* part of join_kernel_ms: deferred verification */
+  /* 1NN (SCAMP_PROFILE_1NN): the best correlation per window as float32,
+   * -2.0f = none (the reference's float profile, src/common.cpp:290-292);
+   * in/out like profile_a / profile_b. */
+  float *max_a;
+  float *max_b;
 } scamp_c_result;
 
 /* Runs one join.  Inputs and results are HOST memory; the engine copies them

@@ -20,7 +20,9 @@ REF_PATH = os.path.join(HERE, "_ref", "libscampref.so")
 
 PROFILE_1NN_INDEX = 1
 PROFILE_SUM_THRESH = 2
-_PROFILE = {"1NN_INDEX": PROFILE_1NN_INDEX, "SUM_THRESH": PROFILE_SUM_THRESH}
+PROFILE_1NN = 6
+_PROFILE = {"1NN_INDEX": PROFILE_1NN_INDEX, "SUM_THRESH": PROFILE_SUM_THRESH,
+            "1NN": PROFILE_1NN}
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -45,6 +47,7 @@ class _Args(ctypes.Structure):
         ("brute_force", ctypes.c_int),
         ("high_precision_stats", ctypes.c_int),
         ("exact_flat", ctypes.c_int),
+        ("combined_terms", ctypes.c_int),
     ]
 
 
@@ -126,13 +129,27 @@ def pack(corr, idx):
 def join(a, b=None, m=None, profile="1NN_INDEX", computing_rows=True,
          computing_cols=True, keep_rows=False, aligned=False, start_row=-1,
          start_col=-1, threshold=0.0, threads=0, brute=False,
-         high_precision_stats=False, exact_flat=False):
+         high_precision_stats=False, exact_flat=False, precision=3):
     """Matrix-profile join on the CPU oracle.
+
+    ``precision`` takes the reference's SCAMPPrecisionType values; 4 (ULTRA)
+    selects its brute-force statistics and combined update terms
+    (src/SCAMP.cpp:200-212), any other value the DOUBLE path.
 
     Returns a dict with, per profile side that is produced, ``corr_*``
     (double, -2 where no match), ``idx_*`` (int64, -1 where no match),
     ``packed_*`` (reference uint64 layout) for 1NN_INDEX, or ``sum_*``.
     """
+    if profile == "1NN":
+        # the reference's PROFILE_TYPE_1NN: each window's best correlation as
+        # float32, -2 where none (the 1NN_INDEX search without the index)
+        r = join(a, b, m, "1NN_INDEX", computing_rows, computing_cols, keep_rows, aligned,
+                 start_row, start_col, threshold, threads, brute, high_precision_stats,
+                 exact_flat, precision)
+        r["max_a"] = r["corr_a"].astype(np.float32)
+        if keep_rows:
+            r["max_b"] = r["corr_b"].astype(np.float32)
+        return r
     lib = load()
     a = np.ascontiguousarray(a, dtype=np.float64)
     has_b = b is not None
@@ -145,7 +162,8 @@ def join(a, b=None, m=None, profile="1NN_INDEX", computing_rows=True,
                  len(b) if has_b else 0, m, ptype, int(computing_rows),
                  int(computing_cols), int(keep_rows), int(aligned), start_row,
                  start_col, float(threshold), int(threads), int(brute),
-                 int(high_precision_stats), int(exact_flat))
+                 int(high_precision_stats or precision == 4), int(exact_flat),
+                 int(precision == 4))
     res = {}
     out = _Out()
     if ptype == PROFILE_1NN_INDEX:
@@ -218,6 +236,10 @@ def ref_join(a, b=None, m=None, profile="1NN_INDEX", computing_rows=True,
         res = {"packed_a": pa}
         if keep_rows:
             res["packed_b"] = pb
+    elif ptype == PROFILE_1NN:
+        res = {"max_a": sa.astype(np.float32)}
+        if keep_rows:
+            res["max_b"] = sb.astype(np.float32)
     else:
         res = {"sum_a": sa}
         if keep_rows:

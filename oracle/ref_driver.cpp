@@ -72,6 +72,14 @@ extern "C" int ref_scamp_join(const double* a, uint64_t na, const double* b,
         const auto& pb = args.profile_b.data[0].double_value;
         std::memcpy(sum_b, pb.data(), pb.size() * sizeof(double));
       }
+    } else if (args.profile_type == SCAMP::PROFILE_TYPE_1NN) {
+      // float profile, returned widened to double in sum_a / sum_b
+      const auto& pa = args.profile_a.data[0].float_value;
+      for (size_t i = 0; i < pa.size(); ++i) sum_a[i] = pa[i];
+      if (keep_rows && sum_b) {
+        const auto& pb = args.profile_b.data[0].float_value;
+        for (size_t i = 0; i < pb.size(); ++i) sum_b[i] = pb[i];
+      }
     }
   } catch (const std::exception& e) {
     std::strncpy(err, e.what(), errlen);

@@ -148,6 +148,33 @@ void oracle_stats(const double *T_clean, const unsigned char *nanwin, int64_t n,
   dg[ns - 1] = 0;
 }
 
+/* Restates compute_combined_stats_cpu, src/cpu_stats.cpp:162-196: the
+ * update terms ULTRA uses instead of df/dg (src/tile.cpp:404-409).  Series A
+ * (role 0) gets df = -(T[i] - mu[i]), dg = T[i+m] - mu[i+1]; series B (role 1)
+ * gets df = T[i+m] - mu'[i+1], dg = T[i] - mu'[i+1], with mu' the brute-force
+ * (m-1)-sample means.  The reference fills the last window's terms from one
+ * sample past the series; the recurrence never uses them, and they are 0
+ * here. */
+void oracle_combined_terms(const double *T_clean, int64_t n, int64_t m,
+                           const double *means, int role, double *df,
+                           double *dg) {
+  int64_t ns = n - m + 1;
+  for (int64_t i = 0; i < ns - 1; ++i) {
+    if (role == 0) {
+      df[i] = -1 * (T_clean[i] - means[i]);
+      dg[i] = T_clean[i + m] - means[i + 1];
+    } else {
+      double sum = 0;
+      for (int64_t j = 0; j < m - 1; ++j) sum += T_clean[i + 1 + j];
+      double mu1 = sum / (double)(m - 1);
+      df[i] = T_clean[i + m] - mu1;
+      dg[i] = T_clean[i] - mu1;
+    }
+  }
+  df[ns - 1] = 0;
+  dg[ns - 1] = 0;
+}
+
 /* Restates compute_QT_CPU, src/qt_helper.cpp:52-72: the first row of a tile,
  * QT[j] = sum_t (T[j+t] - mu_T[j]) * (Q[t] - mu_Q[0]), with window means from
  * a plain rolling sum, for j in [0, count). */
@@ -204,6 +231,7 @@ typedef struct {
   int brute_force;  /* 1: every cell from a fresh compensated dot product */
   int high_precision_stats; /* 1: ULTRA-style brute force means / ssd */
   int exact_flat; /* 1: decide flatness (ssd <= 1e-13) from an exact ssd */
+  int combined_terms; /* 1: ULTRA's combined update terms (see below) */
 } oracle_args;
 
 typedef struct {
@@ -333,11 +361,12 @@ typedef struct {
   double *T_clean;
   unsigned char *nanwin;
   double *mu, *in, *df, *dg;
+  double *df_rows, *dg_rows; /* the row role's terms (ULTRA self-join), or df/dg */
   int64_t n, ns;
 } series_t;
 
 static int series_init(series_t *s, const double *T, int64_t n, int64_t m,
-                       int hp, int exact_flat) {
+                       int hp, int exact_flat, int role, int rows_role) {
   s->n = n;
   s->ns = n - m + 1;
   s->T_clean = malloc(sizeof(double) * n);
@@ -350,6 +379,19 @@ static int series_init(series_t *s, const double *T, int64_t n, int64_t m,
     return -1;
   oracle_clean(T, n, m, s->T_clean, s->nanwin);
   oracle_stats(s->T_clean, s->nanwin, n, m, hp, s->mu, s->in, s->df, s->dg);
+  s->df_rows = s->df;
+  s->dg_rows = s->dg;
+  /* ULTRA (role >= 0): this series' combined terms replace df/dg; a
+   * self-join's rows (rows_role >= 0) take the other role's terms */
+  if (role >= 0)
+    oracle_combined_terms(s->T_clean, n, m, s->mu, role, s->df, s->dg);
+  if (rows_role >= 0 && rows_role != role) {
+    s->df_rows = malloc(sizeof(double) * s->ns);
+    s->dg_rows = malloc(sizeof(double) * s->ns);
+    if (!s->df_rows || !s->dg_rows) return -1;
+    oracle_combined_terms(s->T_clean, n, m, s->mu, rows_role, s->df_rows,
+                          s->dg_rows);
+  }
   if (exact_flat) {
     /* The reference's sequential ssd recurrence can leave a rounding residue
      * above 1e-13 on exactly flat windows; this mode applies the flatness
@@ -371,6 +413,8 @@ static int series_init(series_t *s, const double *T, int64_t n, int64_t m,
 }
 
 static void series_free(series_t *s) {
+  if (s->df_rows != s->df) free(s->df_rows);
+  if (s->dg_rows != s->dg) free(s->dg_rows);
   free(s->T_clean);
   free(s->nanwin);
   free(s->mu);
@@ -389,9 +433,9 @@ static band_t make_band(const series_t *rows, const series_t *cols,
   b.mu_c = cols->mu;
   b.in_r = rows->in;
   b.in_c = cols->in;
-  b.df_r = rows->df;
+  b.df_r = rows->df_rows;
   b.df_c = cols->df;
-  b.dg_r = rows->dg;
+  b.dg_r = rows->dg_rows;
   b.dg_c = cols->dg;
   b.n_r = rows->ns;
   b.n_c = cols->ns;
@@ -423,11 +467,14 @@ int oracle_join(const oracle_args *args, oracle_out *out) {
   if (ptype != ORACLE_PROFILE_1NN_INDEX && ptype != ORACLE_PROFILE_SUM_THRESH)
     return -2;
   series_t A, B;
+  /* ULTRA: A takes the "A" terms and B the "B" terms (the reference's
+   * roles); a self-join's rows take the "B" terms of A */
+  int ct = args->combined_terms;
   if (series_init(&A, args->a, args->na, m, args->high_precision_stats,
-                  args->exact_flat))
+                  args->exact_flat, ct ? 0 : -1, (ct && self) ? 1 : -1))
     return -3;
   if (!self && series_init(&B, args->b, args->nb, m, args->high_precision_stats,
-                           args->exact_flat)) {
+                           args->exact_flat, ct ? 1 : -1, -1)) {
     series_free(&A);
     return -3;
   }

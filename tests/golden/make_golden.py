@@ -2,10 +2,11 @@
 
 Run where the reference tree exists (it builds oracle/_ref/libscampref.so
 from the reference's sources with oracle/Makefile):
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [fixture names]
 Each fixture holds seeded inputs, the join options and the reference's
-output (packed 1NN_INDEX entries or SUM_THRESH sums, DOUBLE precision, one
-thread, the pyscamp default max_tile_size of 128000 unless stated).
+output (packed 1NN_INDEX entries, SUM_THRESH sums or 1NN float profiles;
+DOUBLE precision, one thread, the pyscamp default max_tile_size of 128000
+unless stated).
 """
 import os
 import sys
@@ -37,13 +38,23 @@ def cases():
     out.append(("sum_self_t05_m64", rw(2500), None, 64, {"profile": "SUM_THRESH", "threshold": 0.5}))
     out.append(("sum_ab_keep_t025_m32", rw(2000), rw(1500), 32,
                 {"profile": "SUM_THRESH", "threshold": 0.25, "keep_rows": True}))
+    # ULTRA precision (the reference's SCAMPPrecisionType 4): brute-force
+    # statistics and combined update terms
+    out.append(("ultra_self_rw3000_m64", rw(3000), None, 64, {"precision": 4}))
+    out.append(("ultra_ab_keep_offset_m50", 1e4 + rw(2500), 1e4 + rw(1800), 50,
+                {"precision": 4, "keep_rows": True}))
+    # PROFILE_TYPE_1NN: the best correlation per window, float32, no index
+    out.append(("nn_self_rw3000_m64", rw(3000), None, 64, {"profile": "1NN"}))
+    out.append(("nn_ab_keep_m40", rw(2000), rw(1500), 40, {"profile": "1NN", "keep_rows": True}))
     return out
 
 
-def main():
+def main(only=()):
     if not oracle.ref_available():
         raise SystemExit("build the reference first: make -C oracle ref")
     for name, a, b, m, kw in cases():
+        if only and name not in only:
+            continue
         res = oracle.ref_join(a, b, m, threads=1, **kw)
         data = {"a": a, "m": np.int64(m)}
         if b is not None:
@@ -58,4 +69,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

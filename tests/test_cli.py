@@ -48,6 +48,14 @@ def test_write_profile_format(tmp_path):
     assert scamp_gb300.NO_MATCH  # the package imports without a GPU
 
 
+def test_write_max_profile_format(tmp_path):
+    mp = tmp_path / "mp"
+    cli.write_max_profile(str(mp), np.array([0.5, -2.0, 1.0], dtype=np.float32), False, 10)
+    assert mp.read_text().split() == [format(np.sqrt(10.0), ".10g"), "nan", "0"]
+    cli.write_max_profile(str(mp), np.array([0.5, -2.0, 1.0], dtype=np.float32), True, 10)
+    assert mp.read_text().split() == ["0.5", "nan", "1"]
+
+
 @pytest.mark.parametrize("argv,msg", [
     (["--window=2", "--input_a_file_name=x"], "Subsequence length must be at least 3"),
     (["--window=10"], "primary input filename"),
@@ -101,3 +109,18 @@ def test_cli_abjoin_keep_rows(gpu_engine, tmp_path):
         assert np.array_equal(got_i, i)
         ok = c >= -1
         assert np.allclose(got_c[ok], c[ok], rtol=0, atol=1e-9)
+
+
+@pytest.mark.gpu
+def test_cli_profile_type_1nn(gpu_engine, tmp_path):
+    rng = np.random.default_rng(6)
+    a = np.cumsum(rng.standard_normal(3000))
+    fa = tmp_path / "a.txt"
+    fa.write_text("".join(repr(float(v)) + "\n" for v in a) + "\n")
+    mp = tmp_path / "mp"
+    assert cli.main(["--window=50", "--input_a_file_name=%s" % fa, "--profile_type=1NN",
+                     "--output_pearson", "--output_a_file_name=%s" % mp]) == 0
+    got = np.array([float(v) for v in mp.read_text().split()])
+    r = gpu_engine.join(a, None, 50, "1NN_INDEX", "double")
+    c, _ = gpu_engine.unpack_profile(r["profile_a"])
+    assert np.max(np.abs(got - c.astype(np.float64))) < 1e-8

@@ -20,13 +20,14 @@ def rw(rng, n):
 
 
 def run_1nn(engine, oracle, a, b, m, precision, tol, keep_rows=False, rows=True,
-            aligned=False, name="", brute=False, **kw):
+            aligned=False, name="", brute=False, oracle_precision=3, **kw):
     got = engine.join(a, b, m, "1NN_INDEX", precision, computing_rows=rows,
                       keep_rows=keep_rows, aligned=aligned, return_corr=True, **kw)
     # exact_flat: flatness decided from an exact ssd (the engine's rule); the
     # reference's sequential ssd can leave flat windows "valid".
     want = oracle.join(a, b, m, "1NN_INDEX", computing_rows=rows, keep_rows=keep_rows,
-                       aligned=aligned, exact_flat=True, brute=brute)
+                       aligned=aligned, exact_flat=True, brute=brute,
+                       precision=oracle_precision)
     _, gi = engine.unpack_profile(got["profile_a"])
     T_other = a if b is None else b
     check_1nn(name + "/A", got["corr_a"], gi, want["corr_a"], want["idx_a"], tol, a, T_other, m)
@@ -104,6 +105,54 @@ def test_selfjoin_keep_rows_separate(gpu_engine, oracle_mod, precision, tol):
     rng = np.random.default_rng(9)
     a = rw(rng, 3000)
     run_1nn(gpu_engine, oracle_mod, a, None, 40, precision, tol, keep_rows=True, name="selfkr")
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_profile_type_1nn(gpu_engine, oracle_mod, precision):
+    """PROFILE_TYPE_1NN: the best correlation per window (float32, -2 where
+    none) -- the 1NN_INDEX search without the index -- merged by max into a
+    given best-so-far profile."""
+    rng = np.random.default_rng(44)
+    a = rw(rng, 3000)
+    b = rw(rng, 2200)
+    tol = TOL_FP64 if precision == "double" else TOL_MIXED
+    for bb, kw in ((None, {}), (b, {"keep_rows": True})):
+        got = gpu_engine.join(a, bb, 60, "1NN", precision, **kw)
+        want = oracle_mod.join(a, bb, 60, profile="1NN", **kw)
+        for side in ("a", "b"):
+            if "max_" + side not in want:
+                continue
+            g = got["profile_" + side]
+            assert g.dtype == np.float32
+            w = want["max_" + side].astype(np.float64)
+            assert np.array_equal(g < -1, w < -1)
+            assert np.max(np.abs(g[w >= -1] - w[w >= -1])) <= tol + 2.5e-7
+    # merge: a best-so-far above every correlation survives; -2 entries fill
+    init = np.full(len(a) - 60 + 1, -2.0, dtype=np.float32)
+    init[::7] = 1.0
+    got = gpu_engine.join(a, None, 60, "1NN", precision, profile_a=init)
+    plain = gpu_engine.join(a, None, 60, "1NN", precision)
+    assert np.all(got["profile_a"][::7] == 1.0)
+    mask = np.ones(len(init), bool)
+    mask[::7] = False
+    assert np.array_equal(got["profile_a"][mask], plain["profile_a"][mask])
+
+
+def test_ultra_against_oracle(gpu_engine, oracle_mod):
+    """ULTRA: brute-force window statistics and the reference's combined
+    update terms (the oracle's precision=4 restates them; the reference's own
+    ULTRA output is pinned by the golden fixtures), FP64 tolerance."""
+    rng = np.random.default_rng(41)
+    a = rw(rng, 4000)
+    b = rw(rng, 2500)
+    run_1nn(gpu_engine, oracle_mod, a, None, 64, "ultra", TOL_FP64, name="ultra-self",
+            oracle_precision=4)
+    run_1nn(gpu_engine, oracle_mod, a, None, 64, "ultra", TOL_FP64, keep_rows=True,
+            name="ultra-self-kr", oracle_precision=4)
+    run_1nn(gpu_engine, oracle_mod, a, b, 64, "ultra", TOL_FP64, keep_rows=True,
+            name="ultra-ab", oracle_precision=4)
+    run_1nn(gpu_engine, oracle_mod, 1e4 + a, 1e4 + b, 50, "ultra", TOL_FP64, keep_rows=True,
+            name="ultra-ab-offset", oracle_precision=4)
 
 
 @pytest.mark.parametrize("precision", ["double", "mixed"])
@@ -216,10 +265,16 @@ def test_against_reference_golden_fixtures(gpu_engine, precision, tol):
         profile = kw.pop("profile", "1NN_INDEX")
         thr = kw.pop("threshold", 0.0)
         rows = kw.pop("computing_rows", True)
+        form = precision
+        if kw.pop("precision", 3) == 4:
+            # an ULTRA fixture: the reference's ULTRA path against ours
+            if precision != "double":
+                continue
+            form = "ultra"
         a = z["a"]
         b = z["b"] if "b" in z.files else None
         m = int(z["m"])
-        got = gpu_engine.join(a, b, m, profile, precision, computing_rows=rows,
+        got = gpu_engine.join(a, b, m, profile, form, computing_rows=rows,
                               threshold=thr, **kw)
         for side in ("a", "b"):
             if "packed_" + side in z.files:
@@ -243,6 +298,11 @@ def test_against_reference_golden_fixtures(gpu_engine, precision, tol):
                 if mism.size:
                     r = pair_corr(other, mine, m, gi[mism], mism)
                     assert np.all(np.abs(r - wc[mism]) <= tol + 2.5e-7), f
+            if "max_" + side in z.files:
+                w = z["max_" + side].astype(np.float64)
+                g = got["profile_" + side].astype(np.float64)
+                assert np.array_equal(w < -1, g < -1), f
+                assert np.max(np.abs(w[w >= -1] - g[w >= -1])) <= tol + 2.5e-7, f
             if "sum_" + side in z.files:
                 rt = 1e-9 if precision == "double" else 2e-5
                 check_sum(f, got["sum_" + side], z["sum_" + side], thr, rt,

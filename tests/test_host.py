@@ -61,6 +61,9 @@ def test_validate_rejects(engine, field, value, msg):
 def test_validate_accepts(engine):
     ca, _keep = _args(engine)
     assert engine._lib.load().scamp_gb300_validate(ctypes.byref(ca), None, 0) == 0
+    for ptype in (1, 2, 6):  # 1NN_INDEX, SUM_THRESH, 1NN
+        ca.profile_type = ptype
+        assert engine._lib.load().scamp_gb300_validate(ctypes.byref(ca), None, 0) == 0
 
 
 @pytest.mark.parametrize("n,m", [(131072, 100), (1000, 3), (5000, 1024), (64, 64)])

@@ -130,6 +130,10 @@ def test_oracle_vs_committed_golden_fixtures(oracle_mod):
                 assert np.max(np.abs(wc[ok].astype(np.float64) - gc[ok])) <= 2.5e-7, f
             if "sum_" + side in z.files:
                 np.testing.assert_allclose(got["sum_" + side], z["sum_" + side], rtol=1e-6, atol=1e-6)
+            if "max_" + side in z.files:
+                w, g = z["max_" + side].astype(np.float64), got["max_" + side].astype(np.float64)
+                assert np.array_equal(w < -1, g < -1), f
+                assert np.max(np.abs(w[w >= -1] - g[w >= -1])) <= 2.5e-7, f
 
 
 @pytest.mark.parametrize("m", [4, 10, 33])

@@ -17,7 +17,7 @@ def _walk(seed, n):
     return np.cumsum(np.random.default_rng(seed).standard_normal(n))
 
 
-def _call(entry, torch, a, b, m, profile, keep_rows=False, threshold=0.0):
+def _call(entry, torch, a, b, m, profile, keep_rows=False, threshold=0.0, precision="double"):
     """Runs one join through `entry` (a C-ABI function taking device
     pointers) on fresh best-so-far buffers; returns host copies."""
     import scamp_gb300
@@ -31,7 +31,7 @@ def _call(entry, torch, a, b, m, profile, keep_rows=False, threshold=0.0):
     nn = profile == "1NN_INDEX"
     no_match = np.array([scamp_gb300.NO_MATCH], dtype=np.uint64).view(np.int64)[0]
     outs = {}
-    ca = scamp_gb300._args(None, None, m, profile, "double", True, True, keep_rows, False,
+    ca = scamp_gb300._args(None, None, m, profile, precision, True, True, keep_rows, False,
                            threshold, -1, -1, 128000, 0, 0, True)
     ca.timeseries_a = a_d.data_ptr()
     ca.len_a = len(a)
@@ -71,11 +71,13 @@ def _compare(got, ref, nn):
 
 
 CASES = [
-    # (seed, len_a, len_b, m, profile, keep_rows, threshold)
-    (1, 20000, None, 100, "1NN_INDEX", False, 0.0),
-    (2, 30000, 20000, 64, "1NN_INDEX", True, 0.0),
-    (3, 65536, None, 256, "1NN_INDEX", False, 0.0),
-    (4, 12000, None, 50, "SUM_THRESH", False, 0.5),
+    # (seed, len_a, len_b, m, profile, keep_rows, threshold, precision)
+    (1, 20000, None, 100, "1NN_INDEX", False, 0.0, "double"),
+    (2, 30000, 20000, 64, "1NN_INDEX", True, 0.0, "double"),
+    (3, 65536, None, 256, "1NN_INDEX", False, 0.0, "double"),
+    (4, 12000, None, 50, "SUM_THRESH", False, 0.5, "double"),
+    (5, 20000, None, 64, "1NN_INDEX", False, 0.0, "ultra"),
+    (6, 15000, 10000, 50, "1NN_INDEX", True, 0.0, "ultra"),
 ]
 
 
@@ -84,14 +86,14 @@ def test_noalloc_equals_join_dev_twice(gpu_engine):
     from scamp_gb300 import _lib
 
     lib = _lib.load()
-    for seed, la, lb, m, profile, keep, thr in CASES:
+    for seed, la, lb, m, profile, keep, thr, prec in CASES:
         a = _walk(seed, la)
         b = _walk(seed + 100, lb) if lb else None
-        rc, msg, ref = _call(lib.scamp_gb300_join_dev, torch, a, b, m, profile, keep, thr)
+        rc, msg, ref = _call(lib.scamp_gb300_join_dev, torch, a, b, m, profile, keep, thr, prec)
         assert rc == 0, msg
         for _ in range(2):  # two calls in a row on the same static scratch
             rc, msg, got = _call(lib.scamp_gb300_join_dev_noalloc, torch, a, b, m, profile,
-                                 keep, thr)
+                                 keep, thr, prec)
             assert rc == 0, msg
             _compare(got, ref, profile == "1NN_INDEX")
 
