@@ -49,7 +49,7 @@ OPS_PER_CELL = 4
 # workload: one single-pass ncu capture of the full-size launch
 # (profiles/join_mixed_1nn_cfg2.txt).  Mostly the verification requests and
 # profile atomics: the series, statistics and profiles stay in the 129 MB L2.
-DRAM_BYTES_PER_LAUNCH = 51.12e6 + 109.69e6
+DRAM_BYTES_PER_LAUNCH = 51.47e6 + 109.83e6
 
 
 def max_over_ranks(x, dist, device):
