@@ -172,6 +172,33 @@ def test_sum_thresh(gpu_engine, oracle_mod, precision, thr):
     check_sum("absum/B", got["sum_b"], want["sum_b"], thr, rtol, ctol)
 
 
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_sum_thresh_geometries(gpu_engine, oracle_mod, precision):
+    """SUM_THRESH over the other join geometries: AB columns only, aligned
+    AB with distributed offsets, NaN gaps and flat stretches, a window of 8."""
+    rng = np.random.default_rng(52)
+    rtol = 1e-9 if precision == "double" else 2e-5
+    ctol = 0.0 if precision == "double" else TOL_MIXED
+    a = rw(rng, 3500)
+    b = rw(rng, 2600)
+    thr = 0.6
+    cases = [
+        (a, b, 64, dict(computing_rows=False)),
+        (a, a[:3000].copy(), 64, dict(aligned=True, keep_rows=True, start_row=100, start_col=130)),
+        (a, None, 8, {}),
+    ]
+    g = a.copy()
+    g[rng.choice(len(g), 10, replace=False)] = np.nan
+    g[900:1000] = 3.0
+    cases.append((g, None, 48, {}))
+    for x, y, m, kw in cases:
+        got = gpu_engine.join(x, y, m, "SUM_THRESH", precision, threshold=thr, **kw)
+        want = oracle_mod.join(x, y, m, "SUM_THRESH", threshold=thr, exact_flat=True, **kw)
+        check_sum("geom/A %s" % sorted(kw), got["sum_a"], want["sum_a"], thr, rtol, ctol)
+        if "sum_b" in want:
+            check_sum("geom/B %s" % sorted(kw), got["sum_b"], want["sum_b"], thr, rtol, ctol)
+
+
 def test_sum_thresh_many_units(gpu_engine):
     """Mixed SUM_THRESH over thousands of band units of both AB problems
     (their column series differ in length), against the FP64 form, which the
