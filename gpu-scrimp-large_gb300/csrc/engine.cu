@@ -28,6 +28,8 @@ namespace scamp_gb300 {
 int fp64_band_width();
 int fp64_slab_rows();
 int fp64_threads();
+int visit_band_width();
+int visit_threads();
 int mixed_1nn_band_width();
 int mixed_1nn_slab_rows();
 int mixed_1nn_threads();
@@ -97,9 +99,21 @@ int validate(const scamp_c_args* a, std::string* msg) {
     return SCAMP_ERR_INVALID_ARGS;
   }
   if (a->profile_type != SCAMP_PROFILE_1NN_INDEX && a->profile_type != SCAMP_PROFILE_SUM_THRESH &&
-      a->profile_type != SCAMP_PROFILE_1NN) {
-    *msg = "Error: profile type not supported by this engine (1NN_INDEX, SUM_THRESH, 1NN)";
+      a->profile_type != SCAMP_PROFILE_1NN &&
+      a->profile_type != SCAMP_PROFILE_APPROX_ALL_NEIGHBORS &&
+      a->profile_type != SCAMP_PROFILE_MATRIX_SUMMARY) {
+    *msg = "Error: profile type not supported by this engine";
     return SCAMP_ERR_UNIMPLEMENTED;
+  }
+  if (a->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS &&
+      (a->max_matches_per_column < 1 || a->max_matches_per_column > 1024)) {
+    *msg = "Error: max_matches_per_column must be between 1 and 1024";
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  if (a->profile_type == SCAMP_PROFILE_MATRIX_SUMMARY &&
+      (a->matrix_height <= 0 || a->matrix_width <= 0)) {
+    *msg = "Error: matrix height and width must be greater than 0";
+    return SCAMP_ERR_INVALID_ARGS;
   }
   if (a->precision_type < SCAMP_PRECISION_SINGLE || a->precision_type > SCAMP_PRECISION_ULTRA) {
     *msg = "Error: invalid precision type";
@@ -246,7 +260,7 @@ enum Slot {
   S_KEY_A, S_KEY_B, S_SUM_A, S_SUM_B, S_PROF_A, S_PROF_B, S_CORR_A, S_CORR_B,
   S_PREFIX, S_COUNTER, S_T32_A, S_T32_B, S_BHI_A, S_BLO_A, S_MUREL_A,
   S_BHI_B, S_BLO_B, S_MUREL_B, S_VREQ, S_PAA_A, S_PAA_B, S_SEED_A, S_SEED_B,
-  S_BATCH, S_MAX_A, S_MAX_B,
+  S_BATCH, S_MAX_A, S_MAX_B, S_KNN_A, S_KNN_B, S_MAT,
 };
 
 #define CUDA_TRY(expr)                                                     \
@@ -258,6 +272,13 @@ enum Slot {
       return SCAMP_ERR_CUDA;                                               \
     }                                                                      \
   } while (0)
+
+// Device outputs of the profile types beyond 1NN_INDEX and SUM_THRESH.
+struct ExtraOut {
+  float* max[2] = {nullptr, nullptr};     // 1NN: best correlation per window
+  uint64_t* knn[2] = {nullptr, nullptr};  // APPROX_ALL_NEIGHBORS: k entries per window
+  float* matrix = nullptr;                // MATRIX_SUMMARY: height x width
+};
 
 struct SeriesBufs {
   double *T, *mean, *inv, *df, *dg;
@@ -334,8 +355,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
                const double* dA, const double* dB, uint64_t* dprof_a,
                uint64_t* dprof_b, double* dsum_a, double* dsum_b,
                double* dcorr_a, double* dcorr_b, cudaStream_t st,
-               std::string* msg, bool nested = false, float* dmax_a = nullptr,
-               float* dmax_b = nullptr);
+               std::string* msg, bool nested = false, const ExtraOut* ex = nullptr);
 
 // Block-averaged join of the inputs (window m / 8) into the seed profiles
 // S_SEED_A/B; returns their device pointers (seed_b null when not kept).
@@ -396,11 +416,22 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
                const double* dA, const double* dB, uint64_t* dprof_a,
                uint64_t* dprof_b, double* dsum_a, double* dsum_b,
                double* dcorr_a, double* dcorr_b, cudaStream_t st,
-               std::string* msg, bool nested, float* dmax_a, float* dmax_b) {
+               std::string* msg, bool nested, const ExtraOut* ex) {
+  scamp_c_args a_local;
+  if (a->profile_type == SCAMP_PROFILE_MATRIX_SUMMARY) {
+    // matrix summaries reduce along the columns only (src/common.cpp:98-105)
+    a_local = *a;
+    a_local.computing_rows = 0;
+    a_local.keep_rows_separate = 0;
+    a = &a_local;
+  }
   Plan plan = make_plan(a);
-  // 1NN (float best correlation, no index) runs as 1NN_INDEX on the keys
+  // 1NN (float best correlation, no index) runs as 1NN_INDEX on the keys;
+  // the k-best and matrix-summary types run the FP64 visit kernel
   const bool max_only = a->profile_type == SCAMP_PROFILE_1NN;
   const bool is_1nn = a->profile_type == SCAMP_PROFILE_1NN_INDEX || max_only;
+  const bool visit = a->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS ||
+                     a->profile_type == SCAMP_PROFILE_MATRIX_SUMMARY;
   const bool mixed = a->precision_type == SCAMP_PRECISION_MIXED ||
                      a->precision_type == SCAMP_PRECISION_SINGLE;
   const bool ultra = a->precision_type == SCAMP_PRECISION_ULTRA;
@@ -489,8 +520,31 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     if (q.col_target >= 0) used[q.col_target] = true;
     if (q.row_target >= 0) used[q.row_target] = true;
   }
-  float* maxs[2] = {dmax_a, dmax_b};
-  if (is_1nn) {
+  float* maxs[2] = {ex ? ex->max[0] : nullptr, ex ? ex->max[1] : nullptr};
+  unsigned long long* vkeys[2] = {nullptr, nullptr};
+  unsigned* vmat = nullptr;
+  const int64_t knn_k = a->max_matches_per_column;
+  const int64_t mat_n = static_cast<int64_t>(a->matrix_height) * a->matrix_width;
+  if (visit && a->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS) {
+    for (int s = 0; s < 2; ++s) {
+      if (!used[s]) continue;
+      if (!ex || !ex->knn[s]) { *msg = "Error: profile buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
+      void* p;
+      if ((rc = ensure(ws, s == 0 ? S_KNN_A : S_KNN_B, nsz[s] * knn_k * 8, &p, msg))) return rc;
+      vkeys[s] = static_cast<unsigned long long*>(p);
+      profile_to_keys_kernel<<<static_cast<unsigned>((nsz[s] * knn_k + 255) / 256), 256, 0, st>>>(
+          ex->knn[s], reinterpret_cast<uint64_t*>(vkeys[s]), nsz[s] * knn_k, kl);
+      ++launches;
+    }
+  } else if (visit) {
+    if (!ex || !ex->matrix) { *msg = "Error: profile buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
+    void* p;
+    if ((rc = ensure(ws, S_MAT, mat_n * 4, &p, msg))) return rc;
+    vmat = static_cast<unsigned*>(p);
+    floats_to_ord_kernel<<<static_cast<unsigned>((mat_n + 255) / 256), 256, 0, st>>>(
+        ex->matrix, vmat, mat_n);
+    ++launches;
+  } else if (is_1nn) {
     for (int s = 0; s < 2; ++s) {
       if (max_only) {
         if (!used[s] && !(s == 0 && maxs[0])) continue;
@@ -538,14 +592,18 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   // Kernel choice: FP64 form, or the mixed band kernel (FP32 filter; for
   // 1NN_INDEX its candidates are verified, for SUM_THRESH the filter
   // threshold is the sum threshold and every cell above it is accumulated).
-  enum { K_FP64, K_MIXED } kind = !mixed ? K_FP64 : K_MIXED;
-  const void* kfn = kind == K_FP64 ? reinterpret_cast<const void*>(join_fp64_kernel)
+  // The k-best and matrix-summary types run the FP64 visit kernel.
+  enum { K_FP64, K_MIXED, K_VISIT } kind = visit ? K_VISIT : !mixed ? K_FP64 : K_MIXED;
+  const void* kfn = kind == K_VISIT ? reinterpret_cast<const void*>(join_visit_kernel)
+                  : kind == K_FP64 ? reinterpret_cast<const void*>(join_fp64_kernel)
                   : is_1nn ? reinterpret_cast<const void*>(join_mixed_1nn_kernel)
                            : reinterpret_cast<const void*>(join_mixed_sum_kernel);
-  const int W = kind == K_FP64 ? fp64_band_width() : mixed_1nn_band_width();
-  const int slab = kind == K_FP64 ? fp64_slab_rows() : mixed_1nn_slab_rows();
-  const int nthreads = kind == K_FP64 ? fp64_threads() : mixed_1nn_threads();
-  const size_t smem = kind == K_FP64 ? 0 : mixed_1nn_smem_bytes();
+  const int W = kind == K_VISIT ? visit_band_width()
+              : kind == K_FP64 ? fp64_band_width() : mixed_1nn_band_width();
+  const int slab = kind == K_MIXED ? mixed_1nn_slab_rows() : fp64_slab_rows();
+  const int nthreads = kind == K_VISIT ? visit_threads()
+                     : kind == K_FP64 ? fp64_threads() : mixed_1nn_threads();
+  const size_t smem = kind == K_MIXED ? mixed_1nn_smem_bytes() : 0;
   if (smem > 0)
     CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(smem)));
@@ -559,7 +617,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   int64_t K;
   const double cells_d = static_cast<double>(plan.cells);
   const int64_t k_lb = static_cast<int64_t>(cells_d / (8.0 * resident * 2.0 * W));
-  if (mixed) {
+  if (kind == K_MIXED) {
     K = a->anchor_interval > 0 ? a->anchor_interval : default_anchor_interval(m);
   } else {
     K = fp64_segment(m);
@@ -663,6 +721,22 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
         ws.timed_verify = true;
       }
       verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
+    } else if (kind == K_VISIT) {
+      VisitArgs V{};
+      V.mode = a->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS ? 0 : 1;
+      V.topk[0] = vkeys[0];
+      V.topk[1] = vkeys[1];
+      V.k = static_cast<int>(knn_k);
+      V.mat = vmat;
+      V.mat_w = a->matrix_width;
+      // grid rows: windows of B (of A in a self-join), columns: windows of A
+      V.rows_per_cell = V.mode == 1 ? (nsz[1] + a->matrix_height - 1) / a->matrix_height : 1;
+      V.cols_per_cell = V.mode == 1 ? (nsz[0] + a->matrix_width - 1) / a->matrix_width : 1;
+      for (int p = 0; p < P.nprob; ++p) {
+        V.col_target[p] = plan.probs[p].col_target;
+        V.row_target[p] = plan.probs[p].row_target;
+      }
+      join_visit_kernel<<<static_cast<unsigned>(grid), nthreads, 0, st>>>(P, V);
     } else
       join_fp64_kernel<<<static_cast<unsigned>(grid), nthreads, 0, st>>>(P);
     ++launches;
@@ -671,6 +745,17 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   }
 
   // ---- keys -> packed entries (+ optional double correlations) ----
+  for (int s = 0; s < 2; ++s) {
+    if (!vkeys[s]) continue;
+    keys_to_profile_kernel<<<static_cast<unsigned>((nsz[s] * knn_k + 255) / 256), 256, 0, st>>>(
+        reinterpret_cast<const uint64_t*>(vkeys[s]), ex->knn[s], nullptr, nsz[s] * knn_k, kl);
+    ++launches;
+  }
+  if (vmat) {
+    ord_to_floats_kernel<<<static_cast<unsigned>((mat_n + 255) / 256), 256, 0, st>>>(
+        vmat, ex->matrix, mat_n);
+    ++launches;
+  }
   if (is_1nn) {
     double* corr[2] = {dcorr_a, dcorr_b};
     for (int s = 0; s < 2; ++s) {
@@ -790,9 +875,15 @@ extern "C" int scamp_gb300_join_dev(const scamp_c_args* args, scamp_c_result* re
   if ((rc = init_workspace(args->device, &ws, &msg))) { set_err(errbuf, errlen, msg); return rc; }
   std::lock_guard<std::mutex> lock(ws->mu);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  ExtraOut ex;
+  ex.max[0] = res->max_a;
+  ex.max[1] = res->max_b;
+  ex.knn[0] = res->knn_a;
+  ex.knn[1] = res->knn_b;
+  ex.matrix = res->matrix;
   rc = run_device(*ws, args, res, args->timeseries_a, args->has_b ? args->timeseries_b : args->timeseries_a,
                   res->profile_a, res->profile_b, res->sum_a, res->sum_b, res->corr_a, res->corr_b, st, &msg,
-                  false, res->max_a, res->max_b);
+                  false, &ex);
   if (rc == SCAMP_OK) {
     cudaError_t e = cudaEventSynchronize(ws->ev1);
     if (e != cudaSuccess) { msg = std::string("CUDA error: ") + cudaGetErrorString(e); rc = SCAMP_ERR_CUDA; }
@@ -816,6 +907,8 @@ extern "C" int scamp_gb300_join(const scamp_c_args* args, scamp_c_result* res,
   cudaStream_t st = ws->stream;
   const bool is_1nn = args->profile_type == SCAMP_PROFILE_1NN_INDEX;
   const bool max_only = args->profile_type == SCAMP_PROFILE_1NN;
+  const bool knn = args->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS;
+  const bool matrix = args->profile_type == SCAMP_PROFILE_MATRIX_SUMMARY;
   const int64_t na = static_cast<int64_t>(args->len_a);
   const int64_t nb = args->has_b ? static_cast<int64_t>(args->len_b) : 0;
   const int64_t nsa = na - static_cast<int64_t>(args->window) + 1;
@@ -836,22 +929,37 @@ extern "C" int scamp_gb300_join(const scamp_c_args* args, scamp_c_result* res,
     if ((rc = ensure(*ws, S_RAW_B, nb * 8, &pb, &msg))) return fail(rc);
     HOST_CUDA(cudaMemcpyAsync(pb, args->timeseries_b, nb * 8, cudaMemcpyHostToDevice, st));
   }
-  const bool want_b = args->keep_rows_separate != 0;
+  const bool want_b = args->keep_rows_separate != 0 && !matrix;
   uint64_t *dprof[2] = {nullptr, nullptr};
   double *dsum[2] = {nullptr, nullptr}, *dcorr[2] = {nullptr, nullptr};
-  float* dmax[2] = {nullptr, nullptr};
+  ExtraOut ex;
   float* hmax[2] = {res->max_a, res->max_b};
+  uint64_t* hknn[2] = {res->knn_a, res->knn_b};
+  const int64_t kk = args->max_matches_per_column;
+  const int64_t mat_n = static_cast<int64_t>(args->matrix_height) * args->matrix_width;
+  if (matrix) {
+    void* p;
+    if (!res->matrix) { msg = "Error: profile buffer missing"; return fail(SCAMP_ERR_INVALID_ARGS); }
+    if ((rc = ensure(*ws, S_MAX_A, mat_n * 4, &p, &msg))) return fail(rc);
+    ex.matrix = static_cast<float*>(p);
+    HOST_CUDA(cudaMemcpyAsync(p, res->matrix, mat_n * 4, cudaMemcpyHostToDevice, st));
+  }
   uint64_t* hprof[2] = {res->profile_a, res->profile_b};
   double* hsum[2] = {res->sum_a, res->sum_b};
   double* hcorr[2] = {res->corr_a, res->corr_b};
   const int64_t nsz[2] = {nsa, nsb};
-  for (int s = 0; s < 2; ++s) {
+  for (int s = 0; s < 2 && !matrix; ++s) {
     if (s == 1 && !want_b) continue;
     void* p;
-    if (max_only) {
+    if (knn) {
+      if (!hknn[s]) { msg = "Error: profile buffer missing"; return fail(SCAMP_ERR_INVALID_ARGS); }
+      if ((rc = ensure(*ws, s ? S_PROF_B : S_PROF_A, nsz[s] * kk * 8, &p, &msg))) return fail(rc);
+      ex.knn[s] = static_cast<uint64_t*>(p);
+      HOST_CUDA(cudaMemcpyAsync(p, hknn[s], nsz[s] * kk * 8, cudaMemcpyHostToDevice, st));
+    } else if (max_only) {
       if (!hmax[s]) { msg = "Error: profile buffer missing"; return fail(SCAMP_ERR_INVALID_ARGS); }
       if ((rc = ensure(*ws, s ? S_MAX_B : S_MAX_A, nsz[s] * 4, &p, &msg))) return fail(rc);
-      dmax[s] = static_cast<float*>(p);
+      ex.max[s] = static_cast<float*>(p);
       HOST_CUDA(cudaMemcpyAsync(p, hmax[s], nsz[s] * 4, cudaMemcpyHostToDevice, st));
       if (hcorr[s]) {
         if ((rc = ensure(*ws, s ? S_CORR_B : S_CORR_A, nsz[s] * 8, &p, &msg))) return fail(rc);
@@ -876,12 +984,15 @@ extern "C" int scamp_gb300_join(const scamp_c_args* args, scamp_c_result* res,
   rc = run_device(*ws, args, res, static_cast<double*>(pa),
                   args->has_b ? static_cast<double*>(pb) : static_cast<double*>(pa),
                   dprof[0], dprof[1], dsum[0], dsum[1], dcorr[0], dcorr[1], st, &msg,
-                  false, dmax[0], dmax[1]);
+                  false, &ex);
   if (rc) return fail(rc);
-  for (int s = 0; s < 2; ++s) {
+  if (matrix) HOST_CUDA(cudaMemcpyAsync(res->matrix, ex.matrix, mat_n * 4, cudaMemcpyDeviceToHost, st));
+  for (int s = 0; s < 2 && !matrix; ++s) {
     if (s == 1 && !want_b) continue;
-    if (max_only) {
-      HOST_CUDA(cudaMemcpyAsync(hmax[s], dmax[s], nsz[s] * 4, cudaMemcpyDeviceToHost, st));
+    if (knn) {
+      HOST_CUDA(cudaMemcpyAsync(hknn[s], ex.knn[s], nsz[s] * kk * 8, cudaMemcpyDeviceToHost, st));
+    } else if (max_only) {
+      HOST_CUDA(cudaMemcpyAsync(hmax[s], ex.max[s], nsz[s] * 4, cudaMemcpyDeviceToHost, st));
       if (hcorr[s]) HOST_CUDA(cudaMemcpyAsync(hcorr[s], dcorr[s], nsz[s] * 8, cudaMemcpyDeviceToHost, st));
     } else if (is_1nn) {
       HOST_CUDA(cudaMemcpyAsync(hprof[s], dprof[s], nsz[s] * 8, cudaMemcpyDeviceToHost, st));
@@ -1010,7 +1121,7 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
     *msg = "Error: the no-allocation join runs the FP64 form only (precision double or ultra)";
     return SCAMP_ERR_INVALID_ARGS;
   }
-  if (a->profile_type == SCAMP_PROFILE_1NN) {
+  if (a->profile_type != SCAMP_PROFILE_1NN_INDEX && a->profile_type != SCAMP_PROFILE_SUM_THRESH) {
     *msg = "Error: the no-allocation join serves 1NN_INDEX and SUM_THRESH";
     return SCAMP_ERR_INVALID_ARGS;
   }

@@ -155,6 +155,18 @@ struct JoinParams {
   float anchor_vcoef;               // initial drift estimate of an anchor / cov^2
 };
 
+// Outputs of the two experimental profile types (join_visit.cu).
+struct VisitArgs {
+  int mode;                        // 0: k best matches per window, 1: matrix summary
+  unsigned long long* topk[2];     // k keys per window of A / B, largest first
+  int k;
+  unsigned* mat;                   // matrix entries (ordered images of floats)
+  int64_t mat_w;
+  int64_t rows_per_cell, cols_per_cell;
+  int col_target[kMaxProblems];    // 0 = A, 1 = B, -1 = none, per problem
+  int row_target[kMaxProblems];
+};
+
 // Locates global band `g` and unit-within-band for unit index `u`.
 __device__ __forceinline__ void decode_unit(const JoinParams& P, int64_t u,
                                             int* prob, int64_t* band,
@@ -226,6 +238,11 @@ __global__ void combined_stats_kernel(const double* __restrict__ T, int64_t n, i
                                       const double* __restrict__ mean, int role_b,
                                       double* __restrict__ df, double* __restrict__ dg);
 __global__ void join_fp64_kernel(JoinParams P);
+__global__ void join_visit_kernel(JoinParams P, VisitArgs V);
+__global__ void floats_to_ord_kernel(const float* __restrict__ in, unsigned* __restrict__ out,
+                                     int64_t n);
+__global__ void ord_to_floats_kernel(const unsigned* __restrict__ in, float* __restrict__ out,
+                                     int64_t n);
 __global__ void join_mixed_1nn_kernel(JoinParams P);  // mixed 1NN_INDEX
 __global__ void join_mixed_sum_kernel(JoinParams P);  // mixed SUM_THRESH
 __global__ void verify_requests_kernel(JoinParams P);

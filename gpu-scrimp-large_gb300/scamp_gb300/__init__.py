@@ -18,7 +18,8 @@ from . import _lib
 from ._lib import SCAMPError
 
 __all__ = [
-    "selfjoin", "abjoin", "selfjoin_sum", "abjoin_sum", "gpu_supported",
+    "selfjoin", "abjoin", "selfjoin_sum", "abjoin_sum", "selfjoin_knn", "abjoin_knn",
+    "selfjoin_matrix", "abjoin_matrix", "gpu_supported",
     "join", "join_device", "SCAMPError", "count_cells", "pipe_peak",
     "unpack_profile", "to_distance", "version",
 ]
@@ -30,7 +31,9 @@ _PRECISION = {
     "ultra": _lib.PRECISION_ULTRA,
 }
 _PROFILE = {"1NN_INDEX": _lib.PROFILE_1NN_INDEX, "SUM_THRESH": _lib.PROFILE_SUM_THRESH,
-            "1NN": _lib.PROFILE_1NN}
+            "1NN": _lib.PROFILE_1NN, "ALL_NEIGHBORS": _lib.PROFILE_APPROX_ALL_NEIGHBORS,
+            "APPROX_ALL_NEIGHBORS": _lib.PROFILE_APPROX_ALL_NEIGHBORS,
+            "MATRIX_SUMMARY": _lib.PROFILE_MATRIX_SUMMARY}
 
 # 1NN_INDEX "no match" entry {corr = -2.0f, index = 0xFFFFFFFF}
 # (src/common.cpp:294-299).
@@ -52,7 +55,7 @@ def gpu_supported():
 
 def _args(a, b, m, profile, precision, computing_rows, computing_cols,
           keep_rows, aligned, threshold, start_row, start_col, max_tile_size,
-          anchor_interval, device, silent):
+          anchor_interval, device, silent, max_matches=5, matrix_height=50, matrix_width=50):
     ca = _lib.CArgs()
     ca.timeseries_a = a.ctypes.data if a is not None else None
     ca.len_a = len(a) if a is not None else 0
@@ -73,6 +76,9 @@ def _args(a, b, m, profile, precision, computing_rows, computing_cols,
     ca.silent_mode = int(bool(silent))
     ca.anchor_interval = int(anchor_interval)
     ca.device = int(device)
+    ca.max_matches_per_column = int(max_matches)
+    ca.matrix_height = int(matrix_height)
+    ca.matrix_width = int(matrix_width)
     return ca
 
 
@@ -113,7 +119,8 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
          computing_rows=True, computing_cols=True, keep_rows=False,
          aligned=False, threshold=0.0, start_row=-1, start_col=-1,
          max_tile_size=128000, anchor_interval=0, device=0, profile_a=None,
-         profile_b=None, return_corr=False, silent=True, inplace=False):
+         profile_b=None, return_corr=False, silent=True, inplace=False, max_matches=5,
+         matrix_height=50, matrix_width=50):
     """Run one join (the C ABI's scamp_gb300_join, host buffers).
 
     For 1NN_INDEX returns ``profile_a`` (and ``profile_b`` with keep_rows) as
@@ -121,7 +128,12 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
     ``profile_b`` given on input are merged into, like a best-so-far profile
     passed to do_SCAMP.  For 1NN (the reference's PROFILE_TYPE_1NN) they are
     float32 arrays of the best correlation, -2 where there is none.  For
-    SUM_THRESH returns ``sum_a`` / ``sum_b``.
+    SUM_THRESH returns ``sum_a`` / ``sum_b``.  For ALL_NEIGHBORS returns
+    ``knn_a`` (and ``knn_b``): ``max_matches`` packed entries per window,
+    best first, -2 / index 0xFFFFFFFF where unused.  For MATRIX_SUMMARY
+    returns ``matrix``, a (matrix_height, matrix_width) float32 array of the
+    largest correlation per grid cell (-2 where none); ``profile_a`` given
+    on input is the initial matrix.
     ``corr_a`` / ``corr_b`` (double correlations) when return_corr.
     With ``inplace`` the given profile arrays (contiguous uint64 / float64)
     are updated directly instead of copied (e.g. pinned host buffers).
@@ -134,7 +146,8 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
         raise ValueError("window m is required")
     ca = _args(a, b, m, profile, precision, computing_rows, computing_cols,
                keep_rows, aligned, threshold, start_row, start_col,
-               max_tile_size, anchor_interval, device, silent)
+               max_tile_size, anchor_interval, device, silent, max_matches,
+               matrix_height, matrix_width)
     err = ctypes.create_string_buffer(1024)
     rc = lib.scamp_gb300_validate(ctypes.byref(ca), err, 1024)
     _check(rc, err)
@@ -154,7 +167,21 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
             return given
         return np.array(given, dtype=dtype, copy=True)
 
-    if is_1nn or max_only:
+    if ca.profile_type == _lib.PROFILE_APPROX_ALL_NEIGHBORS:
+        k = int(max_matches)
+        ka = _buf(profile_a, nsa * k, np.uint64, NO_MATCH)
+        out["knn_a"] = ka
+        res.knn_a = ka.ctypes.data
+        if keep_rows:
+            kb = _buf(profile_b, nsb * k, np.uint64, NO_MATCH)
+            out["knn_b"] = kb
+            res.knn_b = kb.ctypes.data
+    elif ca.profile_type == _lib.PROFILE_MATRIX_SUMMARY:
+        mat = _buf(None if profile_a is None else np.asarray(profile_a).ravel(),
+                   int(matrix_height) * int(matrix_width), np.float32, np.float32(-2.0))
+        out["matrix"] = mat.reshape(int(matrix_height), int(matrix_width))
+        res.matrix = mat.ctypes.data
+    elif is_1nn or max_only:
         dt, fill = (np.float32, np.float32(-2.0)) if max_only else (np.uint64, NO_MATCH)
         pa = _buf(profile_a, nsa, dt, fill)
         out["profile_a"] = pa
@@ -335,6 +362,90 @@ def _parse_kwargs(kwargs, allowed):
                                  "greater than or equal to 0.")
             # Accepted for compatibility; this engine has no CPU workers.
     return opts
+
+
+_KNN_KEYS = _SUM_KEYS
+_MATRIX_KEYS = _SUM_KEYS | {"mheight", "mwidth"}
+
+
+def _convert(corr, pearson, m):
+    """CleanupPearson / ConvertToEuclidean (src/scamp_utils.cpp:127-141):
+    NaN where there is no match."""
+    corr = np.asarray(corr, dtype=np.float64)
+    if pearson:
+        v = corr.copy()
+    else:
+        with np.errstate(invalid="ignore"):
+            v = np.sqrt(np.maximum(2.0 * m * (1.0 - corr), 0.0))
+    v[corr < -1] = np.nan
+    return v
+
+
+def _split_knn(entries, k, pearson, m):
+    """SplitProfileKNN (python/SCAMP_python.cpp:31-49): one (column, row,
+    value) tuple per match, columns in order, each column's matches from
+    the lowest correlation up."""
+    e = np.asarray(entries, dtype=np.uint64).reshape(-1, k)[:, ::-1]
+    corr, idx = unpack_profile(e.ravel())
+    cols = np.repeat(np.arange(e.shape[0], dtype=np.int64), k)
+    ok = idx >= 0
+    vals = _convert(corr[ok], pearson, m).astype(np.float32)
+    return list(zip(cols[ok].tolist(), idx[ok].tolist(), vals.tolist()))
+
+
+def _parse_matrix_kwargs(kwargs):
+    o = _parse_kwargs({k: v for k, v in kwargs.items() if k not in ("mheight", "mwidth")},
+                      _MATRIX_KEYS)
+    for k, name in (("mheight", "height"), ("mwidth", "width")):
+        v = int(kwargs.get(k, 50))
+        if v <= 0:
+            raise ValueError("Invalid matrix %s specified: value must be greater than 0" % name)
+        o[k] = v
+    return o
+
+
+def selfjoin_knn(a, m, k, **kwargs):
+    """The ``k`` best matches above ``threshold`` (default 0) of every window
+    of ``a``: a list of (column, row, value) tuples (pyscamp.selfjoin_knn).
+    These are the exact k best; the reference's lists are approximate."""
+    o = _parse_kwargs(kwargs, _KNN_KEYS)
+    r = join(np.asarray(a, dtype=np.float64), None, int(m), "ALL_NEIGHBORS", o["precision"],
+             computing_rows=True, computing_cols=True, threshold=o["threshold"],
+             silent=o["silent"], device=o["device"], max_matches=int(k))
+    return _split_knn(r["knn_a"], int(k), o["pearson"], int(m))
+
+
+def abjoin_knn(a, b, m, k, **kwargs):
+    """For every window of ``a``, its ``k`` best matches in ``b`` above
+    ``threshold`` (pyscamp.abjoin_knn)."""
+    o = _parse_kwargs(kwargs, _KNN_KEYS)
+    r = join(np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64), int(m),
+             "ALL_NEIGHBORS", o["precision"], computing_rows=False, computing_cols=True,
+             threshold=o["threshold"], silent=o["silent"], device=o["device"],
+             max_matches=int(k))
+    return _split_knn(r["knn_a"], int(k), o["pearson"], int(m))
+
+
+def selfjoin_matrix(a, m, **kwargs):
+    """An (mheight, mwidth) summary of the self-join's distance matrix, each
+    entry the best match above ``threshold`` in its block (pyscamp
+    .selfjoin_matrix); distances, or correlations with pearson=True."""
+    o = _parse_matrix_kwargs(kwargs)
+    r = join(np.asarray(a, dtype=np.float64), None, int(m), "MATRIX_SUMMARY", o["precision"],
+             threshold=o["threshold"], silent=o["silent"], device=o["device"],
+             matrix_height=o["mheight"], matrix_width=o["mwidth"])
+    return _convert(r["matrix"], o["pearson"], int(m)).astype(np.float32)
+
+
+def abjoin_matrix(a, b, m, **kwargs):
+    """An (mheight, mwidth) summary of the AB-join's distance matrix (rows:
+    windows of b, columns: windows of a) (pyscamp.abjoin_matrix)."""
+    o = _parse_matrix_kwargs(kwargs)
+    r = join(np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64), int(m),
+             "MATRIX_SUMMARY", o["precision"], computing_rows=False, computing_cols=True,
+             threshold=o["threshold"], silent=o["silent"], device=o["device"],
+             matrix_height=o["mheight"], matrix_width=o["mwidth"])
+    return _convert(r["matrix"], o["pearson"], int(m)).astype(np.float32)
 
 
 def _split_1nn(packed, pearson, m):

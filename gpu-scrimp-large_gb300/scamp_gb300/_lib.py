@@ -13,6 +13,8 @@ LIB_PATH = os.path.join(PKG_DIR, "libscamp_gb300.so")
 PROFILE_1NN_INDEX = 1
 PROFILE_SUM_THRESH = 2
 PROFILE_1NN = 6
+PROFILE_APPROX_ALL_NEIGHBORS = 7
+PROFILE_MATRIX_SUMMARY = 8
 PRECISION_SINGLE = 1
 PRECISION_MIXED = 2
 PRECISION_DOUBLE = 3
@@ -68,7 +70,10 @@ class CArgs(ctypes.Structure):
         ("silent_mode", ctypes.c_int32),
         ("anchor_interval", ctypes.c_int32),
         ("device", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("max_matches_per_column", ctypes.c_int32),
+        ("matrix_height", ctypes.c_int32),
+        ("matrix_width", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 3),
     ]
 
 
@@ -92,6 +97,9 @@ class CResult(ctypes.Structure):
         ("verify_kernel_ms", ctypes.c_double),
         ("max_a", ctypes.c_void_p),
         ("max_b", ctypes.c_void_p),
+        ("knn_a", ctypes.c_void_p),
+        ("knn_b", ctypes.c_void_p),
+        ("matrix", ctypes.c_void_p),
     ]
 
 

@@ -11,12 +11,14 @@ the row profile goes to --output_b_file_name / --output_b_index_file_name.
 Values are z-normalised Euclidean distances (or Pearson correlations with
 --output_pearson), 10 significant digits; unmatched entries are "nan" with
 index -1.  --profile_type=1NN writes the distances only (no index file),
-SUM_THRESH the per-window sums.  Exit status 1 with the
+SUM_THRESH the per-window sums, ALL_NEIGHBORS "column row value" lines
+(--max_matches_per_column per window), MATRIX_SUMMARY the
+--reduced_height x --reduced_width summary.  Exit status 1 with the
 reference's message for invalid arguments.
 
 Flags of the reference that select other machinery (distributed execution,
-CPU workers, KNN and matrix-summary profiles) are accepted and ignored, except
---no_gpu, which this engine cannot honour (it has no CPU path).
+CPU workers) are accepted and ignored, except --no_gpu, which this engine
+cannot honour (it has no CPU path).
 """
 import math
 import sys
@@ -47,11 +49,11 @@ _FLAGS = {
     "gpus": ("str", ""),
     "print_debug_info": ("bool", False),
     "no_gpu": ("bool", False),
-    # accepted, no effect here
-    "num_cpu_workers": ("int", 0),
     "max_matches_per_column": ("int", 5),
     "reduced_height": ("int", 50),
     "reduced_width": ("int", 50),
+    # accepted, no effect here
+    "num_cpu_workers": ("int", 0),
     "distributed_tile_size": ("int", 4000000),
     "hostname_port": ("str", "localhost:30078"),
 }
@@ -170,6 +172,40 @@ def write_max_profile(path_mp, corr, pearson, window):
         f.write("".join(_fmt(v) + "\n" for v in vals.tolist()))
 
 
+def _values(corr, pearson, window):
+    corr = np.asarray(corr).astype(np.float64)
+    if pearson:
+        vals = corr.copy()
+    else:
+        with np.errstate(invalid="ignore"):
+            vals = np.sqrt(np.maximum(2.0 * window * (1.0 - corr), 0.0))
+    vals[corr < -1] = np.nan
+    return vals
+
+
+def write_knn(path, entries, k, pearson, window):
+    """WriteProfileToFile for ALL_NEIGHBORS (src/scamp_utils.cpp:193-212): one
+    "column row value" line per match, columns in order, best match first."""
+    from . import unpack_profile
+
+    corr, idx = unpack_profile(np.asarray(entries))
+    vals = _values(corr, pearson, window)
+    cols = np.repeat(np.arange(len(idx) // k), k)
+    ok = idx >= 0
+    with open(path, "w") as f:
+        f.write("".join("%d %d %s\n" % (c, i, _fmt(v))
+                        for c, i, v in zip(cols[ok].tolist(), idx[ok].tolist(),
+                                           vals[ok].tolist())))
+
+
+def write_matrix(path, matrix, pearson, window):
+    """write_matrix (src/scamp_utils.cpp:9-28): the summary row by row, each
+    value followed by a space."""
+    vals = _values(np.asarray(matrix), pearson, window)
+    with open(path, "w") as f:
+        f.write("".join("".join(_fmt(v) + " " for v in row) + "\n" for row in vals.tolist()))
+
+
 def write_sums(path, sums):
     with open(path, "w") as f:
         f.write("".join(_fmt(v) + "\n" for v in np.asarray(sums, dtype=np.float64).tolist()))
@@ -197,7 +233,8 @@ def run(argv):
                          "--input_a_file_name")
     if fl["no_gpu"]:
         raise UsageError("Error: this engine runs on the GPU only (--no_gpu is not supported)")
-    if fl["profile_type"] not in ("1NN_INDEX", "SUM_THRESH", "1NN"):
+    if fl["profile_type"] not in ("1NN_INDEX", "SUM_THRESH", "1NN", "ALL_NEIGHBORS",
+                                  "MATRIX_SUMMARY"):
         raise UsageError("Error: profile type %s is not supported by this engine"
                          % fl["profile_type"])
     self_join = not fl["input_b_file_name"]
@@ -213,13 +250,21 @@ def run(argv):
         computing_rows=True if self_join else keep, keep_rows=keep, aligned=fl["aligned"],
         threshold=fl["threshold"], start_row=fl["global_row"], start_col=fl["global_col"],
         max_tile_size=fl["max_tile_size"], device=devices[0],
-        silent=not fl["print_debug_info"])
+        silent=not fl["print_debug_info"], max_matches=fl["max_matches_per_column"],
+        matrix_height=fl["reduced_height"], matrix_width=fl["reduced_width"])
     if fl["profile_type"] == "1NN_INDEX":
         write_profile(fl["output_a_file_name"], fl["output_a_index_file_name"], r["profile_a"],
                       fl["output_pearson"], m)
         if keep:
             write_profile(fl["output_b_file_name"], fl["output_b_index_file_name"],
                           r["profile_b"], fl["output_pearson"], m)
+    elif fl["profile_type"] == "ALL_NEIGHBORS":
+        k = fl["max_matches_per_column"]
+        write_knn(fl["output_a_file_name"], r["knn_a"], k, fl["output_pearson"], m)
+        if keep:
+            write_knn(fl["output_b_file_name"], r["knn_b"], k, fl["output_pearson"], m)
+    elif fl["profile_type"] == "MATRIX_SUMMARY":
+        write_matrix(fl["output_a_file_name"], r["matrix"], fl["output_pearson"], m)
     elif fl["profile_type"] == "1NN":
         write_max_profile(fl["output_a_file_name"], r["profile_a"], fl["output_pearson"], m)
         if keep:

@@ -41,6 +41,8 @@ enum SCAMPProfileType {
   PROFILE_TYPE_1NN_INDEX = SCAMP_PROFILE_1NN_INDEX,
   PROFILE_TYPE_SUM_THRESH = SCAMP_PROFILE_SUM_THRESH,
   PROFILE_TYPE_1NN = SCAMP_PROFILE_1NN,
+  PROFILE_TYPE_APPROX_ALL_NEIGHBORS = SCAMP_PROFILE_APPROX_ALL_NEIGHBORS,
+  PROFILE_TYPE_MATRIX_SUMMARY = SCAMP_PROFILE_MATRIX_SUMMARY,
 };
 
 enum SCAMPPrecisionType {
@@ -52,9 +54,11 @@ enum SCAMPPrecisionType {
 };
 
 struct ProfileData {
-  std::vector<uint64_t> uint64_value;  // 1NN_INDEX: low word float r, high word index
+  // 1NN_INDEX: low word float r, high word index; APPROX_ALL_NEIGHBORS:
+  // max_matches_per_column such entries per window, best first
+  std::vector<uint64_t> uint64_value;
   std::vector<double> double_value;    // SUM_THRESH
-  std::vector<float> float_value;      // 1NN: best correlation
+  std::vector<float> float_value;      // 1NN: best correlation; MATRIX_SUMMARY: the grid
 };
 
 struct Profile {
@@ -62,10 +66,11 @@ struct Profile {
   Profile(SCAMPProfileType t, size_t size) : type(t) { Alloc(size); }
 
   // Best-so-far initial values: {r = -2.0f, index = 0xFFFFFFFF} per 1NN_INDEX
-  // entry, -2.0f per 1NN entry, 0 per SUM_THRESH entry.
+  // (and APPROX_ALL_NEIGHBORS) entry, -2.0f per 1NN (and MATRIX_SUMMARY)
+  // entry, 0 per SUM_THRESH entry.  `size` counts entries.
   void Alloc(size_t size) {
     data.assign(1, ProfileData());
-    if (type == PROFILE_TYPE_1NN_INDEX) {
+    if (type == PROFILE_TYPE_1NN_INDEX || type == PROFILE_TYPE_APPROX_ALL_NEIGHBORS) {
       const float minus_two = -2.0f;
       uint32_t bits;
       static_assert(sizeof bits == sizeof minus_two, "float is 32 bits");
@@ -73,7 +78,7 @@ struct Profile {
       data[0].uint64_value.assign(size, (uint64_t{0xFFFFFFFFu} << 32) | bits);
     } else if (type == PROFILE_TYPE_SUM_THRESH) {
       data[0].double_value.assign(size, 0.0);
-    } else if (type == PROFILE_TYPE_1NN) {
+    } else if (type == PROFILE_TYPE_1NN || type == PROFILE_TYPE_MATRIX_SUMMARY) {
       data[0].float_value.assign(size, -2.0f);
     }
   }
@@ -100,6 +105,9 @@ struct SCAMPArgs {
   bool keep_rows_separate = false;
   bool is_aligned = false;
   bool silent_mode = true;
+  int64_t max_matches_per_column = 5;  // APPROX_ALL_NEIGHBORS
+  int64_t matrix_height = 50;          // MATRIX_SUMMARY
+  int64_t matrix_width = 50;
 };
 
 namespace detail {
@@ -123,6 +131,9 @@ inline scamp_c_args to_c(const SCAMPArgs& a) {
   c.keep_rows_separate = a.keep_rows_separate ? 1 : 0;
   c.is_aligned = a.is_aligned ? 1 : 0;
   c.silent_mode = a.silent_mode ? 1 : 0;
+  c.max_matches_per_column = static_cast<int32_t>(a.max_matches_per_column);
+  c.matrix_height = static_cast<int32_t>(a.matrix_height);
+  c.matrix_width = static_cast<int32_t>(a.matrix_width);
   return c;
 }
 
@@ -141,8 +152,16 @@ inline bool InitProfileMemory(SCAMPArgs* args) {
                          ? static_cast<int64_t>(args->timeseries_b.size()) - static_cast<int64_t>(args->window) + 1
                          : na;
   if (na <= 0 || (args->keep_rows_separate && nb <= 0)) return false;
-  args->profile_a = Profile(args->profile_type, static_cast<size_t>(na));
-  if (args->keep_rows_separate) args->profile_b = Profile(args->profile_type, static_cast<size_t>(nb));
+  int64_t per = 1;
+  if (args->profile_type == PROFILE_TYPE_APPROX_ALL_NEIGHBORS) per = args->max_matches_per_column;
+  if (args->profile_type == PROFILE_TYPE_MATRIX_SUMMARY) {
+    args->profile_a = Profile(args->profile_type,
+                              static_cast<size_t>(args->matrix_height * args->matrix_width));
+    return true;
+  }
+  args->profile_a = Profile(args->profile_type, static_cast<size_t>(na * per));
+  if (args->keep_rows_separate)
+    args->profile_b = Profile(args->profile_type, static_cast<size_t>(nb * per));
   return true;
 }
 
@@ -156,10 +175,15 @@ inline void do_SCAMP(SCAMPArgs* args, const std::vector<int>& devices, int num_t
   scamp_c_args c = detail::to_c(*args);
   c.device = devices.empty() ? 0 : devices[0];
   detail::check(scamp_gb300_validate(&c, msg, sizeof msg), msg);
-  const bool nn = args->profile_type == PROFILE_TYPE_1NN_INDEX;
-  const bool nn_max = args->profile_type == PROFILE_TYPE_1NN;
-  const size_t na = args->timeseries_a.size() - args->window + 1;
-  const size_t nb = args->has_b ? args->timeseries_b.size() - args->window + 1 : na;
+  const bool knn = args->profile_type == PROFILE_TYPE_APPROX_ALL_NEIGHBORS;
+  const bool mat = args->profile_type == PROFILE_TYPE_MATRIX_SUMMARY;
+  const bool nn = args->profile_type == PROFILE_TYPE_1NN_INDEX || knn;
+  const bool nn_max = args->profile_type == PROFILE_TYPE_1NN || mat;
+  const size_t per = knn ? static_cast<size_t>(args->max_matches_per_column) : 1;
+  const size_t na = mat ? static_cast<size_t>(args->matrix_height * args->matrix_width)
+                        : (args->timeseries_a.size() - args->window + 1) * per;
+  const size_t nb = (args->has_b ? args->timeseries_b.size() - args->window + 1
+                                 : args->timeseries_a.size() - args->window + 1) * per;
   auto sized = [&](Profile& p, size_t n) {
     if (p.type != args->profile_type || p.data.empty() ||
         (nn ? p.data[0].uint64_value.size()
@@ -167,9 +191,14 @@ inline void do_SCAMP(SCAMPArgs* args, const std::vector<int>& devices, int num_t
       throw SCAMPException("Error: profile memory not initialised (call InitProfileMemory)");
   };
   sized(args->profile_a, na);
-  if (args->keep_rows_separate) sized(args->profile_b, nb);
+  if (args->keep_rows_separate && !mat) sized(args->profile_b, nb);
   scamp_c_result r{};
-  if (nn) {
+  if (knn) {
+    r.knn_a = args->profile_a.data[0].uint64_value.data();
+    if (args->keep_rows_separate) r.knn_b = args->profile_b.data[0].uint64_value.data();
+  } else if (mat) {
+    r.matrix = args->profile_a.data[0].float_value.data();
+  } else if (nn) {
     r.profile_a = args->profile_a.data[0].uint64_value.data();
     if (args->keep_rows_separate) r.profile_b = args->profile_b.data[0].uint64_value.data();
   } else if (nn_max) {

@@ -30,6 +30,8 @@ enum {
   SCAMP_PROFILE_1NN_INDEX = 1,
   SCAMP_PROFILE_SUM_THRESH = 2,
   SCAMP_PROFILE_1NN = 6, /* best correlation only, float32 (no index) */
+  SCAMP_PROFILE_APPROX_ALL_NEIGHBORS = 7, /* k best matches per window */
+  SCAMP_PROFILE_MATRIX_SUMMARY = 8,       /* max correlation per grid cell */
 };
 enum {
   SCAMP_PRECISION_SINGLE = 1,
@@ -74,7 +76,13 @@ typedef struct scamp_c_args {
   /* Tuning overrides, 0 = automatic. */
   int32_t anchor_interval;    /* mixed: rows between FP64-centred re-anchors */
   int32_t device;             /* CUDA device ordinal */
-  int32_t reserved[6];
+  /* APPROX_ALL_NEIGHBORS: matches kept per window (the reference's
+   * max_matches_per_column); MATRIX_SUMMARY: grid height (windows of B) and
+   * width (windows of A), the reference's matrix_height / matrix_width. */
+  int32_t max_matches_per_column;
+  int32_t matrix_height;
+  int32_t matrix_width;
+  int32_t reserved[3];
 } scamp_c_args;
 
 /* Results.  Profiles are in/out: on entry they hold the best-so-far values
@@ -110,6 +118,19 @@ typedef struct scamp_c_result {
    * in/out like profile_a / profile_b. */
   float *max_a;
   float *max_b;
+  /* APPROX_ALL_NEIGHBORS: max_matches_per_column entries per window in the
+   * 1NN_INDEX layout (correlation, index of the match), best first, unused
+   * entries {-2.0f, 0xFFFFFFFF}; in/out, entries given on input must be in
+   * that order.  Every match has r > distance_threshold, and these are the
+   * exact best matches (the reference's approximate lists may miss some). */
+  uint64_t *knn_a;
+  uint64_t *knn_b;
+  /* MATRIX_SUMMARY: matrix_height x matrix_width floats, row-major; entry
+   * (y, x) is the largest r > distance_threshold over the cells whose B window
+   * (A window in a self-join) falls in row block y and A window in column
+   * block x (blocks of ceil(windows / height or width)), -2.0f where none;
+   * in/out (merged by max).  Columns only, as in the reference. */
+  float *matrix;
 } scamp_c_result;
 
 /* Runs one join.  Inputs and results are HOST memory; the engine copies them

@@ -124,3 +124,32 @@ def test_cli_profile_type_1nn(gpu_engine, tmp_path):
     r = gpu_engine.join(a, None, 50, "1NN_INDEX", "double")
     c, _ = gpu_engine.unpack_profile(r["profile_a"])
     assert np.max(np.abs(got - c.astype(np.float64))) < 1e-8
+
+
+@pytest.mark.gpu
+def test_cli_all_neighbors_and_matrix(gpu_engine, tmp_path):
+    rng = np.random.default_rng(7)
+    a = np.cumsum(rng.standard_normal(2000))
+    fa = tmp_path / "a.txt"
+    fa.write_text("".join(repr(float(v)) + "\n" for v in a))
+    kf, mf = tmp_path / "knn", tmp_path / "mat"
+    assert cli.main(["--window=32", "--input_a_file_name=%s" % fa,
+                     "--profile_type=ALL_NEIGHBORS", "--max_matches_per_column=3",
+                     "--output_pearson", "--output_a_file_name=%s" % kf]) == 0
+    r = gpu_engine.join(a, None, 32, "ALL_NEIGHBORS", "double", max_matches=3)
+    corr, idx = gpu_engine.unpack_profile(r["knn_a"])
+    lines = [l.split() for l in kf.read_text().splitlines()]
+    assert len(lines) == int(np.sum(idx >= 0))
+    ok = np.nonzero(idx >= 0)[0]
+    for (c, i, v), e in zip(lines[:50], ok[:50]):
+        assert int(c) == e // 3 and int(i) == idx[e] and abs(float(v) - corr[e]) < 1e-6
+    assert cli.main(["--window=32", "--input_a_file_name=%s" % fa,
+                     "--profile_type=MATRIX_SUMMARY", "--reduced_height=4", "--reduced_width=6",
+                     "--output_pearson", "--output_a_file_name=%s" % mf]) == 0
+    r = gpu_engine.join(a, None, 32, "MATRIX_SUMMARY", "double", matrix_height=4,
+                        matrix_width=6)
+    rows = [[float(v) for v in l.split()] for l in mf.read_text().splitlines()]
+    got = np.array(rows)
+    assert got.shape == (4, 6)
+    want = np.where(r["matrix"] < -1, np.nan, r["matrix"])
+    np.testing.assert_allclose(got, want, atol=1e-6)

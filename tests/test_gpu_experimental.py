@@ -1,0 +1,141 @@
+"""The reference's experimental profile types, APPROX_ALL_NEIGHBORS (pyscamp
+selfjoin_knn / abjoin_knn) and MATRIX_SUMMARY (selfjoin_matrix /
+abjoin_matrix), against brute-force correlation matrices.  The engine
+computes them exactly (the reference approximates both), so every reported
+value must equal the brute-force one within float32 rounding, and the k best
+per window must be the true k best up to near-ties."""
+import numpy as np
+import pytest
+
+from parity import window_stats
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6  # float32 rounding of an FP64 correlation
+
+
+def corr_matrix(rows, cols, m):
+    """C[i, j]: r of row window i (of `rows`) and column window j."""
+    Tr, mur, invr = window_stats(rows, m)
+    Tc, muc, invc = window_stats(cols, m)
+    Wr = np.lib.stride_tricks.sliding_window_view(Tr, m)[: len(mur)] - mur[:, None]
+    Wc = np.lib.stride_tricks.sliding_window_view(Tc, m)[: len(muc)] - muc[:, None]
+    return (Wr @ Wc.T) * invr[:, None] * invc[None, :]
+
+
+def rw(rng, n):
+    return np.cumsum(rng.standard_normal(n))
+
+
+def check_knn(gpu_engine, entries, k, C, thr, name):
+    """entries: k packed entries per column window; C[:, j]: that column's
+    candidates (NaN where excluded)."""
+    corr, idx = gpu_engine.unpack_profile(np.asarray(entries))
+    corr = corr.reshape(-1, k).astype(np.float64)
+    idx = idx.reshape(-1, k)
+    ns = C.shape[1]
+    assert corr.shape[0] == ns
+    for j in range(ns):
+        col = C[:, j]
+        cand = np.nonzero(col > thr)[0]
+        order = cand[np.lexsort((cand, -col[cand]))][:k]
+        want = col[order]
+        got_ok = idx[j] >= 0
+        assert got_ok.sum() == len(order), (name, j)
+        g = corr[j][got_ok]
+        # best first, values equal to the true k best (ties may swap indices)
+        assert np.all(np.diff(g) <= TOL), (name, j)
+        assert np.max(np.abs(g - want), initial=0.0) <= TOL, (name, j, g, want)
+        # every reported match is the cell it names
+        assert np.max(np.abs(col[idx[j][got_ok]] - g), initial=0.0) <= TOL, (name, j)
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_knn_selfjoin(gpu_engine, precision):
+    rng = np.random.default_rng(61)
+    a = rw(rng, 2500)
+    m, k = 50, 4
+    r = gpu_engine.join(a, None, m, "ALL_NEIGHBORS", precision, threshold=0.3, max_matches=k)
+    C = corr_matrix(a, a, m)
+    ns = C.shape[0]
+    ii, jj = np.indices(C.shape)
+    C[np.abs(ii - jj) < m // 4] = np.nan
+    check_knn(gpu_engine, r["knn_a"], k, C, 0.3, "self")
+    assert ns == len(a) - m + 1
+
+
+def test_knn_abjoin_and_pyscamp_surface(gpu_engine):
+    rng = np.random.default_rng(62)
+    a, b = rw(rng, 2200), rw(rng, 1700)
+    m, k = 40, 3
+    r = gpu_engine.join(a, b, m, "ALL_NEIGHBORS", "double", computing_rows=False,
+                        max_matches=k)
+    C = corr_matrix(b, a, m)  # rows: windows of b, columns: windows of a
+    check_knn(gpu_engine, r["knn_a"], k, C, 0.0, "ab")
+    # pyscamp.abjoin_knn: (column, row, value) tuples, per column from the
+    # lowest correlation up; pearson values are the correlations
+    tup = gpu_engine.abjoin_knn(a, b, m, k, pearson=True)
+    assert len(tup) == int(np.sum(gpu_engine.unpack_profile(r["knn_a"])[1] >= 0))
+    cols = np.array([t[0] for t in tup])
+    assert np.all(np.diff(cols) >= 0)
+    for c, row, v in tup[:200]:
+        assert abs(C[row, c] - v) <= TOL
+    dist = gpu_engine.abjoin_knn(a, b, m, k)
+    c, row, v = dist[0]
+    assert abs(v - np.sqrt(max(2 * m * (1 - C[row, c]), 0))) < 1e-3
+
+
+def check_matrix(mat, C, h, w, thr):
+    rpc = -(-C.shape[0] // h)
+    cpc = -(-C.shape[1] // w)
+    want = np.full((h, w), -2.0)
+    for y in range(h):
+        for x in range(w):
+            blk = C[y * rpc:(y + 1) * rpc, x * cpc:(x + 1) * cpc]
+            v = blk[blk > thr]
+            if v.size:
+                want[y, x] = v.max()
+    assert np.array_equal(mat < -1, want < -1)
+    ok = want >= -1
+    assert np.max(np.abs(mat[ok] - want[ok]), initial=0.0) <= TOL
+
+
+@pytest.mark.parametrize("precision", ["double", "mixed"])
+def test_matrix_summary(gpu_engine, precision):
+    rng = np.random.default_rng(63)
+    a, b = rw(rng, 3000), rw(rng, 2000)
+    m = 64
+    # self-join: columns only, so the cells with j - i >= m/4 (upper triangle)
+    r = gpu_engine.join(a, None, m, "MATRIX_SUMMARY", precision, threshold=0.2,
+                        matrix_height=20, matrix_width=30)
+    C = corr_matrix(a, a, m)
+    ii, jj = np.indices(C.shape)
+    C[jj - ii < m // 4] = np.nan
+    check_matrix(r["matrix"].astype(np.float64), C, 20, 30, 0.2)
+    # AB-join: every (window of b, window of a) cell
+    r = gpu_engine.join(a, b, m, "MATRIX_SUMMARY", precision, computing_rows=False,
+                        matrix_height=17, matrix_width=23)
+    check_matrix(r["matrix"].astype(np.float64), corr_matrix(b, a, m), 17, 23, 0.0)
+    # pyscamp surface: distances (NaN where none), shape (mheight, mwidth)
+    d = gpu_engine.abjoin_matrix(a, b, m, mheight=17, mwidth=23)
+    assert d.shape == (17, 23)
+    mat = r["matrix"].astype(np.float64)
+    want = np.where(mat < -1, np.nan, np.sqrt(np.maximum(2 * m * (1 - mat), 0)))
+    np.testing.assert_allclose(d, want, rtol=1e-5, atol=1e-4)
+    p = gpu_engine.selfjoin_matrix(a, m, pearson=True, mheight=5, mwidth=5)
+    assert p.shape == (5, 5)
+
+
+def test_matrix_merges_into_given_matrix(gpu_engine):
+    rng = np.random.default_rng(64)
+    a = rw(rng, 1500)
+    init = np.full((4, 4), -2.0, dtype=np.float32)
+    init[0, 3] = 1.0
+    r = gpu_engine.join(a, None, 32, "MATRIX_SUMMARY", "double", profile_a=init,
+                        matrix_height=4, matrix_width=4)
+    plain = gpu_engine.join(a, None, 32, "MATRIX_SUMMARY", "double", matrix_height=4,
+                            matrix_width=4)
+    assert r["matrix"][0, 3] == 1.0
+    mask = np.ones((4, 4), bool)
+    mask[0, 3] = False
+    assert np.array_equal(r["matrix"][mask], plain["matrix"][mask])

@@ -47,6 +47,7 @@ def _args(engine, n=1000, m=10, **kw):
     ("max_tile_size", 1500, "2x larger"),
     ("len_a", 5, "subesequence window size"),
     ("profile_type", 4, "not supported"),
+    ("profile_type", 5, "not supported"),
     ("precision_type", 9, "precision"),
 ])
 def test_validate_rejects(engine, field, value, msg):
@@ -61,9 +62,16 @@ def test_validate_rejects(engine, field, value, msg):
 def test_validate_accepts(engine):
     ca, _keep = _args(engine)
     assert engine._lib.load().scamp_gb300_validate(ctypes.byref(ca), None, 0) == 0
-    for ptype in (1, 2, 6):  # 1NN_INDEX, SUM_THRESH, 1NN
+    for ptype in (1, 2, 6, 7, 8):  # 1NN_INDEX, SUM_THRESH, 1NN, ALL_NEIGHBORS, MATRIX
         ca.profile_type = ptype
+        ca.max_matches_per_column, ca.matrix_height, ca.matrix_width = 5, 50, 50
         assert engine._lib.load().scamp_gb300_validate(ctypes.byref(ca), None, 0) == 0
+    ca.profile_type = 7
+    ca.max_matches_per_column = 0
+    assert engine._lib.load().scamp_gb300_validate(ctypes.byref(ca), None, 0) != 0
+    ca.profile_type = 8
+    ca.matrix_height = 0
+    assert engine._lib.load().scamp_gb300_validate(ctypes.byref(ca), None, 0) != 0
 
 
 @pytest.mark.parametrize("n,m", [(131072, 100), (1000, 3), (5000, 1024), (64, 64)])
@@ -112,6 +120,15 @@ def test_pyscamp_kwargs_validation(engine):
         engine.abjoin(a, a, 10, precision="quad")
     with pytest.raises(ValueError, match="greater than or equal to 0"):
         engine.selfjoin(a, 10, threads=-1)
+    # knn takes the sum keys; matrix adds mheight / mwidth
+    with pytest.raises(ValueError, match="unknown argument: mheight"):
+        engine.selfjoin_knn(a, 10, 3, mheight=5)
+    with pytest.raises(ValueError, match="matrix height"):
+        engine.selfjoin_matrix(a, 10, mheight=0)
+    with pytest.raises(ValueError, match="matrix width"):
+        engine.abjoin_matrix(a, a, 10, mwidth=-1)
+    with pytest.raises(ValueError, match="between -1 and 1"):
+        engine.abjoin_knn(a, a, 10, 2, threshold=-2)
 
 
 def test_join_without_gpu_fails_loudly(engine):
