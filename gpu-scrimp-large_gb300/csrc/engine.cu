@@ -663,6 +663,9 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   P.seg_len = K;
   P.band_width = W;
   P.profile_type = is_1nn ? SCAMP_PROFILE_1NN_INDEX : a->profile_type;
+  // a join without seeds starts cold: the band kernel refreshes its ring
+  // columns' bests every slab (seeded joins start near their final bests)
+  P.refresh_cols = (kind == K_MIXED && is_1nn && !seed_a) ? 1 : 0;
   P.threshold = a->distance_threshold;
   P.kl = kl;
   {
@@ -1378,7 +1381,7 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
                b_murel = sz(4 * Nns), b_keys = sz(8 * Nns), b_prof = sz(8 * Nns),
                b_corr = sz(want_corr ? 8 * Nns : 8), b_jobs = sz(sizeof(StatsJob) * count),
                b_jpre = sz(8 * (count + 1)), b_probs = sz(sizeof(Problem) * count),
-               b_counter = sz(64);
+               b_counter = sz(64), b_wpre = sz(8 * (count + 1));
   // band prefix: sized after the problems are known
   int64_t bands_max = 0;
   for (const auto& b : ser) bands_max += (b.ns + mixed_1nn_band_width() - 1) / mixed_1nn_band_width();
@@ -1408,6 +1411,7 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   Problem* d_probs = reinterpret_cast<Problem*>(take(b_probs));
   unsigned long long* d_counter = reinterpret_cast<unsigned long long*>(take(b_counter));
   int64_t* d_bpre = reinterpret_cast<int64_t*>(take(b_bpre));
+  int64_t* d_wpre = reinterpret_cast<int64_t*>(take(b_wpre));
 
   CUDA_TRY(cudaEventRecord(ws.ev0, st));
   uint32_t launches = 0;
@@ -1503,6 +1507,15 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   if (!probs.empty()) {
     CUDA_TRY(cudaMemcpyAsync(d_probs, probs.data(), sizeof(Problem) * probs.size(),
                              cudaMemcpyHostToDevice, st));
+    // seeds from each series' nearest allowed diagonal (diag_seed_kernel)
+    std::vector<int64_t> wpre(probs.size() + 1, 0);
+    for (size_t p = 0; p < probs.size(); ++p) wpre[p + 1] = wpre[p] + probs[p].R.ns;
+    CUDA_TRY(cudaMemcpyAsync(d_wpre, wpre.data(), 8 * wpre.size(), cudaMemcpyHostToDevice, st));
+    const int64_t seed_blocks =
+        std::min<int64_t>((wpre.back() + 7) / 8, static_cast<int64_t>(ws.sms) * 16);
+    diag_seed_kernel<<<static_cast<unsigned>(std::max<int64_t>(seed_blocks, 1)), 256, 0, st>>>(
+        d_probs, d_wpre, static_cast<int>(probs.size()), kl);
+    ++launches;
     CUDA_TRY(cudaMemcpyAsync(d_bpre, bpre.data(), 8 * bpre.size(), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemsetAsync(d_counter, 0, 64, st));
     JoinParams P{};
@@ -1517,6 +1530,7 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     P.error_flag = reinterpret_cast<int*>(d_counter + 6);
     P.profile_type = SCAMP_PROFILE_1NN_INDEX;
     P.kl = kl;
+    P.refresh_cols = 1;  // batches start cold (diagonal seeds only)
     int64_t want = std::max<int64_t>(kMinVerifyReqs, 32 * Nns);
     want = std::max<int64_t>(want, ws.vreq_seen + ws.vreq_seen / 4);
     want = std::max<int64_t>(std::min<int64_t>(want, kMaxVerifyReqs), ws.vreq_cap);

@@ -153,6 +153,7 @@ struct JoinParams {
   double threshold;
   KeyLayout kl;
   float anchor_vcoef;               // initial drift estimate of an anchor / cov^2
+  int refresh_cols;                 // mixed 1NN: refresh kept ring columns' bests per slab
 };
 
 // Outputs of the two experimental profile types (join_visit.cu).
@@ -265,6 +266,8 @@ __global__ void paa_kernel(const double* __restrict__ T, int64_t n_out, int f,
                            double* __restrict__ out);
 __global__ void fill_floor_kernel(uint64_t* __restrict__ p, int64_t n, float floor);
 __global__ void seed_kernel(SeedArgs S);
+__global__ void diag_seed_kernel(const Problem* __restrict__ probs,
+                                 const int64_t* __restrict__ win_prefix, int nprob, KeyLayout kl);
 
 __global__ void floats_to_keys_kernel(const float* __restrict__ in, uint64_t* __restrict__ keys,
                                       int64_t n, KeyLayout kl);

@@ -698,6 +698,31 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
       // consecutive columns or rows) at a time: per 8-column block and per
       // 8-row step the smallest best, the largest inverse norm and the
       // largest |df|, |dg|.
+      if (!sum_mode && q > 0 && P.refresh_cols && pr.key_col) {
+        // Joins that start cold (no seeds): the columns kept from the last
+        // slab take their bests from the profile keys, which other CTAs
+        // raise quickly at the start; ring columns otherwise keep the bests
+        // staged when they entered.
+#pragma unroll 2
+        for (int c = t; c < kCols - kSlab; c += kThreads) {
+          const int rc = ringc(ring0, c);
+          float2 cb = sm.c_best[rc];
+          if (cb.x != kNoTarget) cb.x = fmaxf(cb.x, key_corr_floor(pr.key_col[cbase_g[0] + c], P.kl));
+          if (cb.y != kNoTarget) cb.y = fmaxf(cb.y, key_corr_floor(pr.key_col[cbase_g[1] + c], P.kl));
+          sm.c_best[rc] = cb;
+          float2 mn = cb;
+#pragma unroll
+          for (int o = 1; o < 8; o <<= 1) {
+            mn.x = fminf(mn.x, __shfl_xor_sync(0xffffffffu, mn.x, o));
+            mn.y = fminf(mn.y, __shfl_xor_sync(0xffffffffu, mn.y, o));
+          }
+          if ((lane & 7) == 0) {
+            const int b = rc >> 3;
+            sm.c_blkmin[b] = mn;
+            if (b == 0) sm.c_blkmin[kBlocks] = mn;
+          }
+        }
+      }
 #pragma unroll 3
       for (int c = (q == 0 ? 0 : kCols - kSlab) + t; c < kCols; c += kThreads) {
         const int rc = ringc(ring0, c);
@@ -1072,6 +1097,41 @@ __global__ void __launch_bounds__(256) seed_kernel(SeedArgs S) {
       const uint64_t q = q_from_float_bits(__float_as_uint((cv * ivy) * ivx), S.kl.frac_bits);
       atomicMax(reinterpret_cast<u64*>(S.key_x + i), make_key(q, j, S.kl));
       if (S.key_y) atomicMax(reinterpret_cast<u64*>(S.key_y + j), make_key(q, i, S.kl));
+    }
+  }
+}
+
+// Seeds of self-joins from their nearest allowed diagonal, one warp per
+// window: cell (i, i + d_lo) is a real cell of the join, so its r is a valid
+// starting best for window i (as a row) and window i + d_lo (as a column).
+// Where the series moves slowly against the window length (random walks)
+// it is close to the final best, and the filter starts high instead of
+// sending every block of the first slabs to the exact path.  win_prefix[p]
+// is the first global window of problem p.
+__global__ void __launch_bounds__(256) diag_seed_kernel(const Problem* __restrict__ probs,
+                                                        const int64_t* __restrict__ win_prefix,
+                                                        int nprob, KeyLayout kl) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  const int64_t total = win_prefix[nprob];
+  for (int64_t w = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+       w < total; w += nwarps) {
+    int lo = 0, hi = nprob;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (win_prefix[mid] <= w) lo = mid; else hi = mid;
+    }
+    const Problem& pr = probs[lo];
+    const int64_t i = w - win_prefix[lo];
+    const int64_t j = i + pr.d_lo;
+    if (i >= pr.R.ns || j >= pr.C.ns) continue;
+    const float ivx = pr.R.inv32[i], ivy = pr.C.inv32[j];
+    if (isnan(ivx) || isnan(ivy)) continue;
+    const float cv = verify_cov_warp(pr.R, pr.C, i, j, pr.m, lane);
+    if (lane == 0) {
+      const uint64_t q = q_from_float_bits(__float_as_uint((cv * ivy) * ivx), kl.frac_bits);
+      if (pr.key_row) atomicMax(reinterpret_cast<u64*>(pr.key_row + i), make_key(q, j, kl));
+      if (pr.key_col) atomicMax(reinterpret_cast<u64*>(pr.key_col + j), make_key(q, i, kl));
     }
   }
 }
