@@ -1512,7 +1512,7 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     for (size_t p = 0; p < probs.size(); ++p) wpre[p + 1] = wpre[p] + probs[p].R.ns;
     CUDA_TRY(cudaMemcpyAsync(d_wpre, wpre.data(), 8 * wpre.size(), cudaMemcpyHostToDevice, st));
     const int64_t seed_blocks =
-        std::min<int64_t>((wpre.back() + 7) / 8, static_cast<int64_t>(ws.sms) * 16);
+        std::min<int64_t>((wpre.back() + 255) / 256, static_cast<int64_t>(ws.sms) * 32);
     diag_seed_kernel<<<static_cast<unsigned>(std::max<int64_t>(seed_blocks, 1)), 256, 0, st>>>(
         d_probs, d_wpre, static_cast<int>(probs.size()), kl);
     ++launches;
@@ -1574,6 +1574,16 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   }
   scamp_c_result tot{};
   read_times(ws, &tot);
+  if (!probs.empty()) {
+    // the batch's work counters live in its arena, not in the join counters
+    unsigned long long c[5] = {0, 0, 0, 0, 0};
+    if (cudaMemcpy(c, d_counter, sizeof(c), cudaMemcpyDeviceToHost) == cudaSuccess) {
+      tot.steps = c[1];
+      tot.slow_steps = c[2];
+      tot.verifications = c[3];
+      ws.vreq_seen = std::max<int64_t>(ws.vreq_seen, static_cast<int64_t>(c[4]));
+    }
+  }
   for (int k = 0; k < count; ++k) {
     res[k].elapsed_ms = tot.elapsed_ms;
     res[k].join_kernel_ms = tot.join_kernel_ms;

@@ -1101,21 +1101,22 @@ __global__ void __launch_bounds__(256) seed_kernel(SeedArgs S) {
   }
 }
 
-// Seeds of self-joins from their nearest allowed diagonal, one warp per
-// window: cell (i, i + d_lo) is a real cell of the join, so its r is a valid
-// starting best for window i (as a row) and window i + d_lo (as a column).
-// Where the series moves slowly against the window length (random walks)
-// it is close to the final best, and the filter starts high instead of
-// sending every block of the first slabs to the exact path.  win_prefix[p]
-// is the first global window of problem p.
+// Seeds of self-joins from diagonals near the exclusion zone, one thread per
+// window: cells (i, i + d_lo + 16 s), s < kDiagSeeds, are real cells of the
+// join, so their r are valid starting bests for window i (as a row) and the
+// partner windows (as columns).  Where the series moves slowly against the
+// window length (random walks) they are close to the final bests, and the
+// filter starts high instead of sending every block of the first slabs to
+// the exact path.  win_prefix[p] is the first global window of problem p.
+constexpr int kDiagSeeds = 8;
+constexpr int kDiagSeedStep = 16;
 __global__ void __launch_bounds__(256) diag_seed_kernel(const Problem* __restrict__ probs,
                                                         const int64_t* __restrict__ win_prefix,
                                                         int nprob, KeyLayout kl) {
-  const int lane = threadIdx.x & 31;
-  const int64_t nwarps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
   const int64_t total = win_prefix[nprob];
-  for (int64_t w = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-       w < total; w += nwarps) {
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t w = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; w < total;
+       w += stride) {
     int lo = 0, hi = nprob;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
@@ -1123,16 +1124,22 @@ __global__ void __launch_bounds__(256) diag_seed_kernel(const Problem* __restric
     }
     const Problem& pr = probs[lo];
     const int64_t i = w - win_prefix[lo];
-    const int64_t j = i + pr.d_lo;
-    if (i >= pr.R.ns || j >= pr.C.ns) continue;
-    const float ivx = pr.R.inv32[i], ivy = pr.C.inv32[j];
-    if (isnan(ivx) || isnan(ivy)) continue;
-    const float cv = verify_cov_warp(pr.R, pr.C, i, j, pr.m, lane);
-    if (lane == 0) {
+    if (i >= pr.R.ns) continue;
+    const float ivx = pr.R.inv32[i];
+    if (isnan(ivx)) continue;
+    uint64_t best = 0;
+    for (int s = 0; s < kDiagSeeds; ++s) {
+      const int64_t j = i + pr.d_lo + static_cast<int64_t>(s) * kDiagSeedStep;
+      if (j >= pr.C.ns) break;
+      const float ivy = pr.C.inv32[j];
+      if (isnan(ivy)) continue;
+      const float cv = verify_cov_lane(pr.R, pr.C, i, j, pr.m);
       const uint64_t q = q_from_float_bits(__float_as_uint((cv * ivy) * ivx), kl.frac_bits);
-      if (pr.key_row) atomicMax(reinterpret_cast<u64*>(pr.key_row + i), make_key(q, j, kl));
       if (pr.key_col) atomicMax(reinterpret_cast<u64*>(pr.key_col + j), make_key(q, i, kl));
+      const uint64_t kr = make_key(q, j, kl);
+      best = kr > best ? kr : best;
     }
+    if (pr.key_row && best) atomicMax(reinterpret_cast<u64*>(pr.key_row + i), best);
   }
 }
 
