@@ -226,14 +226,17 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
                 profile_a_ptr=None, profile_b_ptr=None, sum_a_ptr=None,
                 sum_b_ptr=None, corr_a_ptr=None, corr_b_ptr=None, stream=0,
                 anchor_interval=0, device=0, max_tile_size=128000, max_a_ptr=None,
-                max_b_ptr=None):
+                max_b_ptr=None, knn_a_ptr=None, knn_b_ptr=None, matrix_ptr=None,
+                max_matches=5, matrix_height=50, matrix_width=50):
     """scamp_gb300_join_dev: every pointer is device memory (integers, e.g.
     ``tensor.data_ptr()``), results merged in place, ordered on ``stream``.
-    ``max_a_ptr`` / ``max_b_ptr``: float32 profiles of the 1NN type."""
+    ``max_a_ptr`` / ``max_b_ptr``: float32 profiles of the 1NN type;
+    ``knn_a_ptr`` / ``knn_b_ptr``: ``max_matches`` packed entries per window
+    (ALL_NEIGHBORS); ``matrix_ptr``: the float32 grid (MATRIX_SUMMARY)."""
     lib = _lib.load()
     ca = _args(None, None, m, profile, precision, computing_rows, computing_cols,
                keep_rows, aligned, threshold, -1, -1, max_tile_size,
-               anchor_interval, device, True)
+               anchor_interval, device, True, max_matches, matrix_height, matrix_width)
     ca.timeseries_a = a_ptr
     ca.len_a = int(len_a)
     if b_ptr is not None:
@@ -245,6 +248,7 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
     res.sum_a, res.sum_b = sum_a_ptr, sum_b_ptr
     res.corr_a, res.corr_b = corr_a_ptr, corr_b_ptr
     res.max_a, res.max_b = max_a_ptr, max_b_ptr
+    res.knn_a, res.knn_b, res.matrix = knn_a_ptr, knn_b_ptr, matrix_ptr
     err = ctypes.create_string_buffer(1024)
     rc = lib.scamp_gb300_join_dev(ctypes.byref(ca), ctypes.byref(res),
                                   ctypes.c_void_p(stream), err, 1024)

@@ -139,3 +139,44 @@ def test_matrix_merges_into_given_matrix(gpu_engine):
     mask = np.ones((4, 4), bool)
     mask[0, 3] = False
     assert np.array_equal(r["matrix"][mask], plain["matrix"][mask])
+
+
+@pytest.mark.parametrize("profile", ["1NN", "ALL_NEIGHBORS", "MATRIX_SUMMARY"])
+def test_device_entry_matches_host_entry(gpu_engine, profile):
+    """join_device (device buffers, merged in place) gives what join (host
+    buffers) gives for the float32, k-best and matrix outputs."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(65)
+    a, b = rw(rng, 2600), rw(rng, 1900)
+    m, k, h, w = 48, 3, 9, 11
+    kw = dict(max_matches=k, matrix_height=h, matrix_width=w)
+    host = gpu_engine.join(a, b, m, profile, "double", keep_rows=profile != "MATRIX_SUMMARY",
+                           threshold=0.1, **kw)
+    dev = torch.device("cuda", 0)
+    a_d = torch.from_numpy(a).to(dev)
+    b_d = torch.from_numpy(b).to(dev)
+    nsa, nsb = len(a) - m + 1, len(b) - m + 1
+    no_match = int(np.array([gpu_engine.NO_MATCH], np.uint64).view(np.int64)[0])
+    ptrs, outs = {}, {}
+    if profile == "1NN":
+        for side, ns in (("a", nsa), ("b", nsb)):
+            outs["max_" + side] = torch.full((ns,), -2.0, dtype=torch.float32, device=dev)
+            ptrs["max_%s_ptr" % side] = outs["max_" + side].data_ptr()
+    elif profile == "ALL_NEIGHBORS":
+        for side, ns in (("a", nsa), ("b", nsb)):
+            outs["knn_" + side] = torch.full((ns * k,), no_match, dtype=torch.int64, device=dev)
+            ptrs["knn_%s_ptr" % side] = outs["knn_" + side].data_ptr()
+    else:
+        outs["matrix"] = torch.full((h, w), -2.0, dtype=torch.float32, device=dev)
+        ptrs["matrix_ptr"] = outs["matrix"].data_ptr()
+    stream = torch.cuda.current_stream(dev)
+    gpu_engine.join_device(a_d.data_ptr(), len(a), m, b_d.data_ptr(), len(b), profile, "double",
+                           keep_rows=profile != "MATRIX_SUMMARY", threshold=0.1,
+                           stream=stream.cuda_stream, **ptrs, **kw)
+    torch.cuda.synchronize(dev)
+    for key, t in outs.items():
+        got = t.cpu().numpy()
+        want = host[key.replace("max_", "profile_")]
+        if got.dtype == np.int64:
+            got = got.view(np.uint64)
+        assert np.array_equal(got.reshape(want.shape), want), key
