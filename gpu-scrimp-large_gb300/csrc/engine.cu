@@ -16,6 +16,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -227,6 +228,11 @@ struct Workspace {
   // join; requests beyond the capacity are verified inline, more slowly).
   int64_t vreq_cap = 0;
   int64_t vreq_seen = 0;
+  // Batched joins: the executable graph of the last batch layout (replayed
+  // while the layout repeats) and the autotuned segment length per window.
+  cudaGraphExec_t batch_exec = nullptr;
+  std::vector<int64_t> batch_key;
+  std::map<int64_t, int64_t> batch_seg;
 };
 
 constexpr int64_t kMinVerifyReqs = int64_t{1} << 22;
@@ -1334,10 +1340,11 @@ struct BatchSeries {
   uint64_t cells;
 };
 
-// Segment length of one series of a batch: the anchor interval, reduced for
-// short series so that a band's rows split into at least two segments.
-int64_t batch_segment(int64_t m, int64_t ns, int slab) {
-  int64_t K = default_anchor_interval(m);
+// Segment length of one series of a batch: `pref` (the autotuned value for
+// its window, 0 = none) or the anchor interval, reduced for short series so
+// that a band's rows split into at least two segments.
+int64_t batch_segment(int64_t m, int64_t ns, int slab, int64_t pref) {
+  int64_t K = pref > 0 ? pref : default_anchor_interval(m);
   const int64_t half = std::max<int64_t>(slab, (ns / 2 / slab) * slab);
   K = std::min(K, half);
   const int64_t blk = int64_t{1} << block_shift(m);
@@ -1345,8 +1352,17 @@ int64_t batch_segment(int64_t m, int64_t ns, int slab) {
   return K;
 }
 
+// Runs one batch.  `force_K` > 0 sets every series' segment length (the
+// autotuner's trials); 0 takes the tuned value of the series' window, else the
+// anchor-interval rule.
+//
+// The host gathers the inputs and builds every launch's arguments first, then
+// copies them over; the device part (statistics, keys, diagonal seeds, the
+// persistent band kernel, verification, keys back to profiles) is one CUDA
+// graph, captured once per batch layout and replayed while the layout (sizes,
+// arena and request-buffer addresses, grid) repeats.
 int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int count,
-              cudaStream_t st, std::string* msg) {
+              cudaStream_t st, std::string* msg, int64_t force_K = 0) {
   int rc;
   ws.timed_kernel = false;
   ws.timed_verify = false;
@@ -1361,7 +1377,12 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     b.ns = b.n - b.m + 1;
     b.excl = b.m / 4;  // src/tile.cpp:14
     b.bshift = block_shift(b.m);
-    b.K = batch_segment(b.m, b.ns, mixed_1nn_slab_rows());
+    int64_t pref = force_K;
+    if (pref <= 0) {
+      const auto it = ws.batch_seg.find(b.m);
+      pref = it == ws.batch_seg.end() ? 0 : it->second;
+    }
+    b.K = batch_segment(b.m, b.ns, mixed_1nn_slab_rows(), pref);
     b.off_n = Nn;
     b.off_ns = Nns;
     b.off_blk = Nblk;
@@ -1413,19 +1434,13 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   int64_t* d_bpre = reinterpret_cast<int64_t*>(take(b_bpre));
   int64_t* d_wpre = reinterpret_cast<int64_t*>(take(b_wpre));
 
-  CUDA_TRY(cudaEventRecord(ws.ev0, st));
-  uint32_t launches = 0;
-  // ---- inputs: gathered on the host, one copy each way ----
+  // ---- host side: inputs gathered, every launch's arguments built ----
   std::vector<double> h_raw(static_cast<size_t>(Nn));
   std::vector<uint64_t> h_prof(static_cast<size_t>(Nns));
   for (int k = 0; k < count; ++k) {
     std::memcpy(h_raw.data() + ser[k].off_n, args[k].timeseries_a, ser[k].n * 8);
     std::memcpy(h_prof.data() + ser[k].off_ns, res[k].profile_a, ser[k].ns * 8);
   }
-  CUDA_TRY(cudaMemcpyAsync(d_raw, h_raw.data(), Nn * 8, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(d_prof, h_prof.data(), Nns * 8, cudaMemcpyHostToDevice, st));
-
-  // ---- statistics: one launch for the batch ----
   const int chunk = 64;
   std::vector<StatsJob> jobs(count);
   std::vector<int64_t> jpre(count + 1, 0);
@@ -1451,25 +1466,13 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     const int64_t threads = (b.ns + chunk - 1) / chunk;
     jpre[k + 1] = jpre[k] + (threads + 127) / 128;
   }
-  CUDA_TRY(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(StatsJob) * count, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(d_jpre, jpre.data(), 8 * (count + 1), cudaMemcpyHostToDevice, st));
-  stats_batch_kernel<<<static_cast<unsigned>(jpre[count]), 128, 0, st>>>(d_jobs, d_jpre, count, 0, chunk);
-  ++launches;
-
-  // ---- keys ----
   const KeyLayout kl = make_key_layout(ns_max);
-  profile_to_keys_kernel<<<static_cast<unsigned>((Nns + 255) / 256), 256, 0, st>>>(d_prof, d_keys, Nns, kl);
-  ++launches;
-  CUDA_TRY(cudaGetLastError());
-
-  // ---- problems and the work queue ----
   const int W = mixed_1nn_band_width();
   std::vector<Problem> probs;
   probs.reserve(count);
   std::vector<int64_t> bpre;
   bpre.push_back(0);
   int64_t band_total = 0;
-  uint64_t cells_total = 0;
   for (int k = 0; k < count; ++k) {
     const BatchSeries& b = ser[k];
     if (b.cells == 0) continue;
@@ -1501,24 +1504,18 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
       bpre.push_back(bpre.back() + (rows + 2 * b.K - 1) / (2 * b.K));
     }
     band_total += pr.nbands;
-    cells_total += b.cells;
     probs.push_back(pr);
   }
+  // seeds from each series' nearest allowed diagonal (diag_seed_kernel)
+  std::vector<int64_t> wpre(probs.size() + 1, 0);
+  for (size_t p = 0; p < probs.size(); ++p) wpre[p + 1] = wpre[p] + probs[p].R.ns;
+  const int64_t seed_blocks = std::max<int64_t>(
+      std::min<int64_t>((wpre.back() + 255) / 256, static_cast<int64_t>(ws.sms) * 32), 1);
+  JoinParams P{};
+  int64_t grid = 0;
+  const size_t smem = mixed_1nn_smem_bytes();
+  const void* kfn = reinterpret_cast<const void*>(join_mixed_1nn_kernel);
   if (!probs.empty()) {
-    CUDA_TRY(cudaMemcpyAsync(d_probs, probs.data(), sizeof(Problem) * probs.size(),
-                             cudaMemcpyHostToDevice, st));
-    // seeds from each series' nearest allowed diagonal (diag_seed_kernel)
-    std::vector<int64_t> wpre(probs.size() + 1, 0);
-    for (size_t p = 0; p < probs.size(); ++p) wpre[p + 1] = wpre[p] + probs[p].R.ns;
-    CUDA_TRY(cudaMemcpyAsync(d_wpre, wpre.data(), 8 * wpre.size(), cudaMemcpyHostToDevice, st));
-    const int64_t seed_blocks =
-        std::min<int64_t>((wpre.back() + 255) / 256, static_cast<int64_t>(ws.sms) * 32);
-    diag_seed_kernel<<<static_cast<unsigned>(std::max<int64_t>(seed_blocks, 1)), 256, 0, st>>>(
-        d_probs, d_wpre, static_cast<int>(probs.size()), kl);
-    ++launches;
-    CUDA_TRY(cudaMemcpyAsync(d_bpre, bpre.data(), 8 * bpre.size(), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemsetAsync(d_counter, 0, 64, st));
-    JoinParams P{};
     P.nprob = 0;
     P.batch = d_probs;
     P.nbatch = static_cast<int64_t>(probs.size());
@@ -1539,27 +1536,80 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     ws.vreq_cap = want;
     P.vreq = static_cast<VerifyReq*>(q);
     P.vreq_cap = want;
-    const size_t smem = mixed_1nn_smem_bytes();
-    const void* kfn = reinterpret_cast<const void*>(join_mixed_1nn_kernel);
     CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int occ = 1;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, mixed_1nn_threads(), smem));
-    const int64_t grid = std::min<int64_t>(static_cast<int64_t>(ws.sms) * std::max(occ, 1), P.total_units);
-    CUDA_TRY(cudaEventRecord(ws.evk0, st));
-    ws.timed_kernel = true;
-    join_mixed_1nn_kernel<<<static_cast<unsigned>(grid), mixed_1nn_threads(), smem, st>>>(P);
-    ++launches;
-    CUDA_TRY(cudaEventRecord(ws.evkv, st));
-    ws.timed_verify = true;
-    verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
-    ++launches;
-    CUDA_TRY(cudaGetLastError());
-    CUDA_TRY(cudaEventRecord(ws.evk1, st));
+    grid = std::min<int64_t>(static_cast<int64_t>(ws.sms) * std::max(occ, 1), P.total_units);
   }
-  keys_to_profile_kernel<<<static_cast<unsigned>((Nns + 255) / 256), 256, 0, st>>>(
-      d_keys, d_prof, want_corr ? d_corr : nullptr, Nns, kl);
-  ++launches;
-  CUDA_TRY(cudaGetLastError());
+
+  // ---- copies in ----
+  CUDA_TRY(cudaEventRecord(ws.ev0, st));
+  CUDA_TRY(cudaMemcpyAsync(d_raw, h_raw.data(), Nn * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d_prof, h_prof.data(), Nns * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(StatsJob) * count, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d_jpre, jpre.data(), 8 * (count + 1), cudaMemcpyHostToDevice, st));
+  if (!probs.empty()) {
+    CUDA_TRY(cudaMemcpyAsync(d_probs, probs.data(), sizeof(Problem) * probs.size(),
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_wpre, wpre.data(), 8 * wpre.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_bpre, bpre.data(), 8 * bpre.size(), cudaMemcpyHostToDevice, st));
+  }
+
+  // ---- device part: one graph ----
+  uint32_t launches = probs.empty() ? 3 : 6;
+  const std::vector<int64_t> key = {
+      reinterpret_cast<int64_t>(arena), Nn, Nns, Nblk, count, want_corr ? 1 : 0, bands_max,
+      jpre[count], kl.idx_bits, static_cast<int64_t>(probs.size()), seed_blocks, band_total,
+      P.total_units, grid, reinterpret_cast<int64_t>(P.vreq), P.vreq_cap,
+      static_cast<int64_t>(smem), reinterpret_cast<int64_t>(st)};
+  if (!ws.batch_exec || ws.batch_key != key) {
+    auto enqueue = [&]() -> cudaError_t {
+      cudaError_t e;
+      stats_batch_kernel<<<static_cast<unsigned>(jpre[count]), 128, 0, st>>>(d_jobs, d_jpre, count, 0,
+                                                                              chunk);
+      profile_to_keys_kernel<<<static_cast<unsigned>((Nns + 255) / 256), 256, 0, st>>>(d_prof, d_keys,
+                                                                                       Nns, kl);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      if (!probs.empty()) {
+        diag_seed_kernel<<<static_cast<unsigned>(seed_blocks), 256, 0, st>>>(
+            d_probs, d_wpre, static_cast<int>(probs.size()), kl);
+        if ((e = cudaMemsetAsync(d_counter, 0, 64, st)) != cudaSuccess) return e;
+        if ((e = cudaEventRecordWithFlags(ws.evk0, st, cudaEventRecordExternal)) != cudaSuccess) return e;
+        join_mixed_1nn_kernel<<<static_cast<unsigned>(grid), mixed_1nn_threads(), smem, st>>>(P);
+        if ((e = cudaEventRecordWithFlags(ws.evkv, st, cudaEventRecordExternal)) != cudaSuccess) return e;
+        verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
+        if ((e = cudaEventRecordWithFlags(ws.evk1, st, cudaEventRecordExternal)) != cudaSuccess) return e;
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      }
+      keys_to_profile_kernel<<<static_cast<unsigned>((Nns + 255) / 256), 256, 0, st>>>(
+          d_keys, d_prof, want_corr ? d_corr : nullptr, Nns, kl);
+      return cudaGetLastError();
+    };
+    if (ws.batch_exec) {
+      CUDA_TRY(cudaStreamSynchronize(st));
+      cudaGraphExecDestroy(ws.batch_exec);
+      ws.batch_exec = nullptr;
+      ws.batch_key.clear();
+    }
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t ce = enqueue();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(st, &graph);
+    cudaError_t ie = cudaSuccess;
+    if (ce == cudaSuccess && ee == cudaSuccess) ie = cudaGraphInstantiate(&ws.batch_exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    const cudaError_t bad = ce != cudaSuccess ? ce : (ee != cudaSuccess ? ee : ie);
+    if (bad != cudaSuccess) {
+      ws.batch_exec = nullptr;
+      *msg = std::string("CUDA error: ") + cudaGetErrorString(bad) + " while building the batch graph";
+      return SCAMP_ERR_CUDA;
+    }
+    ws.batch_key = key;
+  }
+  CUDA_TRY(cudaGraphLaunch(ws.batch_exec, st));
+  ws.timed_kernel = ws.timed_verify = !probs.empty();
+
+  // ---- copies out ----
   CUDA_TRY(cudaMemcpyAsync(h_prof.data(), d_prof, Nns * 8, cudaMemcpyDeviceToHost, st));
   std::vector<double> h_corr;
   if (want_corr) {
@@ -1594,7 +1644,100 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     res[k].slow_steps = tot.slow_steps;
     res[k].verifications = tot.verifications;
   }
-  (void)cells_total;
+  return SCAMP_OK;
+}
+
+// Autotuner of the batched join's tile height.  A band unit is W diagonals x
+// two segments of K rows; K is also the mixed form's anchor interval.  For
+// each window length among the series (all of them, or with `retune` = 0 the
+// ones not tuned yet), it runs the band kernel on a sample of those series
+// (in batch order, until kTuneCells comparisons) at K = the anchor-interval
+// rule's value, half and a quarter of it (never below 256 rows), twice each,
+// and keeps the K with the shortest band + verification kernel time; a
+// shorter K must win by 2% to replace a longer one.  Candidates stop at the
+// rule's value because longer intervals let the FP32 recurrence drift
+// further between anchors.  The sample's profiles are scratch.
+constexpr uint64_t kTuneCells = uint64_t{1} << 34;
+
+int tune_batch(Workspace& ws, const scamp_c_args* args, int count, bool retune,
+               std::string* msg) {
+  std::map<int64_t, std::vector<int>> by_window;
+  for (int k = 0; k < count; ++k) by_window[static_cast<int64_t>(args[k].window)].push_back(k);
+  for (const auto& w : by_window) {
+    const int64_t m = w.first;
+    if (!retune && ws.batch_seg.count(m)) continue;
+    std::vector<scamp_c_args> sa;
+    uint64_t cells = 0;
+    for (int k : w.second) {
+      if (cells >= kTuneCells) break;
+      const int64_t ns = static_cast<int64_t>(args[k].len_a) - m + 1;
+      if (ns <= m / 4) continue;
+      sa.push_back(args[k]);
+      cells += diag_cells(ns, ns, m / 4, ns);
+    }
+    const int64_t k_rule = default_anchor_interval(m);
+    if (sa.empty()) {
+      ws.batch_seg[m] = k_rule;
+      continue;
+    }
+    std::vector<scamp_c_result> sr(sa.size());
+    std::vector<std::vector<uint64_t>> prof(sa.size());
+    for (size_t k = 0; k < sa.size(); ++k) {
+      prof[k].resize(sa[k].len_a - sa[k].window + 1);
+      sr[k] = scamp_c_result{};
+      sr[k].profile_a = prof[k].data();
+    }
+    const uint64_t no_match = (uint64_t{0xFFFFFFFF} << 32) | 0xC0000000u;  // {-2.0f, 0xFFFFFFFF}
+    int64_t best = k_rule;
+    double best_ms = 0;
+    for (int64_t K = k_rule; K >= std::min<int64_t>(k_rule, 256); K /= 2) {
+      if (K < k_rule / 4) break;
+      double t = -1;
+      for (int rep = 0; rep < 2; ++rep) {
+        for (auto& p : prof) std::fill(p.begin(), p.end(), no_match);
+        const int rc = run_batch(ws, sa.data(), sr.data(), static_cast<int>(sa.size()), ws.stream, msg, K);
+        if (rc) return rc;
+        const double ms = sr[0].join_kernel_ms;
+        if (t < 0 || ms < t) t = ms;
+      }
+      if (K == k_rule || t < 0.98 * best_ms) {
+        best = K;
+        best_ms = t;
+      }
+      if (K <= 256) break;
+    }
+    ws.batch_seg[m] = best;
+  }
+  return SCAMP_OK;
+}
+
+// Checks shared by scamp_gb300_join_batch and scamp_gb300_tune_batch (`res`
+// null: no result buffers to check).
+int validate_batch(const scamp_c_args* args, const scamp_c_result* res, int count,
+                   std::string* msg) {
+  for (int k = 0; k < count; ++k) {
+    const scamp_c_args* a = &args[k];
+    std::string m;
+    int rc = validate(a, &m);
+    if (rc == SCAMP_OK) {
+      if (a->has_b || a->is_aligned || a->keep_rows_separate || !a->computing_rows ||
+          !a->computing_columns || a->distributed_start_row >= 0 || a->distributed_start_col >= 0)
+        m = "Error: batched joins are plain self-joins (rows and columns into profile A)";
+      else if (a->profile_type != SCAMP_PROFILE_1NN_INDEX)
+        m = "Error: batched joins compute 1NN_INDEX profiles";
+      else if (a->precision_type != SCAMP_PRECISION_MIXED && a->precision_type != SCAMP_PRECISION_SINGLE)
+        m = "Error: batched joins run the mixed form (precision single or mixed)";
+      else if (a->device != args[0].device)
+        m = "Error: a batch runs on one device";
+      else if (res && !res[k].profile_a)
+        m = "Error: profile buffer missing";
+      if (!m.empty()) rc = SCAMP_ERR_INVALID_ARGS;
+    }
+    if (rc) {
+      *msg = "series " + std::to_string(k) + ": " + m;
+      return rc;
+    }
+  }
   return SCAMP_OK;
 }
 
@@ -1608,33 +1751,39 @@ extern "C" int scamp_gb300_join_batch(const scamp_c_args* args, scamp_c_result* 
     set_err(errbuf, errlen, "Error: empty batch");
     return SCAMP_ERR_INVALID_ARGS;
   }
-  for (int k = 0; k < count; ++k) {
-    const scamp_c_args* a = &args[k];
-    int rc = validate(a, &msg);
-    if (rc == SCAMP_OK) {
-      if (a->has_b || a->is_aligned || a->keep_rows_separate || !a->computing_rows ||
-          !a->computing_columns || a->distributed_start_row >= 0 || a->distributed_start_col >= 0)
-        msg = "Error: batched joins are plain self-joins (rows and columns into profile A)";
-      else if (a->profile_type != SCAMP_PROFILE_1NN_INDEX)
-        msg = "Error: batched joins compute 1NN_INDEX profiles";
-      else if (a->precision_type != SCAMP_PRECISION_MIXED && a->precision_type != SCAMP_PRECISION_SINGLE)
-        msg = "Error: batched joins run the mixed form (precision single or mixed)";
-      else if (a->device != args[0].device)
-        msg = "Error: a batch runs on one device";
-      else if (!res[k].profile_a)
-        msg = "Error: profile buffer missing";
-      if (!msg.empty()) rc = SCAMP_ERR_INVALID_ARGS;
-    }
-    if (rc) {
-      set_err(errbuf, errlen, "series " + std::to_string(k) + ": " + msg);
-      return rc;
-    }
-  }
+  int rc = validate_batch(args, res, count, &msg);
+  if (rc) { set_err(errbuf, errlen, msg); return rc; }
   Workspace* ws;
-  int rc = init_workspace(args[0].device, &ws, &msg);
+  rc = init_workspace(args[0].device, &ws, &msg);
   if (rc) { set_err(errbuf, errlen, msg); return rc; }
   std::lock_guard<std::mutex> lock(ws->mu);
   rc = run_batch(*ws, args, res, count, ws->stream, &msg);
   if (rc) set_err(errbuf, errlen, msg);
   return rc;
+}
+
+extern "C" int scamp_gb300_tune_batch(const scamp_c_args* args, int count, int retune,
+                                      int64_t* segment, char* errbuf, size_t errlen) {
+  std::string msg;
+  if (!args || count <= 0) {
+    set_err(errbuf, errlen, "Error: empty batch");
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  int rc = validate_batch(args, nullptr, count, &msg);
+  if (rc) { set_err(errbuf, errlen, msg); return rc; }
+  Workspace* ws;
+  rc = init_workspace(args[0].device, &ws, &msg);
+  if (rc) { set_err(errbuf, errlen, msg); return rc; }
+  std::lock_guard<std::mutex> lock(ws->mu);
+  rc = tune_batch(*ws, args, count, retune != 0, &msg);
+  if (rc) { set_err(errbuf, errlen, msg); return rc; }
+  if (segment) {
+    for (int k = 0; k < count; ++k) {
+      const int64_t m = static_cast<int64_t>(args[k].window);
+      const auto it = ws->batch_seg.find(m);
+      segment[k] = batch_segment(m, static_cast<int64_t>(args[k].len_a) - m + 1, mixed_1nn_slab_rows(),
+                                 it == ws->batch_seg.end() ? 0 : it->second);
+    }
+  }
+  return SCAMP_OK;
 }

@@ -20,7 +20,7 @@ from ._lib import SCAMPError
 __all__ = [
     "selfjoin", "abjoin", "selfjoin_sum", "abjoin_sum", "selfjoin_knn", "abjoin_knn",
     "selfjoin_matrix", "abjoin_matrix", "gpu_supported",
-    "join", "join_device", "SCAMPError", "count_cells", "pipe_peak",
+    "join", "join_device", "join_batch", "tune_batch", "SCAMPError", "count_cells", "pipe_peak",
     "unpack_profile", "to_distance", "version",
 ]
 
@@ -261,12 +261,8 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
             "gpu_launches": int(res.gpu_launches)}
 
 
-def join_batch(series, windows, precision="mixed", return_corr=False, device=0):
-    """scamp_gb300_join_batch: independent 1NN_INDEX self-joins of every
-    series in ``series`` (window ``windows[k]``, or one int for all) in one
-    batched call.  Returns a list of dicts with ``profile_a`` (packed
-    entries), ``corr_a`` (with ``return_corr``) and the batch's timings."""
-    lib = _lib.load()
+def _batch_args(series, windows, precision, device):
+    """(float64 arrays, windows, CArgs array) of a batch of self-joins."""
     n = len(series)
     if isinstance(windows, (int, np.integer)):
         windows = [int(windows)] * n
@@ -274,12 +270,45 @@ def join_batch(series, windows, precision="mixed", return_corr=False, device=0):
         raise ValueError("one window per series")
     arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in series]
     cargs = (_lib.CArgs * n)()
-    cres = (_lib.CResult * n)()
-    profs, corrs = [], []
     for k, (x, m) in enumerate(zip(arrs, windows)):
         ca = _args(x, None, m, "1NN_INDEX", precision, True, True, False, False, 0.0,
                    -1, -1, max(128000, 2 * int(m)), 0, device, True)
         ctypes.memmove(ctypes.byref(cargs[k]), ctypes.byref(ca), ctypes.sizeof(ca))
+    return arrs, windows, cargs
+
+
+def tune_batch(series, windows, precision="mixed", retune=False, device=0):
+    """scamp_gb300_tune_batch: picks, per window length, the batched join's
+    segment length (tile height, also the anchor interval) by timing the
+    band kernel on a sample of these series; later join_batch calls on the
+    device use it.  Windows tuned before are kept unless ``retune``.
+    Returns the segment length each series will use."""
+    lib = _lib.load()
+    arrs, windows, cargs = _batch_args(series, windows, precision, device)
+    n = len(arrs)
+    seg = np.zeros(n, dtype=np.int64)
+    err = ctypes.create_string_buffer(1024)
+    rc = lib.scamp_gb300_tune_batch(cargs, n, 1 if retune else 0,
+                                    seg.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), err, 1024)
+    _check(rc, err)
+    return seg
+
+
+def join_batch(series, windows, precision="mixed", return_corr=False, device=0,
+               autotune=False):
+    """scamp_gb300_join_batch: independent 1NN_INDEX self-joins of every
+    series in ``series`` (window ``windows[k]``, or one int for all) in one
+    batched call.  Returns a list of dicts with ``profile_a`` (packed
+    entries), ``corr_a`` (with ``return_corr``) and the batch's timings.
+    ``autotune``: first run tune_batch for windows not tuned yet."""
+    lib = _lib.load()
+    if autotune:
+        tune_batch(series, windows, precision, False, device)
+    arrs, windows, cargs = _batch_args(series, windows, precision, device)
+    n = len(arrs)
+    cres = (_lib.CResult * n)()
+    profs, corrs = [], []
+    for k, (x, m) in enumerate(zip(arrs, windows)):
         ns = len(x) - int(m) + 1
         p = np.full(max(ns, 0), NO_MATCH, dtype=np.uint64)
         profs.append(p)

@@ -37,6 +37,7 @@ EXPORTED_SYMBOLS = (
     "scamp_gb300_join_dev",
     "scamp_gb300_join_dev_noalloc",
     "scamp_gb300_join_batch",
+    "scamp_gb300_tune_batch",
     "scamp_gb300_validate",
     "scamp_gb300_count_cells",
     "scamp_gb300_gpu_supported",
@@ -137,6 +138,10 @@ def load():
     lib.scamp_gb300_join_batch.argtypes = [ctypes.POINTER(CArgs), ctypes.POINTER(CResult),
                                            ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
     lib.scamp_gb300_join_batch.restype = ctypes.c_int
+    lib.scamp_gb300_tune_batch.argtypes = [ctypes.POINTER(CArgs), ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_int64), ctypes.c_char_p,
+                                           ctypes.c_size_t]
+    lib.scamp_gb300_tune_batch.restype = ctypes.c_int
     lib.scamp_gb300_validate.argtypes = [ctypes.POINTER(CArgs), ctypes.c_char_p, ctypes.c_size_t]
     lib.scamp_gb300_validate.restype = ctypes.c_int
     lib.scamp_gb300_count_cells.argtypes = [ctypes.POINTER(CArgs)]

@@ -158,6 +158,17 @@ int scamp_gb300_join_dev(const scamp_c_args *args, scamp_c_result *res,
 int scamp_gb300_join_batch(const scamp_c_args *args, scamp_c_result *res, int count,
                            char *errbuf, size_t errlen);
 
+/* Autotuner of scamp_gb300_join_batch's tile height: for each window length
+ * among the count series (same rules as scamp_gb300_join_batch; no result
+ * buffers), times the band kernel on a sample of those series at the
+ * segment lengths K (rows per half-unit, also the anchor interval) of the
+ * default rule, half and a quarter of it, and keeps the fastest for every
+ * later batch on args[0].device.  retune = 0 skips windows already tuned.
+ * segment (optional, count entries) receives the K each series will use.
+ * No counterpart in the reference, which has no batched joins. */
+int scamp_gb300_tune_batch(const scamp_c_args *args, int count, int retune, int64_t *segment,
+                           char *errbuf, size_t errlen);
+
 /* The FP64 form of scamp_gb300_join_dev without any allocation: every
  * intermediate buffer lives in one static device array of the library
  * (about 8.6 MB per device), so the join calls no allocator.  For callers

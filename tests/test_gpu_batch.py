@@ -47,6 +47,56 @@ def test_batch_equals_single_joins(gpu_engine):
         assert np.max(np.abs(single["corr_a"][ok] - r["corr_a"][ok]), initial=0.0) <= TOL_MIXED
 
 
+def _close(x, y):
+    ok = x["corr_a"] >= -1
+    assert np.array_equal(ok, y["corr_a"] >= -1)
+    assert np.max(np.abs(x["corr_a"][ok] - y["corr_a"][ok]), initial=0.0) <= TOL_MIXED
+
+
+def test_batch_graph_replay(gpu_engine):
+    """The device part of a batch is one captured graph, replayed while the
+    layout repeats: a repeated call gives the same profiles (within the
+    mixed tolerance: which cells take the exact path depends on timing),
+    the band kernel's events inside the graph time it, and another layout
+    captures a new graph."""
+    series, windows = _batch(9, 16)
+    a = gpu_engine.join_batch(series, windows, return_corr=True)
+    b = gpu_engine.join_batch(series, windows, return_corr=True)
+    for r in (a[0], b[0]):
+        assert 0 < r["join_kernel_ms"] <= r["elapsed_ms"]
+        assert r["counters"]["steps"] > 0
+    for x, y in zip(a, b):
+        _close(x, y)
+    c = gpu_engine.join_batch(series[:10], windows[:10], return_corr=True)
+    for x, y in zip(a[:10], c):
+        _close(x, y)
+
+
+def test_batch_autotune(gpu_engine, oracle_mod):
+    """tune_batch picks each window's segment length among the rule's value
+    (1024 rows for these windows), half and a quarter of it, capped for
+    short series as the rule is; batches joined after tuning still match
+    the oracle."""
+    series, windows = _batch(21, 24)
+    seg = gpu_engine.tune_batch(series, windows, retune=True)
+    assert len(seg) == len(series)
+    for x, m, K in zip(series, windows, seg):
+        half = max(128, ((len(x) - m + 1) // 2 // 128) * 128)
+        assert K in {min(c, half) for c in (1024, 512, 256)}, (len(x), m, K)
+    by_m = {}
+    for x, m, K in zip(series, windows, seg):
+        if (len(x) - m + 1) // 2 >= 1024:
+            by_m.setdefault(m, set()).add(int(K))
+    assert all(len(v) == 1 for v in by_m.values())  # one choice per window
+    out = gpu_engine.join_batch(series, windows, precision="mixed", return_corr=True,
+                                autotune=True)
+    for k, (x, m, r) in enumerate(zip(series, windows, out)):
+        want = oracle_mod.join(x, None, m, "1NN_INDEX", exact_flat=True)
+        _, gi = gpu_engine.unpack_profile(r["profile_a"])
+        check_1nn("tuned%d" % k, r["corr_a"], gi, want["corr_a"], want["idx_a"], TOL_MIXED,
+                  x, x, m)
+
+
 def test_batch_rejects_unsupported(gpu_engine):
     with pytest.raises(ValueError):
         gpu_engine.join_batch([np.arange(500.0)], [600])

@@ -139,6 +139,22 @@ def test_join_without_gpu_fails_loudly(engine):
         engine.join(a, None, 20)
 
 
+def test_batch_entries_validate_before_the_device(engine):
+    """Batched joins and their autotuner reject what they do not run
+    (checked on the host, so without a GPU too)."""
+    x = np.cumsum(np.random.default_rng(1).standard_normal(600))
+    for call in (engine.join_batch, engine.tune_batch):
+        with pytest.raises(ValueError, match="mixed form"):
+            call([x, x], [32, 64], precision="double")
+        with pytest.raises(ValueError, match="series 1"):
+            call([x, x[:20]], [32, 32])
+        with pytest.raises(ValueError, match="one window per series"):
+            call([x, x], [32])
+    if not engine.gpu_supported():
+        with pytest.raises(engine.SCAMPError, match="no CUDA device"):
+            engine.tune_batch([x], 32)
+
+
 def test_key_layout_roundtrip_host():
     # The fixed-point key (engine.cuh): q = floor((r + 2) * 2^F); decoding
     # recovers r within 2^-F and preserves order.
