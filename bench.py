@@ -382,6 +382,10 @@ def main():
                    help="log2 length of A (B is half); smaller only for profiling captures")
     p.add_argument("--profile-form", default="mixed", choices=["mixed", "double"],
                    help="form run by --profile-only")
+    p.add_argument("--anchor-study", action="store_true",
+                   help="--workload self: also time the mixed form at anchor intervals "
+                        "K = 128, 256, 1024, 4096 rows on the FP64 leg's samples, each with "
+                        "its max |r| error and index agreement against the FP64 form")
     p.add_argument("--profile-only", action="store_true",
                    help="run only the timed mixed joins (for ncu captures); prints no JSON")
     args = p.parse_args()
@@ -439,8 +443,9 @@ def main():
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     nm = no_match - (1 << 64) if no_match >= (1 << 63) else no_match
 
-    def one(precision, n_a=None):
-        """One join (the whole workload, or the self-join's first n_a samples)."""
+    def one(precision, n_a=None, anchor=0):
+        """One join (the whole workload, or the self-join's first n_a samples;
+        anchor: the mixed form's anchor interval, 0 = its default rule)."""
         with torch.cuda.stream(stream):
             prof_a.fill_(nm)
             prof_b.fill_(nm)
@@ -454,7 +459,7 @@ def main():
             computing_rows=True, keep_rows=not self_join, profile_a_ptr=prof_a.data_ptr(),
             profile_b_ptr=None if self_join else prof_b.data_ptr(), corr_a_ptr=corr_a.data_ptr(),
             corr_b_ptr=None if self_join else corr_b.data_ptr(), stream=stream.cuda_stream,
-            device=local)
+            anchor_interval=anchor, device=local)
         ev1.record(stream)
         ev1.synchronize()
         # the join's own CUDA events on this stream bracket its device work
@@ -522,6 +527,21 @@ def main():
             max_err = max(max_err, float(np.max(np.abs(mixed_corr[k][ok] - f_corr[k][ok]))))
         idx_agree += int(np.sum(mixed_idx[k][ok] == f_idx[k][ok]))
         n_valid += int(ok.sum())
+    study = []
+    if args.anchor_study and self_join:
+        # the precision study's anchor intervals (one slab, 128 rows, is the
+        # shortest segment the band kernel runs)
+        ok = f_corr[0] >= -1
+        for K in (128, 256, 1024, 4096):
+            ms, rk = one("mixed", n_fp64, anchor=K)
+            c = corr_a.cpu().numpy()[:n_f]
+            ix = (prof_a.cpu().numpy().view(np.uint64) >> np.uint64(32))[:n_f]
+            study.append({"anchor_interval": K, "ms": ms, "comparisons": rk["comparisons"],
+                          "comparisons_per_s": rk["comparisons"] / (ms * 1e-3),
+                          "max_abs_r_err_vs_fp64": float(np.max(np.abs(c[ok] - f_corr[0][ok]),
+                                                                initial=0.0)),
+                          "index_agreement_vs_fp64": float(np.mean(ix[ok] == f_idx[0][ok])),
+                          "work_counters": rk["counters"]})
 
     # ---- e2e through the host-buffer C ABI ----
     a_pin = torch.from_numpy(a_np).pin_memory().numpy()
@@ -603,6 +623,8 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    if study:
+        line["anchor_study"] = study
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_leg()
     print(json.dumps(line), flush=True)
