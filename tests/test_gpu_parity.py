@@ -27,7 +27,7 @@ def run_1nn(engine, oracle, a, b, m, precision, tol, keep_rows=False, rows=True,
     # reference's sequential ssd can leave flat windows "valid".
     want = oracle.join(a, b, m, "1NN_INDEX", computing_rows=rows, keep_rows=keep_rows,
                        aligned=aligned, exact_flat=True, brute=brute,
-                       precision=oracle_precision)
+                       precision=oracle_precision, **kw)
     _, gi = engine.unpack_profile(got["profile_a"])
     T_other = a if b is None else b
     check_1nn(name + "/A", got["corr_a"], gi, want["corr_a"], want["idx_a"], tol, a, T_other, m)
@@ -212,6 +212,36 @@ def test_sum_thresh_many_units(gpu_engine):
             got = gpu_engine.join(a, b, 64, "SUM_THRESH", "mixed", threshold=thr, keep_rows=True)
             check_sum("A", got["sum_a"], want["sum_a"], thr, 2e-5, TOL_MIXED)
             check_sum("B", got["sum_b"], want["sum_b"], thr, 2e-5, TOL_MIXED)
+
+
+def test_single_precision_is_served_by_the_mixed_form(gpu_engine, oracle_mod):
+    """PRECISION_SINGLE (pyscamp precision='single') runs the mixed engine,
+    so it meets the mixed tolerance (stricter than the reference's SINGLE)."""
+    rng = np.random.default_rng(71)
+    a, b = rw(rng, 4000), rw(rng, 2500)
+    run_1nn(gpu_engine, oracle_mod, a, None, 64, "single", TOL_MIXED, name="single/self")
+    run_1nn(gpu_engine, oracle_mod, a, b, 50, "single", TOL_MIXED, keep_rows=True,
+            name="single/ab")
+    got = gpu_engine.join(a, b, 64, "SUM_THRESH", "single", threshold=0.7, keep_rows=True)
+    want = oracle_mod.join(a, b, 64, "SUM_THRESH", threshold=0.7, keep_rows=True)
+    check_sum("single/sumA", got["sum_a"], want["sum_a"], 0.7, 2e-5, TOL_MIXED)
+    check_sum("single/sumB", got["sum_b"], want["sum_b"], 0.7, 2e-5, TOL_MIXED)
+    prof, idx = gpu_engine.selfjoin(a, 64, precision="single")
+    assert prof.dtype == np.float32 and len(idx) == len(a) - 63
+
+
+@pytest.mark.parametrize("precision,tol", PRECISIONS)
+def test_distributed_offsets_1nn(gpu_engine, oracle_mod, precision, tol):
+    """1NN_INDEX with the distributed tile offsets (--global_row/col): an
+    aligned AB-join of two pieces of one series whose global positions make
+    the exclusion zone cut through the join, and an unaligned one."""
+    rng = np.random.default_rng(72)
+    x = rw(rng, 6000)
+    a, b = x[:3500].copy(), x[1200:4400].copy()
+    run_1nn(gpu_engine, oracle_mod, a, b, 64, precision, tol, keep_rows=True, aligned=True,
+            start_row=1200, start_col=0, name="offsets/aligned")
+    run_1nn(gpu_engine, oracle_mod, a, b, 64, precision, tol, keep_rows=True,
+            start_row=1200, start_col=0, name="offsets/plain")
 
 
 @pytest.mark.parametrize("precision,tol", PRECISIONS)
