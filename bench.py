@@ -49,9 +49,10 @@ CPU_NA, CPU_NB = 1 << 17, 1 << 16
 OPS_PER_CELL = 4
 # DRAM bytes (read + write) of one launch of the mixed join kernel on this
 # workload: one single-pass ncu capture of the full-size launch
-# (profiles/join_mixed_1nn_cfg2.txt).  Mostly the verification requests and
-# profile atomics: the series, statistics and profiles stay in the 129 MB L2.
-DRAM_BYTES_PER_LAUNCH = 51.47e6 + 109.83e6
+# (profiles/join_mixed_1nn_cfg2.txt; mean of the five main launches).  Mostly
+# the verification requests (16 B each, 1.5e7 per join) and profile write-back:
+# the series, statistics and profiles stay in the 129 MB L2.
+DRAM_BYTES_PER_LAUNCH = 57.45e6 + 202.48e6
 
 
 def max_over_ranks(x, dist, device):

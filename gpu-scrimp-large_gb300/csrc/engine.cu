@@ -39,14 +39,30 @@ int measure_pipe_peak(int device, int kind, double* ops_per_s);
 
 namespace {
 
-// Rows between re-anchors of the mixed form: 8 m within [1024, 4096], the
-// measured best.  AB-join of 2^20 x 2^19 random walks, m = 256, with seeds and
-// kTrust = 5e-6: K = 1024 114.4 ms, 1536 109.6, 2048 107.4 (max |r| error
-// 5.7e-6, 5.7e-6, 6.6e-6).  Self-join of a 2^22 noisy random walk, m = 1024:
-// K = 1024 2.45 s, 2048 2.08, 4096 1.89 (max error 4.9e-6).
-// Windows longer than 2048 allow 2 m rows (anchors then cost 1/8 of the
-// steps' FMA work, as at m = 256).
+// Rows between re-anchors of the mixed form: 32 m within [1024, 16384], and
+// at least 2 m.  Longer intervals trade anchor dots (m FP32 FMAs per diagonal
+// per interval) for exact verifications of the cells whose drift bound
+// passes the trust threshold, so the error of the reported values does not
+// grow with K.  Measured (time per join, max |r| error vs FP64):
+//   AB-join 2^20 x 2^19 random walks, m = 256: K = 2048 107.6 ms, 4096
+//     104.9, 8192 104.4, 12288 105.7 (6.6e-6 at every K);
+//   self-join of a 2^21 noisy random walk, m = 1024: K = 4096 423 ms, 8192
+//     404, 16384 396 (3.0e-6, 3.0e-6, 2.9e-6);
+//   2^21 random walk with NaN gaps, m = 4096: K = 8192 533 ms, 16384 509,
+//     32768 512 (2.6e-6, 2.5e-6, 2.5e-6);
+//   2^21 random walk, m = 128: K = 1024 447 ms, 2048 426, 4096 416; m = 64:
+//     K = 1024 601 ms, 2048 583 (3.0e-6 and 2.9e-6 at every K).
 int64_t default_anchor_interval(int64_t m) {
+  return std::min<int64_t>(std::max<int64_t>(1024, 32 * m), std::max<int64_t>(16384, 2 * m));
+}
+
+// Anchor interval of joins that start cold (batched joins: diagonal seeds
+// only, the bests still rising through the first slabs): 8 m within [1024,
+// 4096].  A longer interval widens the filter margin while many cells are
+// still near their rows' and columns' bests.  4096-series batch (lengths
+// 2^10-2^16, m in {32, 64, 128}): 1157 ms with 1024 rows for every window,
+// 1224 ms with 2048 rows for m = 64 and 128.
+int64_t cold_anchor_interval(int64_t m) {
   return std::min<int64_t>(std::max<int64_t>(4096, 2 * m), std::max<int64_t>(1024, 8 * m));
 }
 
@@ -1341,10 +1357,10 @@ struct BatchSeries {
 };
 
 // Segment length of one series of a batch: `pref` (the autotuned value for
-// its window, 0 = none) or the anchor interval, reduced for short series so
-// that a band's rows split into at least two segments.
+// its window, 0 = none) or the cold-start anchor interval, reduced for short
+// series so that a band's rows split into at least two segments.
 int64_t batch_segment(int64_t m, int64_t ns, int slab, int64_t pref) {
-  int64_t K = pref > 0 ? pref : default_anchor_interval(m);
+  int64_t K = pref > 0 ? pref : cold_anchor_interval(m);
   const int64_t half = std::max<int64_t>(slab, (ns / 2 / slab) * slab);
   K = std::min(K, half);
   const int64_t blk = int64_t{1} << block_shift(m);
@@ -1651,12 +1667,13 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
 // two segments of K rows; K is also the mixed form's anchor interval.  For
 // each window length among the series (all of them, or with `retune` = 0 the
 // ones not tuned yet), it runs the band kernel on a sample of those series
-// (in batch order, until kTuneCells comparisons) at K = the anchor-interval
-// rule's value, half and a quarter of it (never below 256 rows), twice each,
+// (in batch order, until kTuneCells comparisons) at K = the cold-start
+// anchor interval, half and a quarter of it (never below 256 rows), twice each,
 // and keeps the K with the shortest band + verification kernel time; a
 // shorter K must win by 2% to replace a longer one.  Candidates stop at the
-// rule's value because longer intervals let the FP32 recurrence drift
-// further between anchors.  The sample's profiles are scratch.
+// cold-start value: on a sample, longer intervals time within a few percent
+// of it, yet on the whole 4096-series batch they were 6% slower.  The
+// sample's profiles are scratch.
 constexpr uint64_t kTuneCells = uint64_t{1} << 34;
 
 int tune_batch(Workspace& ws, const scamp_c_args* args, int count, bool retune,
@@ -1675,7 +1692,7 @@ int tune_batch(Workspace& ws, const scamp_c_args* args, int count, bool retune,
       sa.push_back(args[k]);
       cells += diag_cells(ns, ns, m / 4, ns);
     }
-    const int64_t k_rule = default_anchor_interval(m);
+    const int64_t k_rule = cold_anchor_interval(m);
     if (sa.empty()) {
       ws.batch_seg[m] = k_rule;
       continue;

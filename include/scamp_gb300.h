@@ -162,8 +162,9 @@ int scamp_gb300_join_batch(const scamp_c_args *args, scamp_c_result *res, int co
  * among the count series (same rules as scamp_gb300_join_batch; no result
  * buffers), times the band kernel on a sample of those series at the
  * segment lengths K (rows per half-unit, also the anchor interval) of the
- * default rule, half and a quarter of it, and keeps the fastest for every
- * later batch on args[0].device.  retune = 0 skips windows already tuned.
+ * cold-start rule (8 m within [1024, 4096]), half and a quarter of it, and
+ * keeps the fastest for every later batch on args[0].device.  retune = 0
+ * skips windows already tuned.
  * segment (optional, count entries) receives the K each series will use.
  * No counterpart in the reference, which has no batched joins. */
 int scamp_gb300_tune_batch(const scamp_c_args *args, int count, int retune, int64_t *segment,

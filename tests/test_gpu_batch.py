@@ -73,19 +73,19 @@ def test_batch_graph_replay(gpu_engine):
 
 
 def test_batch_autotune(gpu_engine, oracle_mod):
-    """tune_batch picks each window's segment length among the rule's value
-    (1024 rows for these windows), half and a quarter of it, capped for
-    short series as the rule is; batches joined after tuning still match
-    the oracle."""
+    """tune_batch picks each window's segment length among the cold-start
+    anchor interval (8 m within [1024, 4096]), half and a quarter of it,
+    capped for short series as the rule is; batches joined after tuning
+    still match the oracle."""
     series, windows = _batch(21, 24)
     seg = gpu_engine.tune_batch(series, windows, retune=True)
     assert len(seg) == len(series)
-    for x, m, K in zip(series, windows, seg):
-        half = max(128, ((len(x) - m + 1) // 2 // 128) * 128)
-        assert K in {min(c, half) for c in (1024, 512, 256)}, (len(x), m, K)
     by_m = {}
     for x, m, K in zip(series, windows, seg):
-        if (len(x) - m + 1) // 2 >= 1024:
+        rule = min(max(4096, 2 * m), max(1024, 8 * m))
+        half = max(128, ((len(x) - m + 1) // 2 // 128) * 128)
+        assert K in {min(c, half) for c in (rule, rule // 2, rule // 4)}, (len(x), m, K)
+        if (len(x) - m + 1) // 2 >= rule:
             by_m.setdefault(m, set()).add(int(K))
     assert all(len(v) == 1 for v in by_m.values())  # one choice per window
     out = gpu_engine.join_batch(series, windows, precision="mixed", return_corr=True,
