@@ -46,6 +46,22 @@ def cases():
     # PROFILE_TYPE_1NN: the best correlation per window, float32, no index
     out.append(("nn_self_rw3000_m64", rw(3000), None, 64, {"profile": "1NN"}))
     out.append(("nn_ab_keep_m40", rw(2000), rw(1500), 40, {"profile": "1NN", "keep_rows": True}))
+    # distributed self-join pieces (--global_row / --global_col): aligned
+    # AB-joins of tiles of one series, W = 1500 windows each, placed at
+    # multiples of W; the trivial-match zone touches a corner of the
+    # off-diagonal tiles and runs along the main diagonal of the diagonal ones
+    x = rw(4600)
+    W, mm = 1500, 64
+    tile = lambda k: x[k * W:(k + 1) * W + mm - 1].copy()  # noqa: E731
+    out.append(("ab_dist_tile10_m64", tile(0), tile(1), mm,
+                {"aligned": True, "keep_rows": True, "start_row": W, "start_col": 0}))
+    out.append(("ab_dist_tile01_m64", tile(1), tile(0), mm,
+                {"aligned": True, "keep_rows": True, "start_row": 0, "start_col": W}))
+    out.append(("ab_dist_tile22_m64", tile(2)[:W], tile(2)[:W], mm,
+                {"aligned": True, "keep_rows": True, "start_row": 2 * W, "start_col": 2 * W}))
+    out.append(("sum_ab_dist_tile10_t06_m64", tile(0), tile(1), mm,
+                {"profile": "SUM_THRESH", "threshold": 0.6, "aligned": True, "keep_rows": True,
+                 "start_row": W, "start_col": 0}))
     return out
 
 

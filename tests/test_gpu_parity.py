@@ -232,16 +232,18 @@ def test_single_precision_is_served_by_the_mixed_form(gpu_engine, oracle_mod):
 
 @pytest.mark.parametrize("precision,tol", PRECISIONS)
 def test_distributed_offsets_1nn(gpu_engine, oracle_mod, precision, tol):
-    """1NN_INDEX with the distributed tile offsets (--global_row/col): an
-    aligned AB-join of two pieces of one series whose global positions make
-    the exclusion zone cut through the join, and an unaligned one."""
+    """1NN_INDEX with the distributed tile offsets (--global_row/col): the
+    aligned AB-joins of a self-join split into tiles of W windows at
+    multiples of W (the layout of SCAMP's distributed joins), where the
+    trivial-match zone runs along a diagonal tile's main diagonal or touches
+    an off-diagonal tile's corner."""
     rng = np.random.default_rng(72)
-    x = rw(rng, 6000)
-    a, b = x[:3500].copy(), x[1200:4400].copy()
-    run_1nn(gpu_engine, oracle_mod, a, b, 64, precision, tol, keep_rows=True, aligned=True,
-            start_row=1200, start_col=0, name="offsets/aligned")
-    run_1nn(gpu_engine, oracle_mod, a, b, 64, precision, tol, keep_rows=True,
-            start_row=1200, start_col=0, name="offsets/plain")
+    W, m = 6000, 64
+    x = rw(rng, 3 * W + m)
+    tile = lambda k: x[k * W:(k + 1) * W + m - 1].copy()  # noqa: E731
+    for r, c in ((1, 0), (0, 1), (1, 1)):
+        run_1nn(gpu_engine, oracle_mod, tile(c), tile(r), m, precision, tol, keep_rows=True,
+                aligned=True, start_row=r * W, start_col=c * W, name="tile%d%d" % (r, c))
 
 
 @pytest.mark.parametrize("precision,tol", PRECISIONS)
