@@ -187,12 +187,11 @@ Plan make_plan(const scamp_c_args* a) {
     ProblemPlan lo{0, 1, p.ns_a, p.ns_b, 1, p.ns_b, 0, 0, row_t, col_t};
     if (a->is_aligned) {
       // Trivial-match exclusion |global_col - global_row| < m/4.  The
-      // reference applies it per tile, where the zone passes through a
-      // tile's corner (src/tile.cpp:12-19, 44-138): the same cells for the
-      // layouts its distributed joins use (tiles of a self-join at
-      // multiples of the tile width).  Offsets that put the zone through a
-      // tile's interior leave the reference's trivial matches in place;
-      // here they are excluded.
+      // reference decides it per tile from the tile's corners
+      // (src/tile.cpp:12-19, 44-138): the same cells when the global
+      // offsets differ by a multiple of its tile width (the tiles of its
+      // distributed joins); for other offsets its zone is shifted or
+      // missing, depending on its tile width.
       int64_t off = 0;
       if (a->distributed_start_row >= 0 && a->distributed_start_col >= 0)
         off = a->distributed_start_col - a->distributed_start_row;
