@@ -4,7 +4,9 @@
    (test/SampleOutput/mp_*, mpi_*; tolerances of test/difference.py:24 and
    test/run_tests.sh:36) -- read where the reference tree is present.
 2. Against the reference's own CPU path compiled from its sources
-   (oracle/_ref/libscampref.so) on seeded inputs -- where it was built.
+   (oracle/_ref/libscampref.so) on seeded inputs, including 40 randomized
+   configurations of profile type, geometry and edge cases -- where it was
+   built.
 3. Against the committed fixtures tests/golden/*.npz, produced by that same
    compiled reference (tests/golden/make_golden.py) -- always.
 4. Against a brute-force compensated-dot evaluation of every cell and
@@ -93,6 +95,60 @@ def test_oracle_vs_compiled_reference(oracle_mod, case):
         # (test/test_common.py:3-16)
         mism = ok & (wi != gi)
         assert np.all(np.abs(wc[mism].astype(np.float64) - gc[mism]) <= 2.5e-7)
+
+
+def _random_case(seed):
+    """One seeded join configuration: window, lengths, self or AB, NaN and
+    flat stretches, profile type, threshold, keep_rows / columns-only /
+    aligned."""
+    rng = np.random.default_rng(seed)
+    m = int(rng.choice([3, 4, 8, 16, 33, 64]))
+    na = int(rng.integers(m, 2500))
+    ab = rng.random() < 0.6
+    nb = int(rng.integers(m, 2500)) if ab else None
+    a = np.cumsum(rng.standard_normal(na))
+    b = np.cumsum(rng.standard_normal(nb)) if ab else None
+    if rng.random() < 0.3:
+        a[rng.integers(0, na, 3)] = np.nan
+    if rng.random() < 0.2:
+        s = int(rng.integers(0, max(1, na - 50)))
+        a[s:s + 40] = 1.5
+    kw = {"profile": str(rng.choice(["1NN_INDEX", "SUM_THRESH", "1NN"]))}
+    if kw["profile"] == "SUM_THRESH":
+        kw["threshold"] = float(rng.choice([0.0, 0.3, 0.8]))
+    if rng.random() < 0.5:
+        kw["keep_rows"] = True
+    if ab and rng.random() < 0.3:
+        kw["computing_rows"] = False
+        kw.pop("keep_rows", None)
+    if ab and rng.random() < 0.25:
+        kw["aligned"] = True
+    return a, b, m, kw
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_oracle_vs_compiled_reference_randomized(oracle_mod, seed):
+    """Seeded random configurations, one reference tile (the tile-free
+    engine's semantics): same no-match pattern and values to float32
+    resolution for every profile the reference returns."""
+    if not oracle_mod.ref_available():
+        pytest.skip("reference CPU path not built here")
+    a, b, m, kw = _random_case(1000 + seed)
+    want = oracle_mod.ref_join(a, b, m, threads=1, **kw)
+    got = oracle_mod.join(a, b, m, **kw)
+    for side in ("a", "b"):
+        if "packed_" + side in want:
+            wc, _ = oracle_mod.unpack(want["packed_" + side])
+            gc, _ = oracle_mod.unpack(got["packed_" + side])
+            assert np.array_equal(wc < -1, gc < -1)
+            ok = wc >= -1
+            assert np.max(np.abs(wc[ok].astype(np.float64) - gc[ok]), initial=0.0) <= 2.5e-7
+        if "max_" + side in want:
+            w, g = want["max_" + side].astype(np.float64), got["max_" + side].astype(np.float64)
+            assert np.array_equal(w < -1, g < -1)
+            assert np.max(np.abs(w[w >= -1] - g[w >= -1]), initial=0.0) <= 2.5e-7
+        if "sum_" + side in want:
+            np.testing.assert_allclose(got["sum_" + side], want["sum_" + side], rtol=1e-6, atol=1e-6)
 
 
 @pytest.mark.parametrize("thr", [0.0, 0.5])
