@@ -6,20 +6,23 @@
 // profile enums (src/common.h:34-58), Profile/ProfileData storage of the
 // results (src/common.h:96-150, 1NN_INDEX in data[0].uint64_value with the
 // mp_entry layout, SUM_THRESH in data[0].double_value, 1NN in
-// data[0].float_value), InitProfileMemory
+// data[0].float_value, APPROX_ALL_NEIGHBORS as max_matches_per_column
+// entries per window in data[0].uint64_value, MATRIX_SUMMARY as the grid in
+// data[0].float_value), SCAMPArgs::validate / print
+// (src/common.cpp:417-436, 495-515), InitProfileMemory
 // (src/scamp_utils.cpp:226-245), do_SCAMP (src/SCAMP.h:15-18) and
-// SCAMPException for every failure (src/scamp_exception.h:7-22,
-// src/common.cpp:417-436).  Link with libscamp_gb300.so.
+// SCAMPException for every failure (src/scamp_exception.h:7-22).  Link with
+// libscamp_gb300.so.
 //
-// Only the profile types the engine computes exist here (1NN_INDEX,
-// SUM_THRESH); the experimental GPU-only types of the reference are not part
-// of this engine.
+// FREQUENCY_THRESH and 1NN_MULTIDIM, which the reference declares but does
+// not implement, are absent.
 #ifndef SCAMP_GB300_SCAMP_H
 #define SCAMP_GB300_SCAMP_H
 
 #include <cstdint>
 #include <cstring>
 #include <exception>
+#include <iostream>
 #include <string>
 #include <vector>
 
@@ -88,6 +91,12 @@ struct Profile {
 };
 
 struct SCAMPArgs {
+  // Throws SCAMPException for arguments the join rejects (the reference's
+  // checks, src/common.cpp:417-436, and this engine's own).
+  void validate() const;
+  // The fields, one per line (src/common.cpp:495-515).
+  void print() const;
+
   std::vector<double> timeseries_a;
   std::vector<double> timeseries_b;
   Profile profile_a;
@@ -142,6 +151,52 @@ inline void check(int rc, const char* msg) {
 }
 
 }  // namespace detail
+
+inline std::string GetProfileTypeString(SCAMPProfileType t) {
+  switch (t) {
+    case PROFILE_TYPE_1NN_INDEX: return "PROFILE_TYPE_1NN_INDEX";
+    case PROFILE_TYPE_SUM_THRESH: return "PROFILE_TYPE_SUM_THRESH";
+    case PROFILE_TYPE_1NN: return "PROFILE_TYPE_1NN";
+    case PROFILE_TYPE_APPROX_ALL_NEIGHBORS: return "PROFILE_TYPE_APPROX_ALL_NEIGHBORS";
+    case PROFILE_TYPE_MATRIX_SUMMARY: return "PROFILE_TYPE_MATRIX_SUMMARY";
+    default: return "PROFILE_TYPE_INVALID";
+  }
+}
+
+inline std::string GetPrecisionTypeString(SCAMPPrecisionType t) {
+  switch (t) {
+    case PRECISION_SINGLE: return "PRECISION_SINGLE";
+    case PRECISION_MIXED: return "PRECISION_MIXED";
+    case PRECISION_DOUBLE: return "PRECISION_DOUBLE";
+    case PRECISION_ULTRA: return "PRECISION_ULTRA";
+    default: return "PRECISION_INVALID";
+  }
+}
+
+inline void SCAMPArgs::validate() const {
+  char msg[512] = {0};
+  const scamp_c_args c = detail::to_c(*this);
+  detail::check(scamp_gb300_validate(&c, msg, sizeof msg), msg);
+}
+
+inline void SCAMPArgs::print() const {
+  std::cout << "window: " << window << std::endl;
+  std::cout << "max_tile_size: " << max_tile_size << std::endl;
+  std::cout << "has_b: " << has_b << std::endl;
+  std::cout << "keep_rows_separate: " << keep_rows_separate << std::endl;
+  std::cout << "distributed_start_row: " << distributed_start_row << std::endl;
+  std::cout << "distributed_start_col: " << distributed_start_col << std::endl;
+  std::cout << "computing_rows: " << computing_rows << std::endl;
+  std::cout << "computing_columns: " << computing_columns << std::endl;
+  std::cout << "is_aligned: " << is_aligned << std::endl;
+  std::cout << "profile_type: " << GetProfileTypeString(profile_type) << std::endl;
+  std::cout << "precision_type: " << GetPrecisionTypeString(precision_type) << std::endl;
+  std::cout << "distance_threshold: " << distance_threshold << std::endl;
+  std::cout << "silent_mode: " << silent_mode << std::endl;
+  std::cout << "max_matches_per_column: " << max_matches_per_column << std::endl;
+  std::cout << "timeseries_a size: " << timeseries_a.size() << std::endl;
+  std::cout << "timeseries_b size: " << timeseries_b.size() << std::endl;
+}
 
 // Allocates and initialises the profiles the join writes (the caller calls it
 // before do_SCAMP, as with the reference).  Returns false for a window longer

@@ -31,6 +31,23 @@ int main(int argc, char** argv) {
     a.timeseries_a.assign(100, 1.0);
     a.window = 200;  // longer than the series
     bad += expect_throw(a, "window");
+    // SCAMPArgs::validate checks without running anything
+    try {
+      a.validate();
+      std::cout << "validate: no exception\n";
+      bad += 1;
+    } catch (const SCAMPException& e) {
+      std::cout << "validate: " << e.what() << "\n";
+    }
+    a.window = 2;
+    try {
+      a.validate();
+      bad += 1;
+    } catch (const SCAMPException& e) {
+      std::cout << "validate: " << e.what() << "\n";
+    }
+    a.window = 200;
+    a.print();
     if (SCAMP::InitProfileMemory(&a)) bad += 1;  // must refuse
     a.window = 10;
     a.precision_type = SCAMP::PRECISION_INVALID;
