@@ -88,6 +88,8 @@ struct Profile {
 
   std::vector<ProfileData> data;
   SCAMPProfileType type;
+  // APPROX_ALL_NEIGHBORS: entries per window (max_matches_per_column)
+  int64_t matches_per_window = 1;
 };
 
 struct SCAMPArgs {
@@ -215,8 +217,11 @@ inline bool InitProfileMemory(SCAMPArgs* args) {
     return true;
   }
   args->profile_a = Profile(args->profile_type, static_cast<size_t>(na * per));
-  if (args->keep_rows_separate)
+  args->profile_a.matches_per_window = per;
+  if (args->keep_rows_separate) {
     args->profile_b = Profile(args->profile_type, static_cast<size_t>(nb * per));
+    args->profile_b.matches_per_window = per;
+  }
   return true;
 }
 

@@ -35,6 +35,56 @@ def test_shim_errors(tmp_path):
     assert out.stdout.strip().endswith("OK")
 
 
+def test_shim_utils_match_the_cli_writers(tmp_path):
+    """scamp/scamp_utils.h (the reference's utility functions for callers
+    of do_SCAMP) reads series and writes every profile type exactly as the
+    Python command line does, with and without output_pearson."""
+    import scamp_gb300
+    from scamp_gb300 import cli
+
+    exe = _build(tmp_path)
+    rng = np.random.default_rng(4)
+    m, k, h, w = 16, 3, 4, 5
+    corr = rng.uniform(-1, 1, 40).astype(np.float32)
+    corr[[3, 17]] = -2.0
+    idx = rng.integers(0, 1000, 40).astype(np.uint64)
+    idx[[3, 17]] = 0xFFFFFFFF
+    packed = (idx << np.uint64(32)) | corr.view(np.uint32).astype(np.uint64)
+    packed.tofile(tmp_path / "nn_index.bin")
+    corr.tofile(tmp_path / "nn.bin")
+    sums = rng.uniform(0, 50, 40)
+    sums.tofile(tmp_path / "sum.bin")
+    knn = packed[:36].copy()  # 12 windows x 3 entries
+    knn.tofile(tmp_path / "knn.bin")
+    mat = rng.uniform(-1, 1, h * w).astype(np.float32)
+    mat[7] = -2.0
+    mat.tofile(tmp_path / "matrix.bin")
+    series = "1.5\n-2e3\n0.25\n  7\n\n3.125\n9"  # last value: no newline after it
+    (tmp_path / "in.txt").write_text(series)
+    out = subprocess.run([exe, "utils", str(tmp_path)], capture_output=True, text=True,
+                         timeout=120)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert out.stdout.strip().startswith("OK")
+    got = np.fromfile(tmp_path / "read.bin", dtype=np.float64)
+    assert np.array_equal(got, np.array(cli.read_series(str(tmp_path / "in.txt"))))
+    assert len(got) == 5
+    py = tmp_path / "py"
+    py.mkdir()
+    for pearson in (False, True):
+        s = "_pearson" if pearson else ""
+        cli.write_profile(str(py / "a.txt"), str(py / "ai.txt"), packed, pearson, m)
+        cli.write_max_profile(str(py / "b.txt"), corr, pearson, m)
+        cli.write_knn(str(py / "c.txt"), knn, k, pearson, m)
+        cli.write_matrix(str(py / "d.txt"), mat.reshape(h, w), pearson, m)
+        for mine, theirs in (("a", "out_nn_index"), ("ai", "out_nn_index_i"), ("b", "out_nn"),
+                             ("c", "out_knn"), ("d", "out_matrix")):
+            assert (py / (mine + ".txt")).read_text() == \
+                (tmp_path / (theirs + s + ".txt")).read_text(), (mine, pearson)
+    cli.write_sums(str(py / "e.txt"), sums)
+    assert (py / "e.txt").read_text() == (tmp_path / "out_sum.txt").read_text()
+    assert scamp_gb300.NO_MATCH  # the package imported (engine library present)
+
+
 @pytest.mark.gpu
 def test_shim_selfjoin_matches_python(tmp_path, gpu_engine):
     import scamp_gb300
