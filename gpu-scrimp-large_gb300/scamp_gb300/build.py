@@ -1,4 +1,5 @@
-"""Builds libscamp_gb300.so in-tree with nvcc for sm_103a only.
+"""Builds libscamp_gb300.so in-tree with nvcc for sm_103a only, and the
+command-line program ``scamp_gb300/scamp`` over it.
 
 Translation units compile in parallel into ``gpu-scrimp-large_gb300/_build``
 and link into ``scamp_gb300/libscamp_gb300.so``.  Usage:
@@ -18,6 +19,8 @@ CSRC = os.path.join(ROOT, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG_DIR, "libscamp_gb300.so")
+CLI_SRC = os.path.join(ROOT, "cli", "scamp_main.cpp")
+CLI = os.path.join(PKG_DIR, "scamp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -71,6 +74,11 @@ def build(verbose=False, ptxas_verbose=False):
     tmp = LIB + ".tmp"
     _compile([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
     os.replace(tmp, LIB)
+    # the command-line program (the reference's src/main.cpp) over the library
+    tmp = CLI + ".tmp"
+    _compile([cxx, "-O2", "-std=c++17", "-I" + INCLUDE, CLI_SRC, "-o", tmp, "-L" + PKG_DIR,
+              "-lscamp_gb300", "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, CLI)
     return LIB
 
 

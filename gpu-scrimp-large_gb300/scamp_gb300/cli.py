@@ -20,6 +20,8 @@ Flags of the reference that select other machinery (distributed execution,
 CPU workers) are accepted and ignored, except --no_gpu, which this engine
 cannot honour (it has no CPU path).
 """
+import ctypes
+import errno
 import math
 import sys
 
@@ -98,37 +100,60 @@ def parse_flags(argv):
     return vals
 
 
+_STRTOD = None
+
+
+def _strtod(tok):
+    """C strtod on one token, as the reference's std::stod parses it:
+    (value, characters used, out of range)."""
+    global _STRTOD
+    if _STRTOD is None:
+        libc = ctypes.CDLL(None, use_errno=True)
+        fn = libc.strtod
+        fn.restype = ctypes.c_double
+        fn.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p)]
+        _STRTOD = fn
+    buf = ctypes.create_string_buffer(tok)
+    endp = ctypes.c_char_p()
+    ctypes.set_errno(0)
+    val = _STRTOD(buf, ctypes.byref(endp))
+    err = ctypes.get_errno()
+    used = ctypes.cast(endp, ctypes.c_void_p).value - ctypes.addressof(buf)
+    return val, used, err == errno.ERANGE
+
+
 def read_series(path):
-    """The reference's readFile: whitespace-separated numbers; a token that
-    does not parse is a fatal error.  Like the reference, a value is kept only
-    when more input follows it, so the last value of a file without a
-    trailing newline is dropped."""
+    """The reference's readFile (src/scamp_utils.cpp:30-72): whitespace-
+    separated numbers, each parsed as std::stod does (the longest numeric
+    prefix of the token); a token with no number, or one out of range, is a
+    fatal error that names its first character and its line.  Like the
+    reference, a value is kept only when more input follows it, so the last
+    value of a file without a trailing newline is dropped."""
     try:
-        text = open(path).read()
+        with open(path, "rb") as f:
+            text = f.read()
     except OSError:
         raise UsageError("Unable to open%sfor reading, please make sure it exists" % path)
     out = []
     pos, n = 0, len(text)
-    count = 0
     while True:
-        while pos < n and text[pos].isspace():
+        while pos < n and text[pos:pos + 1].isspace():
             pos += 1
         if pos >= n:
             break
         end = pos
-        while end < n and not text[end].isspace():
+        while end < n and not text[end:end + 1].isspace():
             end += 1
         tok = text[pos:end]
-        try:
-            val = float(tok)
-        except ValueError:
-            raise UsageError("FATAL ERROR: invalid argument: Could not parse line number %d "
-                             "from input file." % (count + 1))
+        val, used, out_of_range = _strtod(tok)
+        if used == 0 or out_of_range:
+            raise UsageError("%s\nFATAL ERROR: %s: Could not parse line number %d from input file."
+                             % (tok[:1].decode("latin-1"),
+                                "out of range" if used else "invalid argument", len(out) + 1))
         pos = end
         if pos >= n:  # nothing follows the value
             break
         out.append(val)
-        count += 1
     return np.asarray(out, dtype=np.float64)
 
 

@@ -153,3 +153,115 @@ def test_cli_all_neighbors_and_matrix(gpu_engine, tmp_path):
     assert got.shape == (4, 6)
     want = np.where(r["matrix"] < -1, np.nan, r["matrix"])
     np.testing.assert_allclose(got, want, atol=1e-6)
+
+
+# ---------------------------------------------------------------------------
+# The native command-line program (scamp_gb300/scamp, built from
+# gpu-scrimp-large_gb300/cli/scamp_main.cpp) behaves as the Python one.
+# ---------------------------------------------------------------------------
+def _native():
+    from conftest import PKG_DIR
+
+    exe = os.path.join(PKG_DIR, "scamp")
+    if not os.path.exists(exe):
+        pytest.skip("native command line not built")
+    return exe
+
+
+def _both(argv, capsys):
+    import subprocess
+
+    rc_py = cli.main(list(argv))
+    out_py = capsys.readouterr().out
+    p = subprocess.run([_native()] + list(argv), capture_output=True, text=True, timeout=120)
+    return (rc_py, out_py), (p.returncode, p.stdout)
+
+
+def test_read_series_tokens_as_the_reference(tmp_path):
+    """Tokens parse as std::stod does: the longest numeric prefix, hex and
+    inf/nan forms; no number, or one out of range, is fatal."""
+    p = tmp_path / "x.txt"
+    p.write_text("1.5\n2x\n0x10\ninf\n-nan\n3e2\n7\n")
+    x = cli.read_series(str(p))
+    assert x[:4].tolist() == [1.5, 2.0, 16.0, float("inf")] and np.isnan(x[4])
+    assert x[5:].tolist() == [300.0, 7.0]
+    for text, what in (("1\nabc\n2\n", "a\nFATAL ERROR: invalid argument: Could not parse "
+                        "line number 2"),
+                       ("1\n1e400\n2\n", "1\nFATAL ERROR: out of range: Could not parse "
+                        "line number 2")):
+        p.write_text(text)
+        with pytest.raises(cli.UsageError, match=what):
+            cli.read_series(str(p))
+
+
+@pytest.mark.parametrize("argv", [
+    ["--window=2", "--input_a_file_name=x"],
+    ["--window=10"],
+    ["--window=10", "--input_a_file_name=x", "--mixed_precision", "--double_precision"],
+    ["--window=10", "--max_tile_size=100", "--input_a_file_name=x"],
+    ["--window=10", "--max_tile_size=1024", "--input_a_file_name=x", "--window=600"],
+    ["--window=abc"],
+    ["--threshold=0.5x"],
+    ["--no_such_flag=1"],
+    ["--window"],
+    ["stray"],
+    ["--window=10", "--input_a_file_name=x", "--no_gpu"],
+    ["--window=10", "--input_a_file_name=x", "--profile_type=FREQUENCY_THRESH"],
+    ["--window=10", "--input_a_file_name=/nonexistent/a.txt"],
+])
+def test_native_cli_errors_match_python(capsys, argv):
+    (rc_py, out_py), (rc_c, out_c) = _both(argv, capsys)
+    assert rc_py == rc_c == 1
+    assert out_py == out_c
+
+
+def test_native_cli_input_errors_match_python(capsys, tmp_path):
+    f = tmp_path / "a.txt"
+    for text in ("1\n2\nabc\n3\n", "1\n1e999\n2\n", "1\n2\n3"):
+        f.write_text(text)
+        (rc_py, out_py), (rc_c, out_c) = _both(["--window=3", "--input_a_file_name=%s" % f],
+                                                capsys)
+        assert rc_py == rc_c == 1
+        assert out_py == out_c
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("extra", [
+    [],
+    ["--keep_rows", "--output_pearson"],
+    ["--profile_type=SUM_THRESH", "--threshold=0.6", "--keep_rows"],
+    ["--profile_type=1NN", "--keep_rows"],
+    ["--profile_type=ALL_NEIGHBORS", "--max_matches_per_column=3", "--keep_rows"],
+    ["--profile_type=MATRIX_SUMMARY", "--reduced_height=5", "--reduced_width=7"],
+])
+def test_native_cli_files_match_python(gpu_engine, capsys, tmp_path, extra):
+    """Same flags, same FP64 join: byte-identical output files (sums, whose
+    FP64 atomic additions run in any order, to 1e-12)."""
+    import subprocess
+
+    rng = np.random.default_rng(8)
+    fa, fb = tmp_path / "a.txt", tmp_path / "b.txt"
+    fa.write_text("".join(repr(float(v)) + "\n" for v in np.cumsum(rng.standard_normal(2500))))
+    fb.write_text("".join(repr(float(v)) + "\n" for v in np.cumsum(rng.standard_normal(1800))))
+    outs = {}
+    for who in ("py", "c"):
+        d = tmp_path / who
+        d.mkdir()
+        argv = ["--window=48", "--input_a_file_name=%s" % fa, "--input_b_file_name=%s" % fb,
+                "--double_precision"] + extra + [
+            "--output_a_file_name=%s" % (d / "ma"), "--output_a_index_file_name=%s" % (d / "ia"),
+            "--output_b_file_name=%s" % (d / "mb"), "--output_b_index_file_name=%s" % (d / "ib")]
+        if who == "py":
+            assert cli.main(argv) == 0
+        else:
+            p = subprocess.run([_native()] + argv, capture_output=True, text=True, timeout=300)
+            assert p.returncode == 0, p.stdout + p.stderr
+        outs[who] = {f: (d / f).read_bytes() for f in sorted(os.listdir(d))}
+    assert outs["py"].keys() == outs["c"].keys() and outs["py"]
+    for f in outs["py"]:
+        if "SUM_THRESH" in " ".join(extra):
+            a = np.array(outs["py"][f].split(), dtype=np.float64)
+            b = np.array(outs["c"][f].split(), dtype=np.float64)
+            np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-12)
+        else:
+            assert outs["py"][f] == outs["c"][f], f
