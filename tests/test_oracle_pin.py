@@ -59,6 +59,35 @@ def test_oracle_vs_reference_goldens_abjoin(oracle_mod, na, nb):
     assert np.sum(i != gi) <= len(gi) // 100
 
 
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
+def test_oracle_aligned_self_as_ab_vs_reference_golden(oracle_mod):
+    """test/run_tests.sh:49-77: an aligned AB-join of a series with itself
+    reproduces its self-join golden."""
+    a = np.loadtxt(os.path.join(REF, "SampleInput", "randomwalk8K.txt"))
+    gd = np.loadtxt(os.path.join(REF, "SampleOutput", "mp_randomwalk8K_w100.txt"))
+    gi = np.loadtxt(os.path.join(REF, "SampleOutput", "mpi_randomwalk8K_w100.txt")).astype(np.int64)
+    d, i = _distance(oracle_mod, oracle_mod.join(a, a.copy(), 100, aligned=True,
+                                                 computing_rows=False)["packed_a"], 100)
+    assert np.max(np.abs(d - gd)) <= 1e-5
+    assert np.sum(i != gi) <= len(gi) // 100
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
+def test_oracle_keep_rows_global_offsets_vs_reference_goldens(oracle_mod):
+    """test/run_tests.sh:137-206: an AB-join with keep_rows and global
+    offsets (not aligned, so they change nothing) reproduces both
+    directions' goldens."""
+    a = np.loadtxt(os.path.join(REF, "SampleInput", "randomwalk32K.txt"))
+    b = np.loadtxt(os.path.join(REF, "SampleInput", "randomwalk16K.txt"))
+    r = oracle_mod.join(a, b, 100, keep_rows=True, start_row=9000000000, start_col=100000)
+    for side, name in (("a", "randomwalk32K_randomwalk16K"), ("b", "randomwalk16K_randomwalk32K")):
+        gd = np.loadtxt(os.path.join(REF, "SampleOutput", "mp_%s_w100.txt" % name))
+        gi = np.loadtxt(os.path.join(REF, "SampleOutput", "mpi_%s_w100.txt" % name)).astype(np.int64)
+        d, i = _distance(oracle_mod, r["packed_" + side], 100)
+        assert np.max(np.abs(d - gd)) <= 1e-5, side
+        assert np.sum(i != gi) <= len(gi) // 100, side
+
+
 def _ref_cases():
     rng = np.random.default_rng(99)
     cases = []
