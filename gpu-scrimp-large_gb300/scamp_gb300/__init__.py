@@ -41,6 +41,7 @@ NO_MATCH = np.uint64((0xFFFFFFFF << 32) | int(np.float32(-2.0).view(np.uint32)))
 
 
 def version():
+    """The engine library's version string."""
     return _lib.load().scamp_gb300_version().decode()
 
 
@@ -83,7 +84,9 @@ def _args(a, b, m, profile, precision, computing_rows, computing_cols,
 
 
 def count_cells(len_a, m, len_b=None, aligned=False, start_row=-1, start_col=-1):
-    """Distance-matrix cells a join evaluates (host logic, no GPU needed)."""
+    """Distance-matrix cells a join evaluates (host logic, no GPU needed):
+    the comparisons of the comparisons/s metric, with the reference's
+    exclusion zones (src/tile.cpp:12-138)."""
     lib = _lib.load()
     a = np.zeros(1)
     ca = _args(None, None, m, "1NN_INDEX", "double", True, True, False, aligned,
@@ -121,7 +124,9 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
          max_tile_size=128000, anchor_interval=0, device=0, profile_a=None,
          profile_b=None, return_corr=False, silent=True, inplace=False, max_matches=5,
          matrix_height=50, matrix_width=50):
-    """Run one join (the C ABI's scamp_gb300_join, host buffers).
+    """Run one join (the C ABI's scamp_gb300_join, host buffers; the
+    reference's SCAMP::do_SCAMP, src/SCAMP.cpp:261-334, with the arguments
+    of SCAMPArgs, src/common.h:164-188).
 
     For 1NN_INDEX returns ``profile_a`` (and ``profile_b`` with keep_rows) as
     uint64 arrays in the reference's packed layout; ``profile_a`` /
@@ -335,8 +340,8 @@ def join_batch(series, windows, precision="mixed", return_corr=False, device=0,
 
 
 def unpack_profile(packed):
-    """(float32 correlation, int64 index) from packed 1NN_INDEX entries;
-    index -1 where there was no match."""
+    """(float32 correlation, int64 index) from packed 1NN_INDEX entries
+    (mp_entry, src/common.h:70-74); index -1 where there was no match."""
     packed = np.asarray(packed, dtype=np.uint64)
     corr = (packed & np.uint64(0xFFFFFFFF)).astype(np.uint32).view(np.float32)
     idx = (packed >> np.uint64(32)).astype(np.int64)
@@ -439,8 +444,9 @@ def _parse_matrix_kwargs(kwargs):
 
 def selfjoin_knn(a, m, k, **kwargs):
     """The ``k`` best matches above ``threshold`` (default 0) of every window
-    of ``a``: a list of (column, row, value) tuples (pyscamp.selfjoin_knn).
-    These are the exact k best; the reference's lists are approximate."""
+    of ``a``: a list of (column, row, value) tuples (pyscamp.selfjoin_knn,
+    python/SCAMP_python.cpp:239-259, 475-490).  These are the exact k best;
+    the reference's lists are approximate."""
     o = _parse_kwargs(kwargs, _KNN_KEYS)
     r = join(np.asarray(a, dtype=np.float64), None, int(m), "ALL_NEIGHBORS", o["precision"],
              computing_rows=True, computing_cols=True, threshold=o["threshold"],
@@ -450,7 +456,8 @@ def selfjoin_knn(a, m, k, **kwargs):
 
 def abjoin_knn(a, b, m, k, **kwargs):
     """For every window of ``a``, its ``k`` best matches in ``b`` above
-    ``threshold`` (pyscamp.abjoin_knn)."""
+    ``threshold`` (pyscamp.abjoin_knn, python/SCAMP_python.cpp:261-280,
+    491-508)."""
     o = _parse_kwargs(kwargs, _KNN_KEYS)
     r = join(np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64), int(m),
              "ALL_NEIGHBORS", o["precision"], computing_rows=False, computing_cols=True,
@@ -462,7 +469,8 @@ def abjoin_knn(a, b, m, k, **kwargs):
 def selfjoin_matrix(a, m, **kwargs):
     """An (mheight, mwidth) summary of the self-join's distance matrix, each
     entry the best match above ``threshold`` in its block (pyscamp
-    .selfjoin_matrix); distances, or correlations with pearson=True."""
+    .selfjoin_matrix, python/SCAMP_python.cpp:320-339, 509-526); distances,
+    or correlations with pearson=True."""
     o = _parse_matrix_kwargs(kwargs)
     r = join(np.asarray(a, dtype=np.float64), None, int(m), "MATRIX_SUMMARY", o["precision"],
              threshold=o["threshold"], silent=o["silent"], device=o["device"],
@@ -472,7 +480,8 @@ def selfjoin_matrix(a, m, **kwargs):
 
 def abjoin_matrix(a, b, m, **kwargs):
     """An (mheight, mwidth) summary of the AB-join's distance matrix (rows:
-    windows of b, columns: windows of a) (pyscamp.abjoin_matrix)."""
+    windows of b, columns: windows of a) (pyscamp.abjoin_matrix,
+    python/SCAMP_python.cpp:341-361, 527-548)."""
     o = _parse_matrix_kwargs(kwargs)
     r = join(np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64), int(m),
              "MATRIX_SUMMARY", o["precision"], computing_rows=False, computing_cols=True,
@@ -495,7 +504,8 @@ def _split_1nn(packed, pearson, m):
 
 def selfjoin(a, m, **kwargs):
     """Matrix profile of series ``a`` with window ``m``: (distances float32,
-    indices int32).  Same contract as pyscamp.selfjoin."""
+    indices int32).  Same contract as pyscamp.selfjoin
+    (python/SCAMP_python.cpp:196-217, 420-430)."""
     o = _parse_kwargs(kwargs, _NN_KEYS)
     r = join(np.asarray(a, dtype=np.float64), None, int(m), "1NN_INDEX", o["precision"],
              computing_rows=True, computing_cols=True, silent=o["silent"], device=o["device"])
@@ -504,7 +514,8 @@ def selfjoin(a, m, **kwargs):
 
 def abjoin(a, b, m, **kwargs):
     """For each window of ``a``, its nearest neighbour in ``b``: (distances
-    float32, indices into b int32).  Same contract as pyscamp.abjoin."""
+    float32, indices into b int32).  Same contract as pyscamp.abjoin
+    (python/SCAMP_python.cpp:219-237, 431-444)."""
     o = _parse_kwargs(kwargs, _NN_KEYS)
     r = join(np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64), int(m),
              "1NN_INDEX", o["precision"], computing_rows=False, computing_cols=True,
@@ -522,7 +533,8 @@ def _sum_out(v):
 
 def selfjoin_sum(a, m, **kwargs):
     """Per window of ``a``, the sum of correlations above ``threshold``
-    (default 0) to the other windows of ``a`` (pyscamp.selfjoin_sum)."""
+    (default 0) to the other windows of ``a`` (pyscamp.selfjoin_sum,
+    python/SCAMP_python.cpp:282-299, 445-458)."""
     o = _parse_kwargs(kwargs, _SUM_KEYS)
     r = join(np.asarray(a, dtype=np.float64), None, int(m), "SUM_THRESH", o["precision"],
              computing_rows=True, computing_cols=True, threshold=o["threshold"],
@@ -532,7 +544,8 @@ def selfjoin_sum(a, m, **kwargs):
 
 def abjoin_sum(a, b, m, **kwargs):
     """Per window of ``a``, the sum of correlations above ``threshold`` to the
-    windows of ``b`` (pyscamp.abjoin_sum)."""
+    windows of ``b`` (pyscamp.abjoin_sum, python/SCAMP_python.cpp:301-318,
+    459-474)."""
     o = _parse_kwargs(kwargs, _SUM_KEYS)
     r = join(np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64), int(m),
              "SUM_THRESH", o["precision"], computing_rows=False, computing_cols=True,
