@@ -19,7 +19,7 @@ import os
 import numpy as np
 import pytest
 
-from parity import pair_corr
+from parity import check_sum, pair_corr
 
 REF = "/root/reference/test"
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -86,6 +86,38 @@ def test_oracle_keep_rows_global_offsets_vs_reference_goldens(oracle_mod):
         d, i = _distance(oracle_mod, r["packed_" + side], 100)
         assert np.max(np.abs(d - gd)) <= 1e-5, side
         assert np.sum(i != gi) <= len(gi) // 100, side
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
+@pytest.mark.parametrize("name", ["poorly_conditioned_test", "randomwalk1K_nan"])
+def test_oracle_vs_compiled_reference_static_inputs(oracle_mod, name):
+    """test/run_tests.py:12-17: the static inputs (a quantized, poorly
+    conditioned series and a walk with NaN samples) at every window the
+    reference tests, 1NN_INDEX and SUM_THRESH at its thresholds, against
+    the reference's compiled CPU path: the same values at float32
+    resolution and NaN pattern; index differences only at float32 ties;
+    sums equal up to whole multiples of the threshold (cells whose r is the
+    threshold itself, frequent in quantized data, fall on either side by
+    one rounding: the reference's own rule, test/test_common.py:25-49)."""
+    if not oracle_mod.ref_available():
+        pytest.skip("reference CPU path not built here")
+    x = np.loadtxt(os.path.join(REF, "SampleInput", name + ".txt"))
+    for m in (5, 7, 13, 25, 33, 78, 92, 100, 189, 339, 500):
+        if m > len(x) // 2:
+            continue
+        want = oracle_mod.ref_join(x, None, m, threads=2)
+        got = oracle_mod.join(x, None, m)
+        wc, wi = oracle_mod.unpack(want["packed_a"])
+        gc, gi = oracle_mod.unpack(got["packed_a"])
+        assert np.array_equal(wc < -1, gc < -1), m
+        ok = wc >= -1
+        assert np.max(np.abs(wc[ok].astype(np.float64) - gc[ok]), initial=0.0) <= 2.5e-7, m
+        mism = ok & (wi != gi)
+        assert np.all(np.abs(wc[mism].astype(np.float64) - gc[mism]) <= 2.5e-7), m
+        for thr in (0.0, 0.125, 0.5):
+            ws = oracle_mod.ref_join(x, None, m, profile="SUM_THRESH", threshold=thr, threads=2)
+            gs = oracle_mod.join(x, None, m, profile="SUM_THRESH", threshold=thr)
+            check_sum("%s m=%d thr=%g" % (name, m, thr), gs["sum_a"], ws["sum_a"], thr, 1e-6)
 
 
 def _ref_cases():
