@@ -265,3 +265,54 @@ def test_native_cli_files_match_python(gpu_engine, capsys, tmp_path, extra):
             np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-12)
         else:
             assert outs["py"][f] == outs["c"][f], f
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_native_cli_matches_python_randomized(capsys, tmp_path, seed):
+    """Seeded random command lines (valid and invalid flags and values,
+    gflags spellings, inputs good and bad): without a GPU every run ends in
+    a message, and the two programs print the same one with the same exit
+    status."""
+    from scamp_gb300 import gpu_supported
+
+    if gpu_supported():
+        pytest.skip("compares the paths that end before the join")
+    rng = np.random.default_rng(seed)
+    good = tmp_path / "good.txt"
+    good.write_text("".join("%r\n" % float(v) for v in np.cumsum(rng.standard_normal(300))))
+    short = tmp_path / "short.txt"
+    short.write_text("1\n2\n3\n")
+    bad = tmp_path / "bad.txt"
+    bad.write_text("1\n2\nzz\n")
+    values = {
+        "window": ["10", "2", "abc", "600", "-5", " 12"],
+        "max_tile_size": ["1024", "100", "131072", "1e3"],
+        "threshold": ["0.5", "x", "-0.25", "1e-3"],
+        "profile_type": ["1NN_INDEX", "SUM_THRESH", "1NN", "ALL_NEIGHBORS", "MATRIX_SUMMARY",
+                         "KNN"],
+        "input_a_file_name": [str(good), str(short), str(bad), str(tmp_path / "missing.txt")],
+        "input_b_file_name": [str(good), str(bad)],
+        "global_row": ["5", "q"],
+        "reduced_height": ["4", "0"],
+        "gpus": ["0", ""],
+    }
+    bools = ["keep_rows", "aligned", "output_pearson", "mixed_precision", "double_precision",
+             "ultra_precision", "no_gpu"]
+    argv = []
+    if rng.random() < 0.8:
+        argv.append("--window=%d" % rng.choice([10, 24]))
+    if rng.random() < 0.7:
+        argv.append("--input_a_file_name=%s" % good)
+    for _ in range(int(rng.integers(0, 6))):
+        r = rng.random()
+        if r < 0.6:
+            name = str(rng.choice(list(values)))
+            val = str(rng.choice(values[name]))
+            argv += (["--%s=%s" % (name, val)] if rng.random() < 0.7 else ["--" + name, val])
+        elif r < 0.9:
+            name = str(rng.choice(bools))
+            argv.append(str(rng.choice(["--%s", "--no%s", "--%s=false", "-%s"])) % name)
+        else:
+            argv.append(str(rng.choice(["--bogus=1", "stray"])))
+    (rc_py, out_py), (rc_c, out_c) = _both(argv, capsys)
+    assert (rc_py, out_py) == (rc_c, out_c), argv
