@@ -152,22 +152,38 @@ def make_workload(na=None, nb=None):
     return workloads.cfg2_abjoin(na=na or NA, nb=nb or NB, m=M)
 
 
-def run_reference(args, world, rank):
-    """CPU path of the reference (oracle restatement), bounded sample."""
-    if rank != 0:
-        return
+def _cpu_join():
+    """The CPU join the reference arm and the baseline leg time: the
+    reference's own CPU path compiled from its sources (oracle/_ref) where it
+    was built on this machine, else the oracle's restatement of it.
+    Returns (join(a, b, m, threads), kind)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
 
     oracle.load()
+    if oracle.ref_available():
+        return (lambda a, b, m, threads: oracle.ref_join(a, b, m, keep_rows=b is not None,
+                                                         threads=threads)), "reference"
+    return (lambda a, b, m, threads: oracle.join(a, b, m, keep_rows=b is not None,
+                                                 threads=threads)), "port"
+
+
+def run_reference(args, world, rank):
+    """CPU path of the reference (its compiled sources where built here, else
+    the oracle restatement), bounded sample."""
+    if rank != 0:
+        return
+    cpu_join, kind = _cpu_join()
+    import oracle  # on sys.path once _cpu_join has run
+
     a, b, cells, sample = cpu_sample()
     m = M if WORKLOAD_KIND == "ab" else SELF_M
     threads = oracle.max_threads()
     for _ in range(args.warmup):
-        oracle.join(a, b, m, keep_rows=b is not None, threads=threads)
+        cpu_join(a, b, m, threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        oracle.join(a, b, m, keep_rows=b is not None, threads=threads)
+        cpu_join(a, b, m, threads)
     dt = (time.perf_counter() - t0) / args.steps
     value = cells / dt
     line = {
@@ -178,7 +194,7 @@ def run_reference(args, world, rank):
         "config": {"workload": WORKLOAD if WORKLOAD_KIND == "ab" else SELF_WORKLOAD,
                    "sample": sample},
         "cpu_baseline": {"value": value, "unit": "comparisons/s", "cores": threads,
-                         "kind": "port", "sample": sample},
+                         "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": "comparisons/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -201,17 +217,16 @@ def cpu_sample():
 
 
 def cpu_baseline_leg():
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle
+    cpu_join, kind = _cpu_join()
+    import oracle  # on sys.path once _cpu_join has run
 
-    oracle.load()
     a, b, cells, sample = cpu_sample()
     m = M if WORKLOAD_KIND == "ab" else SELF_M
     threads = oracle.max_threads()
     t0 = time.perf_counter()
-    oracle.join(a, b, m, keep_rows=b is not None, threads=threads)
+    cpu_join(a, b, m, threads)
     dt = time.perf_counter() - t0
-    return {"value": cells / dt, "unit": "comparisons/s", "cores": threads, "kind": "port",
+    return {"value": cells / dt, "unit": "comparisons/s", "cores": threads, "kind": kind,
             "sample": sample + ", %.1f s" % dt}
 
 
