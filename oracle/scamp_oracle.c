@@ -311,7 +311,62 @@ static void do_strip(const band_t *bd, int64_t d0, int64_t d1, int64_t m,
     cov[s] = brute ? 0 : seed_cov(bd->Tr, bd->Tc, bd->mu_r, bd->mu_c, d0 + s, m);
   int64_t rows = bd->n_c - d0;
   if (rows > bd->n_r) rows = bd->n_r;
-  for (int64_t i = 0; i < rows; ++i) {
+  int64_t i = 0;
+  /* Full-width rows of a strip clear of the excluded diagonals: the same
+   * arithmetic in loops of constant length, which the compiler vectorises
+   * (the reference's unrolled fast case, src/cpu_kernels.cpp:139-172). */
+  if (!brute && nd == STRIP && !(bd->x_lo < d1 && bd->x_hi > d0)) {
+    int64_t fast = bd->n_c - d1 + 1; /* rows where every diagonal is inside */
+    if (fast > rows) fast = rows;
+    for (; i < fast; ++i) {
+      const double ir = bd->in_r[i];
+      const double *inc = bd->in_c + i + d0;
+      const double *dfc = bd->df_c + i + d0;
+      const double *dgc = bd->dg_c + i + d0;
+      for (int s = 0; s < STRIP; ++s) r[s] = cov[s] * inc[s] * ir;
+      if (ptype == ORACLE_PROFILE_1NN_INDEX) {
+        if (pc)
+          for (int s = 0; s < STRIP; ++s) upd_max(pc, i + d0 + s, r[s], i);
+        if (pr) {
+          double best = -2;
+          int64_t bj = -1;
+          for (int s = 0; s < STRIP; ++s) {
+            const double v = r[s], b = cb[s];
+            const int64_t x = ci[s];
+            const int take = (v > b) | ((v == b) & (i < x));
+            cb[s] = take ? v : b;
+            ci[s] = take ? i : x;
+          }
+        }
+        if (pr) {
+          double best = -2;
+          int64_t bj = -1;
+          for (int s = 0; s < STRIP; ++s)
+            if (r[s] > best) {
+              best = r[s];
+              bj = i + d0 + s;
+            }
+          if (bj >= 0) upd_max(pr, i, best, bj);
+        }
+      } else {
+        if (pc)
+          for (int s = 0; s < STRIP; ++s)
+            if (r[s] > thr) pc->sum[i + d0 + s] += r[s];
+        if (pr) {
+          double acc = 0;
+          for (int s = 0; s < STRIP; ++s)
+            if (r[s] > thr) acc += r[s];
+          pr->sum[i] += acc;
+        }
+      }
+      const double dfr = bd->df_r[i], dgr = bd->dg_r[i];
+      for (int s = 0; s < STRIP; ++s) {
+        cov[s] += dfc[s] * dgr;
+        cov[s] += dfr * dgc[s];
+      }
+    }
+  }
+  for (; i < rows; ++i) {
     int64_t lim = bd->n_c - i - d0; /* diagonals still inside the matrix */
     if (lim > nd) lim = nd;
     double ir = bd->in_r[i];
