@@ -330,17 +330,6 @@ static void do_strip(const band_t *bd, int64_t d0, int64_t d1, int64_t m,
         if (pr) {
           double best = -2;
           int64_t bj = -1;
-          for (int s = 0; s < STRIP; ++s) {
-            const double v = r[s], b = cb[s];
-            const int64_t x = ci[s];
-            const int take = (v > b) | ((v == b) & (i < x));
-            cb[s] = take ? v : b;
-            ci[s] = take ? i : x;
-          }
-        }
-        if (pr) {
-          double best = -2;
-          int64_t bj = -1;
           for (int s = 0; s < STRIP; ++s)
             if (r[s] > best) {
               best = r[s];
