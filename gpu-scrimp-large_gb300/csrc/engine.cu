@@ -1073,14 +1073,15 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 struct NoAllocDevice {
   unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch
   int sms = 0;
+  int occ = 1;                       // resident join_fp64_kernel CTAs per SM
 };
 NoAllocDevice g_noalloc_dev[64];
 std::mutex g_noalloc_mu;
 
-// Once per device, with that device current: the scratch's device address
-// and the SM count.  The first call on a device therefore makes runtime
-// calls (module load, symbol lookup) that should happen before any stream
-// capture is started.
+// Once per device, with that device current: the scratch's device address,
+// the SM count and the FP64 join kernel's occupancy.  The first call on a
+// device therefore makes runtime calls (module load, symbol lookup) that
+// should happen before any stream capture is started.
 int noalloc_setup(int device, NoAllocDevice** out, std::string* msg) {
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -1099,6 +1100,10 @@ int noalloc_setup(int device, NoAllocDevice** out, std::string* msg) {
     void* p = nullptr;
     CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
     CUDA_TRY(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, device));
+    int occ = 1;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &occ, reinterpret_cast<const void*>(join_fp64_kernel), fp64_threads(), 0));
+    d.occ = std::max(occ, 1);
     d.scratch = static_cast<unsigned char*>(p);
   }
   *out = &d;
@@ -1132,6 +1137,36 @@ SeriesBufs carve_series(Carver& c, int64_t n, int bshift) {
   s.blo = c.take<float>(4 * (n / 32 + 1));
   s.mu_rel = c.take<float>(4 * n);
   return s;
+}
+
+// Band prefix of the no-allocation join on the device: entry g + 1 is the
+// number of units in bands 0 .. g (the count make_plan's problems give, as
+// run_device() builds it on the host).  One block of kNoAllocPrefixCap
+// threads, thread g for band g.
+__global__ void __launch_bounds__(kNoAllocPrefixCap)
+noalloc_prefix_kernel(JoinParams P, int64_t K, int W, int64_t* __restrict__ prefix) {
+  __shared__ int64_t part[kNoAllocPrefixCap];
+  const int g = threadIdx.x;
+  int64_t units = 0;
+  if (g < P.total_bands) {
+    int p = 0;
+    while (p + 1 < P.nprob && g >= P.prob[p + 1].band_begin) ++p;
+    const Problem& pr = P.prob[p];
+    const int64_t D0 = pr.d_lo + (g - pr.band_begin) * W;
+    const int64_t rows = band_rows(pr.R.ns, pr.C.ns, D0);
+    units = (rows + 2 * K - 1) / (2 * K);
+  }
+  part[g] = units;
+  __syncthreads();
+  // inclusive scan (Hillis-Steele)
+  for (int o = 1; o < kNoAllocPrefixCap; o <<= 1) {
+    const int64_t v = g >= o ? part[g - o] : 0;
+    __syncthreads();
+    part[g] += v;
+    __syncthreads();
+  }
+  if (g == 0) prefix[0] = 0;
+  if (g < P.total_bands) prefix[g + 1] = part[g];
 }
 
 // The FP64 join of run_device() on the static scratch: the same kernels,
@@ -1244,11 +1279,7 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
     }
   }
 
-  int occ = 1;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &occ, reinterpret_cast<const void*>(join_fp64_kernel), nthreads, 0));
-  occ = std::max(occ, 1);
-  const int64_t resident = static_cast<int64_t>(dv.sms) * occ;
+  const int64_t resident = static_cast<int64_t>(dv.sms) * dv.occ;
   // segment length: the FP64 rule of run_device()
   const double cells_d = static_cast<double>(plan.cells);
   const int64_t k_lb = static_cast<int64_t>(cells_d / (8.0 * resident * 2.0 * W));
@@ -1261,9 +1292,10 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
   }
 
   JoinParams P{};
-  int64_t prefix[kNoAllocPrefixCap];
-  int64_t np = 0;
-  prefix[np++] = 0;
+  // The band prefix is counted here (for the total and the grid) and built
+  // again on the device by noalloc_prefix_kernel from the same problems, so
+  // that no host memory is copied.
+  int64_t np = 1, units_total = 0;
   int64_t band_total = 0;
   for (const auto& q : plan.probs) {
     Problem& pr = P.prob[P.nprob++];
@@ -1283,14 +1315,13 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
     for (int64_t b = 0; b < pr.nbands; ++b) {
       const int64_t D0 = q.d_lo + b * W;
       const int64_t rows = band_rows(q.n_r, q.n_c, D0);
-      const int64_t units = (rows + 2 * K - 1) / (2 * K);
-      prefix[np] = prefix[np - 1] + units;
+      units_total += (rows + 2 * K - 1) / (2 * K);
       ++np;
     }
     band_total += pr.nbands;
   }
   P.total_bands = band_total;
-  P.total_units = prefix[np - 1];
+  P.total_units = units_total;
   P.m = m;
   P.seg_len = K;
   P.band_width = W;
@@ -1299,7 +1330,8 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
   P.kl = kl;
 
   if (P.total_units > 0) {
-    CUDA_TRY(cudaMemcpyAsync(dprefix, prefix, np * 8, cudaMemcpyHostToDevice, st));
+    noalloc_prefix_kernel<<<1, kNoAllocPrefixCap, 0, st>>>(P, K, W, dprefix);
+    ++launches;
     // the unit queue head and the work counters must start at zero
     CUDA_TRY(cudaMemsetAsync(counters, 0, 64, st));
     P.band_unit_prefix = dprefix;

@@ -143,7 +143,9 @@ int scamp_gb300_join(const scamp_c_args *args, scamp_c_result *res,
 
 /* Same join with every pointer in args/res being DEVICE memory of
  * args->device, ordered on `stream` (a cudaStream_t, NULL = default stream).
- * Used when the inputs are already resident in HBM. */
+ * Used when the inputs are already resident in HBM.  The call returns once
+ * the join has finished on the device: it waits for the join's last event on
+ * `stream` to read the timing fields and work counters of `res`. */
 int scamp_gb300_join_dev(const scamp_c_args *args, scamp_c_result *res,
                          void *stream, char *errbuf, size_t errlen);
 

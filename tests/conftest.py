@@ -10,7 +10,9 @@ for p in (os.path.join(REPO, "gpu-scrimp-large_gb300"), os.path.join(REPO, "orac
         sys.path.insert(0, p)
 
 PKG_DIR = os.path.join(REPO, "gpu-scrimp-large_gb300", "scamp_gb300")
-REFERENCE_TREE = "/root/reference"
+# The reference tree (its test inputs and sources), where one is present:
+# tests that read it skip when SCAMP_REFERENCE_TREE is unset.
+REFERENCE_TREE = os.environ.get("SCAMP_REFERENCE_TREE", "")
 
 
 def pytest_configure(config):

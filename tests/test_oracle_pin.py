@@ -2,7 +2,10 @@
 
 1. Against the golden outputs shipped with the reference
    (test/SampleOutput/mp_*, mpi_*; tolerances of test/difference.py:24 and
-   test/run_tests.sh:36) -- read where the reference tree is present.
+   test/run_tests.sh:36), and against the reference's compiled CPU path run
+   on its static stress inputs and its earthquake series -- both from the
+   committed fixtures of tests/golden/reference_data
+   (tests/golden/make_reference_fixtures.py) -- always.
 2. Against the reference's own CPU path compiled from its sources
    (oracle/_ref/libscampref.so) on seeded inputs, including 40 randomized
    configurations of profile type, geometry and edge cases -- where it was
@@ -21,9 +24,15 @@ import pytest
 
 from parity import check_sum, pair_corr
 
-REF = "/root/reference/test"
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
+REFDATA = os.path.join(GOLDEN, "reference_data")
+
+
+def _refdata(kind):
+    """The committed fixtures of the reference's test data: 'inputs',
+    'goldens' (its shipped outputs) or 'compiled' (its CPU path's outputs)."""
+    return np.load(os.path.join(REFDATA, kind + ".npz"), allow_pickle=False)
 
 
 def _distance(oracle, packed, m):
@@ -31,13 +40,13 @@ def _distance(oracle, packed, m):
     return oracle.to_distance(c, m), i
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
 @pytest.mark.parametrize("name", ["randomwalk8K", "randomwalk16K", "randomwalk32K",
                                   "randomwalk64K", "randomwalk64K_nan"])
 def test_oracle_vs_reference_goldens_selfjoin(oracle_mod, name):
-    a = np.loadtxt(os.path.join(REF, "SampleInput", name + ".txt"))
-    gd = np.loadtxt(os.path.join(REF, "SampleOutput", "mp_%s_w100.txt" % name))
-    gi = np.loadtxt(os.path.join(REF, "SampleOutput", "mpi_%s_w100.txt" % name)).astype(np.int64)
+    a = _refdata("inputs")[name]
+    g = _refdata("goldens")
+    gd = g["mp_" + name].astype(np.float64)
+    gi = g["mpi_" + name].astype(np.int64)
     d, i = _distance(oracle_mod, oracle_mod.join(a, None, 100)["packed_a"], 100)
     assert np.array_equal(np.isnan(d), np.isnan(gd))
     ok = ~np.isnan(gd)
@@ -46,68 +55,66 @@ def test_oracle_vs_reference_goldens_selfjoin(oracle_mod, name):
     assert np.sum(i != gi) <= len(gi) // 100
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
 @pytest.mark.parametrize("na,nb", [("randomwalk16K", "randomwalk32K"),
                                    ("randomwalk32K", "randomwalk16K")])
 def test_oracle_vs_reference_goldens_abjoin(oracle_mod, na, nb):
-    a = np.loadtxt(os.path.join(REF, "SampleInput", na + ".txt"))
-    b = np.loadtxt(os.path.join(REF, "SampleInput", nb + ".txt"))
-    gd = np.loadtxt(os.path.join(REF, "SampleOutput", "mp_%s_%s_w100.txt" % (na, nb)))
-    gi = np.loadtxt(os.path.join(REF, "SampleOutput", "mpi_%s_%s_w100.txt" % (na, nb))).astype(np.int64)
+    inp = _refdata("inputs")
+    a, b = inp[na], inp[nb]
+    g = _refdata("goldens")
+    gd = g["mp_%s_%s" % (na, nb)].astype(np.float64)
+    gi = g["mpi_%s_%s" % (na, nb)].astype(np.int64)
     d, i = _distance(oracle_mod, oracle_mod.join(a, b, 100, computing_rows=False)["packed_a"], 100)
     assert np.max(np.abs(d - gd)) <= 1e-5
     assert np.sum(i != gi) <= len(gi) // 100
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
 def test_oracle_aligned_self_as_ab_vs_reference_golden(oracle_mod):
     """test/run_tests.sh:49-77: an aligned AB-join of a series with itself
     reproduces its self-join golden."""
-    a = np.loadtxt(os.path.join(REF, "SampleInput", "randomwalk8K.txt"))
-    gd = np.loadtxt(os.path.join(REF, "SampleOutput", "mp_randomwalk8K_w100.txt"))
-    gi = np.loadtxt(os.path.join(REF, "SampleOutput", "mpi_randomwalk8K_w100.txt")).astype(np.int64)
+    a = _refdata("inputs")["randomwalk8K"]
+    g = _refdata("goldens")
+    gd = g["mp_randomwalk8K"].astype(np.float64)
+    gi = g["mpi_randomwalk8K"].astype(np.int64)
     d, i = _distance(oracle_mod, oracle_mod.join(a, a.copy(), 100, aligned=True,
                                                  computing_rows=False)["packed_a"], 100)
     assert np.max(np.abs(d - gd)) <= 1e-5
     assert np.sum(i != gi) <= len(gi) // 100
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
 def test_oracle_keep_rows_global_offsets_vs_reference_goldens(oracle_mod):
     """test/run_tests.sh:137-206: an AB-join with keep_rows and global
     offsets (not aligned, so they change nothing) reproduces both
     directions' goldens."""
-    a = np.loadtxt(os.path.join(REF, "SampleInput", "randomwalk32K.txt"))
-    b = np.loadtxt(os.path.join(REF, "SampleInput", "randomwalk16K.txt"))
+    inp = _refdata("inputs")
+    a, b = inp["randomwalk32K"], inp["randomwalk16K"]
     r = oracle_mod.join(a, b, 100, keep_rows=True, start_row=9000000000, start_col=100000)
+    g = _refdata("goldens")
     for side, name in (("a", "randomwalk32K_randomwalk16K"), ("b", "randomwalk16K_randomwalk32K")):
-        gd = np.loadtxt(os.path.join(REF, "SampleOutput", "mp_%s_w100.txt" % name))
-        gi = np.loadtxt(os.path.join(REF, "SampleOutput", "mpi_%s_w100.txt" % name)).astype(np.int64)
+        gd = g["mp_" + name].astype(np.float64)
+        gi = g["mpi_" + name].astype(np.int64)
         d, i = _distance(oracle_mod, r["packed_" + side], 100)
         assert np.max(np.abs(d - gd)) <= 1e-5, side
         assert np.sum(i != gi) <= len(gi) // 100, side
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference tree not present")
 @pytest.mark.parametrize("name", ["poorly_conditioned_test", "randomwalk1K_nan"])
 def test_oracle_vs_compiled_reference_static_inputs(oracle_mod, name):
     """test/run_tests.py:12-17: the static inputs (a quantized, poorly
     conditioned series and a walk with NaN samples) at every window the
     reference tests, 1NN_INDEX and SUM_THRESH at its thresholds, against
-    the reference's compiled CPU path: the same values at float32
-    resolution and NaN pattern; index differences only at float32 ties;
-    sums equal up to whole multiples of the threshold (cells whose r is the
-    threshold itself, frequent in quantized data, fall on either side by
-    one rounding: the reference's own rule, test/test_common.py:25-49)."""
-    if not oracle_mod.ref_available():
-        pytest.skip("reference CPU path not built here")
-    x = np.loadtxt(os.path.join(REF, "SampleInput", name + ".txt"))
+    the reference's compiled CPU path (its outputs committed as fixtures):
+    the same values at float32 resolution and NaN pattern; index
+    differences only at float32 ties; sums equal up to whole multiples of
+    the threshold (cells whose r is the threshold itself, frequent in
+    quantized data, fall on either side by one rounding: the reference's own
+    rule, test/test_common.py:25-49)."""
+    x = _refdata("inputs")[name]
+    comp = _refdata("compiled")
     for m in (5, 7, 13, 25, 33, 78, 92, 100, 189, 339, 500):
         if m > len(x) // 2:
             continue
-        want = oracle_mod.ref_join(x, None, m, threads=2)
         got = oracle_mod.join(x, None, m)
-        wc, wi = oracle_mod.unpack(want["packed_a"])
+        wc, wi = oracle_mod.unpack(comp["%s_m%d_1nn" % (name, m)])
         gc, gi = oracle_mod.unpack(got["packed_a"])
         assert np.array_equal(wc < -1, gc < -1), m
         ok = wc >= -1
@@ -115,9 +122,47 @@ def test_oracle_vs_compiled_reference_static_inputs(oracle_mod, name):
         mism = ok & (wi != gi)
         assert np.all(np.abs(wc[mism].astype(np.float64) - gc[mism]) <= 2.5e-7), m
         for thr in (0.0, 0.125, 0.5):
-            ws = oracle_mod.ref_join(x, None, m, profile="SUM_THRESH", threshold=thr, threads=2)
+            ws = comp["%s_m%d_sum%g" % (name, m, thr)].astype(np.float64)
             gs = oracle_mod.join(x, None, m, profile="SUM_THRESH", threshold=thr)
-            check_sum("%s m=%d thr=%g" % (name, m, thr), gs["sum_a"], ws["sum_a"], thr, 1e-6)
+            check_sum("%s m=%d thr=%g" % (name, m, thr), gs["sum_a"], ws, thr, 1e-6)
+
+
+@pytest.mark.parametrize("m", [100, 1000])
+def test_oracle_vs_compiled_reference_earthquake(oracle_mod, m):
+    """The series the reference's documentation names as the one that breaks
+    its reduced-precision modes (docs/source/cli.rst:127): the oracle's
+    DOUBLE join equals the reference's compiled CPU path (fixture) at
+    float32 resolution, indices differing only at float32 ties."""
+    x = _refdata("inputs")["earthquake_precision_test100K"]
+    wc, wi = oracle_mod.unpack(_refdata("compiled")["earthquake_precision_test100K_m%d_1nn" % m])
+    gc, gi = oracle_mod.unpack(oracle_mod.join(x, None, m)["packed_a"])
+    assert np.array_equal(wc < -1, gc < -1)
+    ok = wc >= -1
+    assert np.max(np.abs(wc[ok].astype(np.float64) - gc[ok])) <= 2.5e-7
+    mism = ok & (wi != gi)
+    assert np.all(np.abs(wc[mism].astype(np.float64) - gc[mism]) <= 2.5e-7)
+
+
+def test_reference_fixtures_match_reference_tree():
+    """Where the reference tree is present (SCAMP_REFERENCE_TREE), the
+    committed fixtures hold exactly its sample inputs and golden outputs."""
+    from conftest import REFERENCE_TREE
+
+    if not REFERENCE_TREE or not os.path.isdir(os.path.join(REFERENCE_TREE, "test")):
+        pytest.skip("reference tree not present")
+    base = os.path.join(REFERENCE_TREE, "test")
+    inp = _refdata("inputs")
+    for name in inp.files:
+        x = np.loadtxt(os.path.join(base, "SampleInput", name + ".txt"))
+        assert np.array_equal(np.isnan(x), np.isnan(inp[name])), name
+        assert np.array_equal(x[~np.isnan(x)], inp[name][~np.isnan(x)]), name
+    g = _refdata("goldens")
+    for key in g.files:
+        want = np.loadtxt(os.path.join(base, "SampleOutput", key + "_w100.txt"))
+        got = g[key].astype(np.float64)
+        assert np.array_equal(np.isnan(want), np.isnan(got)), key
+        ok = ~np.isnan(want)
+        assert np.max(np.abs(want[ok] - got[ok]) / np.maximum(np.abs(want[ok]), 1.0)) <= 1e-7, key
 
 
 def _ref_cases():

@@ -17,7 +17,8 @@ def _walk(seed, n):
     return np.cumsum(np.random.default_rng(seed).standard_normal(n))
 
 
-def _call(entry, torch, a, b, m, profile, keep_rows=False, threshold=0.0, precision="double"):
+def _call(entry, torch, a, b, m, profile, keep_rows=False, threshold=0.0, precision="double",
+          rows=True):
     """Runs one join through `entry` (a C-ABI function taking device
     pointers) on fresh best-so-far buffers; returns host copies."""
     import scamp_gb300
@@ -31,7 +32,7 @@ def _call(entry, torch, a, b, m, profile, keep_rows=False, threshold=0.0, precis
     nn = profile == "1NN_INDEX"
     no_match = np.array([scamp_gb300.NO_MATCH], dtype=np.uint64).view(np.int64)[0]
     outs = {}
-    ca = scamp_gb300._args(None, None, m, profile, precision, True, True, keep_rows, False,
+    ca = scamp_gb300._args(None, None, m, profile, precision, rows, True, keep_rows, False,
                            threshold, -1, -1, 128000, 0, 0, True)
     ca.timeseries_a = a_d.data_ptr()
     ca.len_a = len(a)
@@ -71,13 +72,21 @@ def _compare(got, ref, nn):
 
 
 CASES = [
-    # (seed, len_a, len_b, m, profile, keep_rows, threshold, precision)
-    (1, 20000, None, 100, "1NN_INDEX", False, 0.0, "double"),
-    (2, 30000, 20000, 64, "1NN_INDEX", True, 0.0, "double"),
-    (3, 65536, None, 256, "1NN_INDEX", False, 0.0, "double"),
-    (4, 12000, None, 50, "SUM_THRESH", False, 0.5, "double"),
-    (5, 20000, None, 64, "1NN_INDEX", False, 0.0, "ultra"),
-    (6, 15000, 10000, 50, "1NN_INDEX", True, 0.0, "ultra"),
+    # (seed, len_a, len_b, m, profile, keep_rows, threshold, precision, computing_rows)
+    (1, 20000, None, 100, "1NN_INDEX", False, 0.0, "double", True),
+    (2, 30000, 20000, 64, "1NN_INDEX", True, 0.0, "double", True),
+    (3, 65536, None, 256, "1NN_INDEX", False, 0.0, "double", True),
+    (4, 12000, None, 50, "SUM_THRESH", False, 0.5, "double", True),
+    (5, 20000, None, 64, "1NN_INDEX", False, 0.0, "ultra", True),
+    (6, 15000, 10000, 50, "1NN_INDEX", True, 0.0, "ultra", True),
+    # self-joins whose rows go to profile B (keep_rows_separate)
+    (7, 18000, None, 80, "1NN_INDEX", True, 0.0, "double", True),
+    (8, 16000, None, 40, "1NN_INDEX", True, 0.0, "ultra", True),
+    # AB-join sums in both directions
+    (9, 14000, 11000, 60, "SUM_THRESH", True, 0.3, "double", True),
+    # columns only (pyscamp's abjoin) and a self-join without rows
+    (10, 25000, 9000, 70, "1NN_INDEX", False, 0.0, "double", False),
+    (11, 12000, None, 32, "1NN_INDEX", False, 0.0, "double", False),
 ]
 
 
@@ -86,14 +95,15 @@ def test_noalloc_equals_join_dev_twice(gpu_engine):
     from scamp_gb300 import _lib
 
     lib = _lib.load()
-    for seed, la, lb, m, profile, keep, thr, prec in CASES:
+    for seed, la, lb, m, profile, keep, thr, prec, rows in CASES:
         a = _walk(seed, la)
         b = _walk(seed + 100, lb) if lb else None
-        rc, msg, ref = _call(lib.scamp_gb300_join_dev, torch, a, b, m, profile, keep, thr, prec)
+        rc, msg, ref = _call(lib.scamp_gb300_join_dev, torch, a, b, m, profile, keep, thr, prec,
+                             rows)
         assert rc == 0, msg
         for _ in range(2):  # two calls in a row on the same static scratch
             rc, msg, got = _call(lib.scamp_gb300_join_dev_noalloc, torch, a, b, m, profile,
-                                 keep, thr, prec)
+                                 keep, thr, prec, rows)
             assert rc == 0, msg
             _compare(got, ref, profile == "1NN_INDEX")
 
