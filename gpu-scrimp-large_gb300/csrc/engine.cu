@@ -71,6 +71,15 @@ int64_t cold_anchor_interval(int64_t m) {
 // the direct-dot seeds at 1/32 of the FP64 pipe's work.
 int64_t fp64_segment(int64_t m) { return std::max<int64_t>(32 * m, 8192); }
 
+// Bound on |reported r - FP64 r| after final_eval_kernel: twice
+// gamma_{ceil(m/32) + 10} (u = 2^-53) for the direct FP64 evaluation, plus
+// the key's resolution 2^-F (final_eval.cu derives it).
+double final_eval_bound(int64_t m, int frac_bits) {
+  const double u = std::ldexp(1.0, -53);
+  const double k = static_cast<double>((m + 31) / 32 + 10);
+  return 2.0 * k * u / (1.0 - k * u) + std::ldexp(1.0, -frac_bits);
+}
+
 struct Error {
   int code;
   std::string msg;
@@ -243,6 +252,10 @@ struct Workspace {
   cudaEvent_t evkv = nullptr;                   // before the verification kernel
   bool timed_kernel = false;
   bool timed_verify = false;
+  // the mixed form's largest trusted drift margin (work counter 4) is the
+  // join's max_tie_margin (1NN) or max_abs_r_err (SUM_THRESH)
+  bool tracked_tie_margin = false;
+  bool tracked_sum_margin = false;
   // Verification requests of the mixed 1NN join: capacity of the buffer, and
   // the largest count a join asked for (the buffer grows to it on the next
   // join; requests beyond the capacity are verified inline, more slowly).
@@ -773,6 +786,30 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     if (!nested) CUDA_TRY(cudaEventRecord(ws.evk1, st));
   }
 
+  // ---- FP64 re-evaluation of every reported cell (1NN types) ----
+  if (is_1nn) {
+    EvalPair E{};
+    E.m = m;
+    E.kl = kl;
+    for (int s = 0; s < 2; ++s) {
+      if (!keys[s]) continue;
+      EvalSide& es = E.side[s];
+      es.keys = keys[s];
+      es.prof_in = max_only ? nullptr : profs[s];
+      es.max_in = max_only ? maxs[s] : nullptr;
+      es.X = s == 0 ? devA : devB;
+      es.Y = plan.self_join ? devA : (s == 0 ? devB : devA);
+      es.ns = nsz[s];
+      es.m = m;
+    }
+    const int64_t nwin = E.side[0].ns + E.side[1].ns;
+    if (nwin > 0) {
+      const int64_t blocks = std::min<int64_t>((nwin + 7) / 8, static_cast<int64_t>(ws.sms) * 16);
+      final_eval_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(E);
+      ++launches;
+    }
+  }
+
   // ---- keys -> packed entries (+ optional double correlations) ----
   for (int s = 0; s < 2; ++s) {
     if (!vkeys[s]) continue;
@@ -803,6 +840,14 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   if (res) {
     res->comparisons = plan.cells;
     res->gpu_launches = launches;
+    // accuracy fields; the mixed form's tracked margin is read with the
+    // work counters (read_times)
+    res->max_abs_r_err = is_1nn ? final_eval_bound(m, kl.frac_bits) : (kind == K_MIXED ? 0.0 : -1.0);
+    res->max_tie_margin = (is_1nn && kind == K_MIXED) ? 0.0 : -1.0;
+  }
+  if (!nested) {
+    ws.tracked_sum_margin = !is_1nn && kind == K_MIXED;
+    ws.tracked_tie_margin = is_1nn && kind == K_MIXED;
   }
   return SCAMP_OK;
 }
@@ -810,12 +855,17 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
 void read_times(Workspace& ws, scamp_c_result* res) {
   res->steps = res->slow_steps = res->verifications = 0;
   if (ws.timed_kernel && ws.bufs.size() > S_COUNTER && ws.bufs[S_COUNTER].p) {
-    unsigned long long c[5] = {0, 0, 0, 0, 0};
+    unsigned long long c[6] = {0, 0, 0, 0, 0, 0};
     if (cudaMemcpy(c, ws.bufs[S_COUNTER].p, sizeof(c), cudaMemcpyDeviceToHost) == cudaSuccess) {
       res->steps = c[1];
       res->slow_steps = c[2];
       res->verifications = c[3];
       ws.vreq_seen = std::max<int64_t>(ws.vreq_seen, static_cast<int64_t>(c[4]));
+      float tm;
+      const uint32_t bits = static_cast<uint32_t>(c[5]);
+      std::memcpy(&tm, &bits, 4);
+      if (ws.tracked_tie_margin) res->max_tie_margin = tm;
+      if (ws.tracked_sum_margin) res->max_abs_r_err = tm;
     }
   }
   float ms = 0;
@@ -1344,6 +1394,28 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
     CUDA_TRY(cudaGetLastError());
   }
   if (is_1nn) {
+    // the FP64 re-evaluation of run_device(), so that both entries report
+    // the same values
+    EvalPair E{};
+    E.m = m;
+    E.kl = kl;
+    for (int s = 0; s < 2; ++s) {
+      if (!keys[s]) continue;
+      EvalSide& es = E.side[s];
+      es.keys = keys[s];
+      es.prof_in = profs[s];
+      es.max_in = nullptr;
+      es.X = s == 0 ? devA : devB;
+      es.Y = plan.self_join ? devA : (s == 0 ? devB : devA);
+      es.ns = nsz[s];
+      es.m = m;
+    }
+    const int64_t nwin = E.side[0].ns + E.side[1].ns;
+    if (nwin > 0) {
+      const int64_t blocks = std::min<int64_t>((nwin + 7) / 8, static_cast<int64_t>(dv.sms) * 16);
+      final_eval_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(E);
+      ++launches;
+    }
     double* corr[2] = {res->corr_a, res->corr_b};
     for (int s = 0; s < 2; ++s) {
       if (!keys[s]) continue;
@@ -1357,6 +1429,8 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
   res->gpu_launches = launches;
   res->elapsed_ms = res->join_kernel_ms = 0;
   res->steps = res->slow_steps = res->verifications = 0;
+  res->max_abs_r_err = is_1nn ? final_eval_bound(m, kl.frac_bits) : -1.0;
+  res->max_tie_margin = -1.0;
   return SCAMP_OK;
 }
 
@@ -1418,6 +1492,7 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   int rc;
   ws.timed_kernel = false;
   ws.timed_verify = false;
+  ws.tracked_tie_margin = ws.tracked_sum_margin = false;
   std::vector<BatchSeries> ser(count);
   int64_t Nn = 0, Nns = 0, Nblk = 0, ns_max = 1;
   bool want_corr = false;
@@ -1454,7 +1529,8 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
                b_murel = sz(4 * Nns), b_keys = sz(8 * Nns), b_prof = sz(8 * Nns),
                b_corr = sz(want_corr ? 8 * Nns : 8), b_jobs = sz(sizeof(StatsJob) * count),
                b_jpre = sz(8 * (count + 1)), b_probs = sz(sizeof(Problem) * count),
-               b_counter = sz(64), b_wpre = sz(8 * (count + 1));
+               b_counter = sz(64), b_wpre = sz(8 * (count + 1)),
+               b_eval = sz(sizeof(EvalSide) * count);
   // band prefix: sized after the problems are known
   int64_t bands_max = 0;
   for (const auto& b : ser) bands_max += (b.ns + mixed_1nn_band_width() - 1) / mixed_1nn_band_width();
@@ -1485,6 +1561,7 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   unsigned long long* d_counter = reinterpret_cast<unsigned long long*>(take(b_counter));
   int64_t* d_bpre = reinterpret_cast<int64_t*>(take(b_bpre));
   int64_t* d_wpre = reinterpret_cast<int64_t*>(take(b_wpre));
+  EvalSide* d_eval = reinterpret_cast<EvalSide*>(take(b_eval));
 
   // ---- host side: inputs gathered, every launch's arguments built ----
   std::vector<double> h_raw(static_cast<size_t>(Nn));
@@ -1558,9 +1635,22 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     band_total += pr.nbands;
     probs.push_back(pr);
   }
-  // seeds from each series' nearest allowed diagonal (diag_seed_kernel)
+  // seeds from each series' nearest allowed diagonal (diag_seed_kernel),
+  // and the FP64 re-evaluation of every reported cell (final_eval_batch_kernel)
   std::vector<int64_t> wpre(probs.size() + 1, 0);
   for (size_t p = 0; p < probs.size(); ++p) wpre[p + 1] = wpre[p] + probs[p].R.ns;
+  std::vector<EvalSide> evs(probs.size());
+  for (size_t p = 0; p < probs.size(); ++p) {
+    EvalSide& e = evs[p];
+    e.keys = probs[p].key_col;
+    e.prof_in = d_prof + (probs[p].key_col - d_keys);
+    e.max_in = nullptr;
+    e.X = e.Y = probs[p].R;
+    e.ns = probs[p].R.ns;
+    e.m = probs[p].m;
+  }
+  const int64_t eval_blocks = std::max<int64_t>(
+      std::min<int64_t>((wpre.back() + 7) / 8, static_cast<int64_t>(ws.sms) * 16), 1);
   const int64_t seed_blocks = std::max<int64_t>(
       std::min<int64_t>((wpre.back() + 255) / 256, static_cast<int64_t>(ws.sms) * 32), 1);
   JoinParams P{};
@@ -1605,10 +1695,12 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
                              cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_wpre, wpre.data(), 8 * wpre.size(), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(d_bpre, bpre.data(), 8 * bpre.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_eval, evs.data(), sizeof(EvalSide) * evs.size(),
+                             cudaMemcpyHostToDevice, st));
   }
 
   // ---- device part: one graph ----
-  uint32_t launches = probs.empty() ? 3 : 6;
+  uint32_t launches = probs.empty() ? 3 : 7;
   const std::vector<int64_t> key = {
       reinterpret_cast<int64_t>(arena), Nn, Nns, Nblk, count, want_corr ? 1 : 0, bands_max,
       jpre[count], kl.idx_bits, static_cast<int64_t>(probs.size()), seed_blocks, band_total,
@@ -1631,6 +1723,8 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
         if ((e = cudaEventRecordWithFlags(ws.evkv, st, cudaEventRecordExternal)) != cudaSuccess) return e;
         verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
         if ((e = cudaEventRecordWithFlags(ws.evk1, st, cudaEventRecordExternal)) != cudaSuccess) return e;
+        final_eval_batch_kernel<<<static_cast<unsigned>(eval_blocks), 256, 0, st>>>(
+            d_eval, d_wpre, static_cast<int>(probs.size()), kl);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
       }
       keys_to_profile_kernel<<<static_cast<unsigned>((Nns + 255) / 256), 256, 0, st>>>(
@@ -1678,12 +1772,16 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   read_times(ws, &tot);
   if (!probs.empty()) {
     // the batch's work counters live in its arena, not in the join counters
-    unsigned long long c[5] = {0, 0, 0, 0, 0};
+    unsigned long long c[6] = {0, 0, 0, 0, 0, 0};
     if (cudaMemcpy(c, d_counter, sizeof(c), cudaMemcpyDeviceToHost) == cudaSuccess) {
       tot.steps = c[1];
       tot.slow_steps = c[2];
       tot.verifications = c[3];
       ws.vreq_seen = std::max<int64_t>(ws.vreq_seen, static_cast<int64_t>(c[4]));
+      const uint32_t bits = static_cast<uint32_t>(c[5]);
+      float tm;
+      std::memcpy(&tm, &bits, 4);
+      tot.max_tie_margin = tm;
     }
   }
   for (int k = 0; k < count; ++k) {
@@ -1695,6 +1793,8 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     res[k].steps = tot.steps;
     res[k].slow_steps = tot.slow_steps;
     res[k].verifications = tot.verifications;
+    res[k].max_abs_r_err = final_eval_bound(ser[k].m, kl.frac_bits);
+    res[k].max_tie_margin = tot.max_tie_margin;
   }
   return SCAMP_OK;
 }

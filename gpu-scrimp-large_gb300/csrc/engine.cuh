@@ -142,7 +142,9 @@ struct JoinParams {
   int64_t total_bands;
   int64_t total_units;
   unsigned long long* unit_counter; // persistent work queue head
-  unsigned long long* counters;     // [steps, slow steps, verifications, requests]
+  // [steps, slow steps, verifications, requests, largest trusted margin
+  // (float bits, mixed form)]
+  unsigned long long* counters;
   VerifyReq* vreq;                  // verification requests (mixed 1NN)
   int64_t vreq_cap;
   int* error_flag;                  // device error word (0 = ok)
@@ -268,6 +270,27 @@ __global__ void fill_floor_kernel(uint64_t* __restrict__ p, int64_t n, float flo
 __global__ void seed_kernel(SeedArgs S);
 __global__ void diag_seed_kernel(const Problem* __restrict__ probs,
                                  const int64_t* __restrict__ win_prefix, int nprob, KeyLayout kl);
+
+// FP64 re-evaluation of the reported 1NN cells (final_eval.cu): one side is
+// one profile's keys, with the series of its windows (X) and of its
+// partners (Y).  prof_in / max_in: the profile given on input (its entries
+// that the join did not change keep their value); either may be null.
+struct EvalSide {
+  uint64_t* keys;
+  const uint64_t* prof_in;
+  const float* max_in;
+  SeriesDev X, Y;
+  int64_t ns, m;
+};
+struct EvalPair {
+  EvalSide side[2];  // ns = 0 for a side that is not reported
+  int64_t m;
+  KeyLayout kl;
+};
+__global__ void final_eval_kernel(EvalPair E);
+__global__ void final_eval_batch_kernel(const EvalSide* __restrict__ sides,
+                                        const int64_t* __restrict__ win_prefix, int nsides,
+                                        KeyLayout kl);
 
 __global__ void floats_to_keys_kernel(const float* __restrict__ in, uint64_t* __restrict__ keys,
                                       int64_t n, KeyLayout kl);

@@ -1,0 +1,122 @@
+// final_eval.cu -- FP64 re-evaluation of every reported 1NN cell.
+//
+// Both join forms choose each window's best partner from a recurrence (FP64
+// in the plain form, FP32 behind a filter in the mixed form).  Before the
+// profile is written back, this kernel recomputes the correlation of every
+// (window, reported partner) pair directly: centred FP64 dot product and
+// centred sums of squares of the two windows, r = dot / sqrt(sxx * syy), so
+// the value a join reports does not carry the recurrence's drift or the
+// statistics' rounding.  This is the reference's correlation formula
+// (src/cpu_kernels.cpp:166-171 with the norms of src/cpu_stats.cpp:85-97,
+// the brute-force ULTRA statistics) evaluated once per reported cell.
+//
+// Error bound (per reported value, against the exact correlation of the two
+// FP64 windows): every centred term x_t = fl(T - mu) carries one rounding;
+// a lane sums ceil(m / 32) products by FMA, five shuffle levels add the lane
+// sums, and the quotient takes three more roundings, so with
+// gamma_k = k u / (1 - k u), u = 2^-53:
+//   |r_hat - r| <= 2 gamma_{ceil(m/32) + 10}
+// (the dot's error is gamma_k * sum |x y| <= gamma_k ||x|| ||y||; each sum of
+// squares is off by at most gamma_k of itself).  The 64-bit key then keeps r
+// to 2^-F.  The host adds the two (final_eval_bound).
+//
+// Entries the join did not change (a best-so-far entry given on input, whose
+// index may refer to another join) are left as they are.
+#include <cstdint>
+
+#include "engine.cuh"
+
+namespace scamp_gb300 {
+
+namespace {
+
+// Direct FP64 correlation of window i of X with window j of Y, one warp;
+// every lane returns the same value (NaN when a window has no spread).
+__device__ __forceinline__ double corr_warp_fp64(const SeriesDev& X, const SeriesDev& Y,
+                                                 int64_t i, int64_t j, int64_t m, int lane) {
+  const double mx = X.mean[i], my = Y.mean[j];
+  const double* __restrict__ tx = X.T + i;
+  const double* __restrict__ ty = Y.T + j;
+  double sxy = 0.0, sxx = 0.0, syy = 0.0;
+  for (int64_t t = lane; t < m; t += 32) {
+    const double x = tx[t] - mx, y = ty[t] - my;
+    sxy = fma(x, y, sxy);
+    sxx = fma(x, x, sxx);
+    syy = fma(y, y, syy);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sxy += __shfl_xor_sync(0xffffffffu, sxy, o);
+    sxx += __shfl_xor_sync(0xffffffffu, sxx, o);
+    syy += __shfl_xor_sync(0xffffffffu, syy, o);
+  }
+  return sxy / sqrt(sxx * syy);
+}
+
+// The key an input profile entry turns into (profile_to_keys_kernel,
+// floats_to_keys_kernel): 0 when there is no entry.
+__device__ __forceinline__ uint64_t initial_key(const EvalSide& s, int64_t w, const KeyLayout& kl) {
+  if (s.prof_in) {
+    const uint64_t e = s.prof_in[w];
+    const uint32_t cbits = static_cast<uint32_t>(e);
+    const uint32_t idx = static_cast<uint32_t>(e >> 32);
+    if (!(__uint_as_float(cbits) >= -1.0f) || static_cast<uint64_t>(idx) > kl.idx_mask) return 0;
+    return make_key(q_from_float_bits(cbits, kl.frac_bits), idx, kl);
+  }
+  if (s.max_in) {
+    const float c = s.max_in[w];
+    if (!(c >= -1.0f)) return 0;
+    return make_key(q_from_float_bits(__float_as_uint(c), kl.frac_bits), 0, kl);
+  }
+  return 0;
+}
+
+__device__ __forceinline__ void eval_window(const EvalSide& s, int64_t w, int64_t m,
+                                            const KeyLayout& kl, int lane) {
+  const uint64_t k = s.keys[w];
+  if (k == 0 || k == initial_key(s, w, kl)) return;
+  const int64_t j = key_to_index(k, kl);
+  if (j < 0 || j >= s.Y.ns) return;
+  const double r = corr_warp_fp64(s.X, s.Y, w, j, m, lane);
+  if (lane == 0 && !isnan(r)) {
+    // |r| <= 1 up to rounding; the key holds r in [-2, 2)
+    const double rc = r > 1.0 ? 1.0 : (r < -1.0 ? -1.0 : r);
+    s.keys[w] = make_key(q_from_double_bits(__double_as_longlong(rc), kl.frac_bits), j, kl);
+  }
+}
+
+}  // namespace
+
+// One warp per window of up to two profile sides (a single join).
+__global__ void __launch_bounds__(256) final_eval_kernel(EvalPair E) {
+  const int lane = threadIdx.x & 31;
+  const int64_t total = E.side[0].ns + E.side[1].ns;
+  const int64_t nwarps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t g = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; g < total;
+       g += nwarps) {
+    const int s = g >= E.side[0].ns;
+    eval_window(E.side[s], g - (s ? E.side[0].ns : 0), E.m, E.kl, lane);
+  }
+}
+
+// One warp per window of a batch: side k covers windows
+// win_prefix[k] .. win_prefix[k + 1] - 1 of the launch.
+__global__ void __launch_bounds__(256) final_eval_batch_kernel(const EvalSide* __restrict__ sides,
+                                                               const int64_t* __restrict__ win_prefix,
+                                                               int nsides, KeyLayout kl) {
+  const int lane = threadIdx.x & 31;
+  const int64_t total = win_prefix[nsides];
+  const int64_t nwarps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t g = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; g < total;
+       g += nwarps) {
+    int lo = 0, hi = nsides;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (win_prefix[mid] <= g) lo = mid; else hi = mid;
+    }
+    const EvalSide& s = sides[lo];
+    eval_window(s, g - win_prefix[lo], s.m, kl, lane);
+  }
+}
+
+}  // namespace scamp_gb300

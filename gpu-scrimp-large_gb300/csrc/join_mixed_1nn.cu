@@ -166,6 +166,7 @@ struct SlowCtx {
   VerifyReq* vreq;                 // deferred verification requests
   unsigned long long* vcount;      // their count (may exceed vcap)
   int64_t vcap;
+  unsigned long long* tmargin;     // largest drift margin of a trusted FP32 value (float bits)
 };
 
 struct Smem {
@@ -376,6 +377,7 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
   const Problem& pr = *cx.pr;
   const int k = (lane & 15) >> 1, g = lane & 1;
   int nreq = 0;
+  float tmax = 0.f;  // largest margin of a value published or added unverified
   for (int p = 0; p < count; p += 2) {
     // every lane runs the pass (warp-wide request reservation); a lane
     // without a block carries the first queued one and checks nothing
@@ -448,8 +450,10 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
           }
         } else if (cx.sum_mode) {
           add = rv > cx.thr ? rv : 0.f;
+          if (add != 0.f) tmax = fmaxf(tmax, mk);
         } else {
           publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
+          tmax = fmaxf(tmax, mk);
         }
       }
       if (cx.sum_mode) {
@@ -468,6 +472,11 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
       c = fmaf(dfr, dgc, c);
     }
   }
+  // the trusted margins, one atomic per drain (non-negative floats order as
+  // their bit patterns)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+  if (lane == 0 && tmax > 0.f) atomicMax(cx.tmargin, static_cast<unsigned long long>(__float_as_uint(tmax)));
   __syncwarp();
   return nreq;
 }
@@ -675,6 +684,7 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
       cx.vreq = P.vreq;
       cx.vcount = P.counters + 3;
       cx.vcap = P.vreq_cap;
+      cx.tmargin = P.counters + 4;
       cx.sum_mode = kSum;
       cx.thr = static_cast<float>(P.threshold);
     }

@@ -222,6 +222,8 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
     out["counters"] = {"steps": int(res.steps), "slow_steps": int(res.slow_steps),
                        "verifications": int(res.verifications),
                        "verify_kernel_ms": float(res.verify_kernel_ms)}
+    out["max_abs_r_err"] = float(res.max_abs_r_err)
+    out["max_tie_margin"] = float(res.max_tie_margin)
     return out
 
 
@@ -263,7 +265,9 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
                          "verifications": int(res.verifications),
                          "verify_kernel_ms": float(res.verify_kernel_ms)},
             "comparisons": int(res.comparisons),
-            "gpu_launches": int(res.gpu_launches)}
+            "gpu_launches": int(res.gpu_launches),
+            "max_abs_r_err": float(res.max_abs_r_err),
+            "max_tie_margin": float(res.max_tie_margin)}
 
 
 def _batch_args(series, windows, precision, device):
@@ -332,7 +336,9 @@ def join_batch(series, windows, precision="mixed", return_corr=False, device=0,
              "gpu_launches": int(cres[k].gpu_launches),
              "counters": {"steps": int(cres[k].steps), "slow_steps": int(cres[k].slow_steps),
                           "verifications": int(cres[k].verifications),
-                          "verify_kernel_ms": float(cres[k].verify_kernel_ms)}}
+                          "verify_kernel_ms": float(cres[k].verify_kernel_ms)},
+             "max_abs_r_err": float(cres[k].max_abs_r_err),
+             "max_tie_margin": float(cres[k].max_tie_margin)}
         if return_corr:
             d["corr_a"] = corrs[k]
         out.append(d)

@@ -101,6 +101,8 @@ class CResult(ctypes.Structure):
         ("knn_a", ctypes.c_void_p),
         ("knn_b", ctypes.c_void_p),
         ("matrix", ctypes.c_void_p),
+        ("max_abs_r_err", ctypes.c_double),
+        ("max_tie_margin", ctypes.c_double),
     ]
 
 

@@ -119,6 +119,11 @@ struct SCAMPArgs {
   int64_t max_matches_per_column = 5;  // APPROX_ALL_NEIGHBORS
   int64_t matrix_height = 50;          // MATRIX_SUMMARY
   int64_t matrix_width = 50;
+  // Filled by do_SCAMP (no counterpart in the reference's SCAMPArgs): the
+  // accuracy statement of the last join, scamp_c_result's max_abs_r_err
+  // and max_tie_margin (-1 where not tracked).
+  double max_abs_r_err = -1.0;
+  double max_tie_margin = -1.0;
 };
 
 namespace detail {
@@ -269,6 +274,8 @@ inline void do_SCAMP(SCAMPArgs* args, const std::vector<int>& devices, int num_t
     if (args->keep_rows_separate) r.sum_b = args->profile_b.data[0].double_value.data();
   }
   detail::check(scamp_gb300_join(&c, &r, msg, sizeof msg), msg);
+  args->max_abs_r_err = r.max_abs_r_err;
+  args->max_tie_margin = r.max_tie_margin;
 }
 
 inline void do_SCAMP(SCAMPArgs* args) { do_SCAMP(args, std::vector<int>{0}, 0); }

@@ -131,6 +131,31 @@ typedef struct scamp_c_result {
    * block x (blocks of ceil(windows / height or width)), -2.0f where none;
    * in/out (merged by max).  Columns only, as in the reference. */
   float *matrix;
+  /* Accuracy of the reported correlations (filled by the engine).
+   * max_abs_r_err: bound on |reported r - FP64 r| for every reported value.
+   *   1NN_INDEX / 1NN (both forms): after the join the correlation of every
+   *   reported (window, partner) pair is recomputed in FP64 from the two
+   *   windows (centred dot product over centred sums of squares); the bound
+   *   is that computation's rounding plus the profile key's resolution,
+   *   deterministic, for corr_a / corr_b (packed float32 entries add their
+   *   own rounding, 2^-24 |r|).  Entries given on input and left unchanged
+   *   keep their value.
+   *   SUM_THRESH, mixed form: the largest drift margin of an FP32
+   *   correlation added without a direct dot product (a bound under the
+   *   filter's rounding model, see max_tie_margin).
+   *   -1 where no bound is tracked (FP64 SUM_THRESH, APPROX_ALL_NEIGHBORS,
+   *   MATRIX_SUMMARY).
+   * max_tie_margin: mixed 1NN forms: the largest drift margin of an FP32
+   *   recurrence value that chose a partner without a direct dot product.
+   *   The reported partner's FP64 correlation is within twice this of the
+   *   window's best as long as the FP32 drift stays within its margin (the
+   *   filter's model: an Azuma-Hoeffding bound over independent roundings),
+   *   plus the rounding of the FP32 direct dot products that chose the
+   *   other partners (verified candidates and seeds; not tracked).
+   *   -1 for the FP64 form, whose partners are chosen from FP64 recurrence
+   *   values (not tracked). */
+  double max_abs_r_err;
+  double max_tie_margin;
 } scamp_c_result;
 
 /* Runs one join.  Inputs and results are HOST memory; the engine copies them

@@ -97,3 +97,60 @@ def check_sum(name, got, want, thr, rtol, cell_tol=0.0):
         n_bad = int(np.sum(bad))
     assert n_bad == 0, "%s: %d sums differ (max rel %.3g)" % (name, n_bad, float((diff / scale).max()))
     return float((diff / scale).max()) if diff.size else 0.0
+
+
+def cell_corr(T_rows, T_cols, m, rows, cols, chunk=4096):
+    """FP64 Pearson correlation of row window rows[k] of T_rows with column
+    window cols[k] of T_cols, computed directly for each pair (centred dot
+    product over centred sums of squares), vectorised in chunks."""
+    Rc = np.where(np.isfinite(T_rows), T_rows, 0.0).astype(np.float64)
+    Cc = np.where(np.isfinite(T_cols), T_cols, 0.0).astype(np.float64)
+    WR = np.lib.stride_tricks.sliding_window_view(Rc, m)
+    WC = np.lib.stride_tricks.sliding_window_view(Cc, m)
+    rows = np.asarray(rows, dtype=np.int64)
+    cols = np.asarray(cols, dtype=np.int64)
+    out = np.empty(len(rows))
+    for s in range(0, len(rows), chunk):
+        X = WR[rows[s:s + chunk]]
+        Y = WC[cols[s:s + chunk]]
+        X = X - X.mean(axis=1, keepdims=True)
+        Y = Y - Y.mean(axis=1, keepdims=True)
+        out[s:s + chunk] = np.einsum("ij,ij->i", X, Y) / np.sqrt(
+            np.einsum("ij,ij->i", X, X) * np.einsum("ij,ij->i", Y, Y))
+    return out
+
+
+def check_1nn_direct(name, got_corr, got_idx, want_idx, tol, T_self, T_other, m, bound=None):
+    """A 1NN_INDEX profile against direct FP64 correlations (for sizes where
+    the oracle's own long recurrences drift by more than the FP64 form's
+    tolerance; the oracle still gives the no-match pattern and its choice of
+    partner):
+      * the no-match pattern equals the oracle's;
+      * every reported value is within tol (and within the engine's reported
+        bound, when given, plus numpy's own rounding) of the direct FP64
+        correlation of its (window, partner) pair;
+      * the reported partner is no worse than the oracle's by more than tol
+        (both evaluated directly).
+    Returns (max |value error|, worst shortfall against the oracle's partner)."""
+    got_corr = np.asarray(got_corr, dtype=np.float64)
+    got_none = got_idx < 0
+    want_none = want_idx < 0
+    assert np.array_equal(got_none, want_none), (
+        "%s: no-match pattern differs at %s" % (name, np.nonzero(got_none != want_none)[0][:10]))
+    w = np.nonzero(~want_none)[0]
+    if w.size == 0:
+        return 0.0, 0.0
+    r_got = cell_corr(T_other, T_self, m, got_idx[w], w)
+    err = np.abs(got_corr[w] - r_got)
+    maxerr = float(err.max())
+    assert maxerr <= tol, "%s: max |r - direct r| %.3g > %.1g" % (name, maxerr, tol)
+    if bound is not None:
+        assert maxerr <= bound + 1e-13, "%s: value error %.3g above the reported bound %.3g" % (
+            name, maxerr, bound)
+    diff = np.nonzero(got_idx[w] != want_idx[w])[0]
+    short = 0.0
+    if diff.size:
+        r_want = cell_corr(T_other, T_self, m, want_idx[w[diff]], w[diff])
+        short = float(np.max(r_want - r_got[diff]))
+        assert short <= tol, "%s: a reported partner is %.3g below the oracle's" % (name, short)
+    return maxerr, short
