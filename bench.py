@@ -1,24 +1,29 @@
-"""Benchmark of the GB300 SCAMP engine on the AB-join configuration.
+"""Benchmark of the GB300 SCAMP engine.
 
-Workload (the configuration the headline metric is quoted on): AB-join of a
-random walk A (2^20 points) with a random walk B (2^19 points) sharing 64
-planted sinusoid motifs, 0.1% NaN samples, window m = 256, 1NN_INDEX in both
-directions (keep_rows); seeded synthetic data of those shapes.
+Default workload (the configuration the headline target is quoted on): a
+self-join of a seeded random walk plus 0.5 N(0,1) noise, n = 2^24 points,
+window m = 1024, 1NN_INDEX, mixed precision.  A step is one complete join
+through the C ABI's scamp_gb300_join with pinned host buffers: ``value`` is
+comparisons/s over the join's device time (the CUDA events the join records
+on its stream around its device work, statistics to final profile, after
+the input copy), ``e2e`` the same comparisons over the wall clock of the
+whole call (host->device copy of the series and the best-so-far profile,
+the join, device->host copy of the profile).  The series (128 MiB) and its
+statistics (1.2 GiB) exceed the 129 MB L2, so nothing is flushed between
+steps.  The FP64 form and the mixed-vs-FP64 error check run on the first
+2^22 samples (the whole FP64 join takes about 17 minutes); the CPU baseline
+on the first 2^17 samples.
 
-A step is one complete join.  ``value`` is comparisons/s of the mixed form
-with the series already resident in HBM (C-ABI scamp_gb300_join_dev);
-``e2e`` is the same metric through scamp_gb300_join with pinned host
-buffers, host<->device copies included.  The FP64 form runs the same join
-for the error check (max |r| difference of the two forms) and its own
-throughput.  The L2 (129 MB, larger than the 12 MB input) is flushed before
-every timed step by writing a 512 MB buffer.  A step's device time comes
-from the CUDA events the join records on the launching stream around its
-device work (statistics to final profile).
+``--workload ab``: the AB-join of 2^20 x 2^19 random walks with planted
+motifs and NaNs, m = 256, 1NN_INDEX both directions; ``value`` with the
+series resident in HBM (scamp_gb300_join_dev), ``e2e`` through
+scamp_gb300_join.  ``--workload batch`` / ``gaps``: the batched and the
+gapped large self-join workloads.
 
-``--impl reference`` times the CPU path instead: the oracle's C restatement
-of the reference's CPU join (the reference tree does not exist on the GPU
-host, so its own sources cannot be compiled there) with every host thread,
-on a bounded sample of the workload per step.
+``--impl reference`` times the CPU path instead: the reference's own CPU
+join compiled from its sources where that was possible, else the oracle's C
+restatement of it (the reference tree does not exist on the GPU host), with
+every host thread, on a bounded sample of the workload per step.
 
 Multi-GPU (torchrun): every rank runs an independent replica of the join
 (the engine is single-GPU); the timed region is barrier-bracketed and the
@@ -140,7 +145,7 @@ class ClockSampler:
 SELF_WORKLOAD = "self-join: random walk + 0.5 N(0,1) noise, n=2^24, m=1024, 1NN_INDEX"
 SELF_M = 1024
 SELF_FP64_PREFIX = 1 << 22
-WORKLOAD_KIND = "ab"
+WORKLOAD_KIND = "self"
 
 
 def make_workload(na=None, nb=None):
@@ -383,6 +388,142 @@ def run_batch_workload(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+# DRAM bytes (read + write) of one band-kernel launch on the 2^24-point
+# self-join, from a one-launch ncu capture of a smaller self-join of the same
+# distribution scaled by comparisons (join_mixed_1nn_selfjoin summary under
+# profiles/); None until measured.
+SELF_DRAM_BYTES_PER_LAUNCH = None
+
+
+def run_self_headline(args, world, rank, local):
+    """The default workload: the 2^24-point m = 1024 self-join, one join per
+    step through scamp_gb300_join (host buffers)."""
+    import torch
+
+    import scamp_gb300
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    a_np, _, m = make_workload()
+    n = len(a_np)
+    ns = n - m + 1
+    a_pin = torch.from_numpy(a_np).pin_memory().numpy()
+    p_pin = torch.empty(ns, dtype=torch.int64).pin_memory().numpy().view(np.uint64)
+
+    def step():
+        p_pin[:] = scamp_gb300.NO_MATCH  # an empty best-so-far profile
+        t0 = time.perf_counter()
+        r = scamp_gb300.join(a_pin, None, m, "1NN_INDEX", "mixed", profile_a=p_pin,
+                             inplace=True, device=local)
+        return time.perf_counter() - t0, r
+
+    for _ in range(args.warmup):
+        step()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    dev_ms, wall, kernel_ms, verify_ms, launches = [], [], [], [], 0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            dt, r = step()
+            wall.append(dt)
+            dev_ms.append(r["elapsed_ms"])
+            kernel_ms.append(r["join_kernel_ms"] - r["counters"]["verify_kernel_ms"])
+            verify_ms.append(r["counters"]["verify_kernel_ms"])
+            launches += r["gpu_launches"]
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks = clk.summary()
+    cells = r["comparisons"]
+    ms_step = max_over_ranks(sum(dev_ms) / len(dev_ms), dist, dev)
+    e2e_s = max_over_ranks(sum(wall) / len(wall), dist, dev)
+    value = replica_value(cells, world, ms_step * 1e-3)
+
+    # FP64 form and the error check on the first 2^22 samples
+    xp = a_np[:SELF_FP64_PREFIX] if n > SELF_FP64_PREFIX else a_np
+    r64 = scamp_gb300.join(xp, None, m, "1NN_INDEX", "double", return_corr=True, device=local)
+    rmx = scamp_gb300.join(xp, None, m, "1NN_INDEX", "mixed", return_corr=True, device=local)
+    ok = r64["corr_a"] >= -1
+    max_err = float(np.max(np.abs(rmx["corr_a"][ok] - r64["corr_a"][ok]), initial=0.0))
+    _, i64 = scamp_gb300.unpack_profile(r64["profile_a"])
+    _, imx = scamp_gb300.unpack_profile(rmx["profile_a"])
+    agree = float(np.mean(i64[ok] == imx[ok])) if ok.any() else 1.0
+    fp64_value = r64["comparisons"] / (r64["elapsed_ms"] * 1e-3)
+
+    peak32 = scamp_gb300.pipe_peak("fp32", local)
+    peak64 = scamp_gb300.pipe_peak("fp64", local)
+    k_ms = sum(kernel_ms) / len(kernel_ms)
+    achieved = cells * OPS_PER_CELL / (k_ms * 1e-3)
+    achieved64 = r64["comparisons"] * OPS_PER_CELL / (r64["join_kernel_ms"] * 1e-3)
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    traffic = None
+    if SELF_DRAM_BYTES_PER_LAUNCH is not None and n == 1 << 24:
+        traffic = SELF_DRAM_BYTES_PER_LAUNCH
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "comparisons/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded random walk plus noise)",
+        "config": {"workload": SELF_WORKLOAD if n == 1 << 24 else
+                   SELF_WORKLOAD.replace("n=2^24", "n=%d" % n),
+                   "form": "mixed (FP32 recurrence behind an FP32 filter, FP64-centred "
+                           "anchors, FP64 re-evaluation of every reported cell)",
+                   "comparisons_per_step": cells,
+                   "l2": "not flushed: inputs larger than L2 (series 128 MiB, statistics and "
+                         "profile 1.2 GiB per join)",
+                   "timing": "value: the join's own device events (statistics to final "
+                             "profile); e2e: wall clock of scamp_gb300_join with pinned host "
+                             "buffers",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "max_abs_r_err": rmx["max_abs_r_err"],
+        "max_tie_margin": rmx["max_tie_margin"],
+        "max_abs_r_err_vs_fp64": max_err,
+        "index_agreement_vs_fp64": agree,
+        "fp64_error_check": "first 2^22 samples: mixed vs FP64 form, both engine joins",
+        "fp64": {"value": fp64_value, "unit": "comparisons/s",
+                 "comparisons_per_step": r64["comparisons"], "ms_per_step": r64["elapsed_ms"],
+                 "sample": "first 2^22 samples of the workload",
+                 "roofline": {"bound": "fp64_fma_pipe", "achieved": achieved64 / 1e12,
+                              "peak": peak64 / 1e12, "unit": "Tops/s",
+                              "frac": achieved64 / peak64, "peak_source": "measured DFMA probe"}},
+        "speedup_mixed_vs_fp64": value / world / fp64_value,
+        "roofline": {"bound": "fp32_fma_pipe", "achieved": achieved / 1e12, "peak": peak32 / 1e12,
+                     "unit": "Tops/s", "frac": achieved / peak32, "traffic": traffic,
+                     "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
+                     "kernel": "join_mixed_1nn_kernel", "kernel_ms": k_ms,
+                     "ops_per_comparison": OPS_PER_CELL,
+                     "verify_kernel_ms": sum(verify_ms) / len(verify_ms),
+                     "work_counters": r["counters"],
+                     "peak_source": "measured packed-FP32 FMA probe (scamp_gb300_pipe_peak)"},
+        "e2e": {"value": replica_value(cells, world, e2e_s), "unit": "comparisons/s",
+                "h2d_bytes_per_step": n * 8 + ns * 8, "d2h_bytes_per_step": ns * 8},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_leg()
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -391,9 +532,9 @@ def main():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--fp64-steps", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="ab", choices=["ab", "self", "batch", "gaps"],
-                   help="ab: the headline AB-join (default); self: the 2^24-point m=1024 "
-                        "self-join of the precision study")
+    p.add_argument("--workload", default="self", choices=["self", "ab", "batch", "gaps"],
+                   help="self: the 2^24-point m=1024 self-join (default); ab: the AB-join "
+                        "of 2^20 x 2^19 random walks with motifs and NaNs, m=256")
     p.add_argument("--na-log2", type=int, default=None,
                    help="log2 length of A (B is half); smaller only for profiling captures")
     p.add_argument("--profile-form", default="mixed", choices=["mixed", "double"],
@@ -418,6 +559,9 @@ def main():
 
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload == "self" and not (args.anchor_study or args.profile_only):
+        run_self_headline(args, world, rank, local)
         return
     if args.workload == "batch":
         run_batch_workload(args, world, rank, local)

@@ -72,11 +72,11 @@ int64_t cold_anchor_interval(int64_t m) {
 int64_t fp64_segment(int64_t m) { return std::max<int64_t>(32 * m, 8192); }
 
 // Bound on |reported r - FP64 r| after final_eval_kernel: twice
-// gamma_{ceil(m/32) + 10} (u = 2^-53) for the direct FP64 evaluation, plus
+// gamma_{ceil(m/16) + 10} (u = 2^-53) for the direct FP64 evaluation, plus
 // the key's resolution 2^-F (final_eval.cu derives it).
 double final_eval_bound(int64_t m, int frac_bits) {
   const double u = std::ldexp(1.0, -53);
-  const double k = static_cast<double>((m + 31) / 32 + 10);
+  const double k = static_cast<double>((m + 15) / 16 + 10);
   return 2.0 * k * u / (1.0 - k * u) + std::ldexp(1.0, -frac_bits);
 }
 
@@ -804,7 +804,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     }
     const int64_t nwin = E.side[0].ns + E.side[1].ns;
     if (nwin > 0) {
-      const int64_t blocks = std::min<int64_t>((nwin + 7) / 8, static_cast<int64_t>(ws.sms) * 16);
+      const int64_t blocks = std::min<int64_t>((nwin + 31) / 32, static_cast<int64_t>(ws.sms) * 16);
       final_eval_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(E);
       ++launches;
     }
@@ -1412,7 +1412,7 @@ int run_device_noalloc(const NoAllocDevice& dv, const scamp_c_args* a, scamp_c_r
     }
     const int64_t nwin = E.side[0].ns + E.side[1].ns;
     if (nwin > 0) {
-      const int64_t blocks = std::min<int64_t>((nwin + 7) / 8, static_cast<int64_t>(dv.sms) * 16);
+      const int64_t blocks = std::min<int64_t>((nwin + 31) / 32, static_cast<int64_t>(dv.sms) * 16);
       final_eval_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(E);
       ++launches;
     }
@@ -1650,7 +1650,7 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     e.m = probs[p].m;
   }
   const int64_t eval_blocks = std::max<int64_t>(
-      std::min<int64_t>((wpre.back() + 7) / 8, static_cast<int64_t>(ws.sms) * 16), 1);
+      std::min<int64_t>((wpre.back() + 31) / 32, static_cast<int64_t>(ws.sms) * 16), 1);
   const int64_t seed_blocks = std::max<int64_t>(
       std::min<int64_t>((wpre.back() + 255) / 256, static_cast<int64_t>(ws.sms) * 32), 1);
   JoinParams P{};

@@ -12,10 +12,11 @@
 //
 // Error bound (per reported value, against the exact correlation of the two
 // FP64 windows): every centred term x_t = fl(T - mu) carries one rounding;
-// a lane sums ceil(m / 32) products by FMA, five shuffle levels add the lane
-// sums, and the quotient takes three more roundings, so with
+// each of a group's 8 lanes sums its terms by FMA into two accumulators of
+// at most ceil(m / 16) terms, one add joins them, three shuffle levels add
+// the lanes' sums, and the quotient takes three more roundings, so with
 // gamma_k = k u / (1 - k u), u = 2^-53:
-//   |r_hat - r| <= 2 gamma_{ceil(m/32) + 10}
+//   |r_hat - r| <= 2 gamma_{ceil(m/16) + 10}
 // (the dot's error is gamma_k * sum |x y| <= gamma_k ||x|| ||y||; each sum of
 // squares is off by at most gamma_k of itself).  The 64-bit key then keeps r
 // to 2^-F.  The host adds the two (final_eval_bound).
@@ -30,27 +31,46 @@ namespace scamp_gb300 {
 
 namespace {
 
-// Direct FP64 correlation of window i of X with window j of Y, one warp;
-// every lane returns the same value (NaN when a window has no spread).
-__device__ __forceinline__ double corr_warp_fp64(const SeriesDev& X, const SeriesDev& Y,
-                                                 int64_t i, int64_t j, int64_t m, int lane) {
+constexpr int kLanes = 8;  // lanes per window: four windows per warp
+
+// Direct FP64 correlation of window i of X with window j of Y by kLanes
+// lanes (a lane sums every kLanes-th term, the partial sums meet in a
+// shuffle tree); the value is valid in the group's first lane (NaN when a
+// window has no spread).
+__device__ __forceinline__ double corr_group_fp64(const SeriesDev& X, const SeriesDev& Y,
+                                                  int64_t i, int64_t j, int64_t m, int sub,
+                                                  bool first) {
   const double mx = X.mean[i], my = Y.mean[j];
   const double* __restrict__ tx = X.T + i;
   const double* __restrict__ ty = Y.T + j;
-  double sxy = 0.0, sxx = 0.0, syy = 0.0;
-  for (int64_t t = lane; t < m; t += 32) {
-    const double x = tx[t] - mx, y = ty[t] - my;
-    sxy = fma(x, y, sxy);
-    sxx = fma(x, x, sxx);
-    syy = fma(y, y, syy);
+  double sxy = 0.0, sxx = 0.0, syy = 0.0, sxy2 = 0.0, sxx2 = 0.0, syy2 = 0.0;
+  int64_t t = sub;
+  for (; t + kLanes < m; t += 2 * kLanes) {
+    const double x0 = tx[t] - mx, y0 = ty[t] - my;
+    const double x1 = tx[t + kLanes] - mx, y1 = ty[t + kLanes] - my;
+    sxy = fma(x0, y0, sxy);
+    sxx = fma(x0, x0, sxx);
+    syy = fma(y0, y0, syy);
+    sxy2 = fma(x1, y1, sxy2);
+    sxx2 = fma(x1, x1, sxx2);
+    syy2 = fma(y1, y1, syy2);
   }
+  if (t < m) {
+    const double x0 = tx[t] - mx, y0 = ty[t] - my;
+    sxy = fma(x0, y0, sxy);
+    sxx = fma(x0, x0, sxx);
+    syy = fma(y0, y0, syy);
+  }
+  sxy += sxy2;
+  sxx += sxx2;
+  syy += syy2;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
+  for (int o = kLanes / 2; o > 0; o >>= 1) {
     sxy += __shfl_xor_sync(0xffffffffu, sxy, o);
     sxx += __shfl_xor_sync(0xffffffffu, sxx, o);
     syy += __shfl_xor_sync(0xffffffffu, syy, o);
   }
-  return sxy / sqrt(sxx * syy);
+  return first ? sxy / sqrt(sxx * syy) : 0.0;
 }
 
 // The key an input profile entry turns into (profile_to_keys_kernel,
@@ -71,14 +91,20 @@ __device__ __forceinline__ uint64_t initial_key(const EvalSide& s, int64_t w, co
   return 0;
 }
 
+// Window w of side s, evaluated by the kLanes lanes of group `sub`; every
+// lane of the warp calls it (the shuffle tree needs them), `active` marks the
+// groups with a window.
 __device__ __forceinline__ void eval_window(const EvalSide& s, int64_t w, int64_t m,
-                                            const KeyLayout& kl, int lane) {
-  const uint64_t k = s.keys[w];
-  if (k == 0 || k == initial_key(s, w, kl)) return;
-  const int64_t j = key_to_index(k, kl);
-  if (j < 0 || j >= s.Y.ns) return;
-  const double r = corr_warp_fp64(s.X, s.Y, w, j, m, lane);
-  if (lane == 0 && !isnan(r)) {
+                                            const KeyLayout& kl, int sub, bool active) {
+  uint64_t k = active ? s.keys[w] : 0;
+  if (k != 0 && k == initial_key(s, w, kl)) k = 0;
+  int64_t j = k ? key_to_index(k, kl) : 0;
+  if (j < 0 || j >= s.Y.ns) k = 0;
+  // groups with nothing to do still take part in the shuffles (no terms)
+  const bool work = k != 0;
+  const double r = corr_group_fp64(s.X, s.Y, work ? w : 0, work ? j : 0, work ? m : 0, sub,
+                                   sub == 0);
+  if (sub == 0 && work && !isnan(r)) {
     // |r| <= 1 up to rounding; the key holds r in [-2, 2)
     const double rc = r > 1.0 ? 1.0 : (r < -1.0 ? -1.0 : r);
     s.keys[w] = make_key(q_from_double_bits(__double_as_longlong(rc), kl.frac_bits), j, kl);
@@ -87,35 +113,49 @@ __device__ __forceinline__ void eval_window(const EvalSide& s, int64_t w, int64_
 
 }  // namespace
 
-// One warp per window of up to two profile sides (a single join).
+// Groups of kLanes lanes, one window each, over up to two profile sides (a
+// single join).  The loop bound is warp-uniform: a warp's four groups stay
+// together for the shuffles.
 __global__ void __launch_bounds__(256) final_eval_kernel(EvalPair E) {
   const int lane = threadIdx.x & 31;
+  const int sub = lane & (kLanes - 1);
   const int64_t total = E.side[0].ns + E.side[1].ns;
   const int64_t nwarps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
-  for (int64_t g = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; g < total;
-       g += nwarps) {
-    const int s = g >= E.side[0].ns;
-    eval_window(E.side[s], g - (s ? E.side[0].ns : 0), E.m, E.kl, lane);
+  constexpr int kGroups = 32 / kLanes;
+  for (int64_t g0 = ((static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * kGroups;
+       g0 < total; g0 += nwarps * kGroups) {
+    const int64_t g = g0 + lane / kLanes;
+    const bool active = g < total;
+    const int s = (active && g >= E.side[0].ns) ? 1 : 0;
+    const int64_t w = active ? g - (s ? E.side[0].ns : 0) : 0;
+    eval_window(E.side[s], w, E.m, E.kl, sub, active);
   }
 }
 
-// One warp per window of a batch: side k covers windows
-// win_prefix[k] .. win_prefix[k + 1] - 1 of the launch.
+// The same over a batch: side k covers windows win_prefix[k] ..
+// win_prefix[k + 1] - 1 of the launch.
 __global__ void __launch_bounds__(256) final_eval_batch_kernel(const EvalSide* __restrict__ sides,
                                                                const int64_t* __restrict__ win_prefix,
                                                                int nsides, KeyLayout kl) {
   const int lane = threadIdx.x & 31;
+  const int sub = lane & (kLanes - 1);
   const int64_t total = win_prefix[nsides];
   const int64_t nwarps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
-  for (int64_t g = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; g < total;
-       g += nwarps) {
-    int lo = 0, hi = nsides;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (win_prefix[mid] <= g) lo = mid; else hi = mid;
+  constexpr int kGroups = 32 / kLanes;
+  for (int64_t g0 = ((static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * kGroups;
+       g0 < total; g0 += nwarps * kGroups) {
+    const int64_t g = g0 + lane / kLanes;
+    const bool active = g < total;
+    int lo = 0;
+    if (active) {
+      int hi = nsides;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (win_prefix[mid] <= g) lo = mid; else hi = mid;
+      }
     }
     const EvalSide& s = sides[lo];
-    eval_window(s, g - win_prefix[lo], s.m, kl, lane);
+    eval_window(s, active ? g - win_prefix[lo] : 0, s.m, kl, sub, active);
   }
 }
 
