@@ -56,6 +56,17 @@ int64_t default_anchor_interval(int64_t m) {
   return std::min<int64_t>(std::max<int64_t>(1024, 32 * m), std::max<int64_t>(16384, 2 * m));
 }
 
+// Windows from which the mixed band kernel filters blocks by the per-step
+// covariance bound (join_mixed_1nn.cu, kCoarse) instead of per-cell r: the
+// inverse norms of windows that overlap in all but a few samples are close,
+// so the bound stays tight.  Band kernel time, per-step bound against
+// per-cell filter (flagged 8-row steps in brackets): random walks of 2^21
+// samples, m = 64: 3260 / 474 ms (5.5e9 / 1.6e8), m = 256: 990 / 365
+// (7.3e8 / 6.5e6), m = 512: 541 / 364 (1.9e8 / 4.0e6); the 2^22-sample
+// noisy walk, m = 1024: 1430 / 1458 (1.5e8 / 9.0e6); a 2^21-sample walk
+// with NaN gaps, m = 4096: 368 / 412.
+constexpr int64_t kCoarseFilterMinWindow = 1024;
+
 // Anchor interval of joins that start cold (batched joins: diagonal seeds
 // only, the bests still rising through the first slabs): 8 m within [1024,
 // 4096].  A longer interval widens the filter margin while many cells are
@@ -152,6 +163,10 @@ int validate(const scamp_c_args* a, std::string* msg) {
     return SCAMP_ERR_INVALID_ARGS;
   }
   if (a->anchor_interval < 0) { *msg = "Error: anchor_interval must be >= 0"; return SCAMP_ERR_INVALID_ARGS; }
+  if (a->filter_mode < 0 || a->filter_mode > 2) {
+    *msg = "Error: filter_mode must be 0, 1 or 2";
+    return SCAMP_ERR_INVALID_ARGS;
+  }
   return SCAMP_OK;
 }
 
@@ -633,10 +648,14 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   // threshold is the sum threshold and every cell above it is accumulated).
   // The k-best and matrix-summary types run the FP64 visit kernel.
   enum { K_FP64, K_MIXED, K_VISIT } kind = visit ? K_VISIT : !mixed ? K_FP64 : K_MIXED;
+  const bool coarse = kind == K_MIXED && (a->filter_mode == 2 ||
+                                          (a->filter_mode == 0 && m >= kCoarseFilterMinWindow));
   const void* kfn = kind == K_VISIT ? reinterpret_cast<const void*>(join_visit_kernel)
                   : kind == K_FP64 ? reinterpret_cast<const void*>(join_fp64_kernel)
-                  : is_1nn ? reinterpret_cast<const void*>(join_mixed_1nn_kernel)
-                           : reinterpret_cast<const void*>(join_mixed_sum_kernel);
+                  : is_1nn ? (coarse ? reinterpret_cast<const void*>(join_mixed_1nn_coarse_kernel)
+                                     : reinterpret_cast<const void*>(join_mixed_1nn_kernel))
+                           : (coarse ? reinterpret_cast<const void*>(join_mixed_sum_coarse_kernel)
+                                     : reinterpret_cast<const void*>(join_mixed_sum_kernel));
   const int W = kind == K_VISIT ? visit_band_width()
               : kind == K_FP64 ? fp64_band_width() : mixed_1nn_band_width();
   const int slab = kind == K_MIXED ? mixed_1nn_slab_rows() : fp64_slab_rows();
@@ -753,8 +772,12 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
       ws.timed_kernel = true;
     }
     if (kind == K_MIXED) {
-      if (is_1nn)
+      if (is_1nn && coarse)
+        join_mixed_1nn_coarse_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
+      else if (is_1nn)
         join_mixed_1nn_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
+      else if (coarse)
+        join_mixed_sum_coarse_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
       else
         join_mixed_sum_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
       ++launches;

@@ -248,6 +248,9 @@ __global__ void ord_to_floats_kernel(const unsigned* __restrict__ in, float* __r
                                      int64_t n);
 __global__ void join_mixed_1nn_kernel(JoinParams P);  // mixed 1NN_INDEX
 __global__ void join_mixed_sum_kernel(JoinParams P);  // mixed SUM_THRESH
+// the same with the per-step covariance bound as the fast path's filter
+__global__ void join_mixed_1nn_coarse_kernel(JoinParams P);
+__global__ void join_mixed_sum_coarse_kernel(JoinParams P);
 __global__ void verify_requests_kernel(JoinParams P);
 
 // Seeds of the mixed 1NN join from a block-averaged pre-pass.

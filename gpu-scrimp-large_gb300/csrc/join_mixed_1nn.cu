@@ -481,9 +481,18 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
   return nreq;
 }
 
-// The band kernel's body; kSum selects SUM_THRESH (two instantiations, so
-// the 1NN_INDEX form carries none of the sum bookkeeping).
-template <bool kSum>
+// The band kernel's body; kSum selects SUM_THRESH (separate instantiations,
+// so the 1NN_INDEX form carries none of the sum bookkeeping).  kCoarse
+// selects the fast path's filter:
+//   false: per cell, r = (cov * inv_c) * inv_r, the block's largest r
+//          against the threshold (8 packed multiplies per row);
+//   true:  per step, the block's largest covariance times the largest
+//          inverse norms of its columns and rows -- an upper bound of every
+//          r in the block, which spares the per-cell multiplies.  It is
+//          tight where the inverse norms of neighbouring windows are close
+//          (long windows); a block it flags goes to the exact path, which
+//          checks every cell with its own r.
+template <bool kSum, bool kCoarse>
 __device__ __forceinline__ void band_body(const JoinParams& P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
@@ -867,39 +876,72 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
 
         // fast path: recurrence + block maximum
         float bx = -3.f, by = -3.f;
-        float2 rprev;
+        if constexpr (kCoarse) {
+          // largest covariance of the block (NaN diagonals ignored), then
+          // the bound max(cov, 0) * max inv_c * max inv_r of every r in it
 #pragma unroll
-        for (int rr = 0; rr < kRows; ++rr) {
-          {
-            const int x = rr + kDiags - 1;
-            cfw[(8 * P + x) & 15] = col_fg(sm, base + x + (x >> 3));
-            ciw[(8 * P + x) & 15] = sm.u.s.c_iv[base + x + (x >> 3)];
-          }
-          const float4 rf = sm.r_fg[r0 + rr];
-          const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
-          const float2 ivr = sm.r_iv[r0 + rr];
-          // the row's largest cov * inv_c, times inv_r (> 0): the largest r
-          // of the row, rounded exactly as (cov * inv_c) * inv_r per cell
-          float mx = -3.f, my = -3.f;
+          for (int rr = 0; rr < kRows; ++rr) {
+            {
+              const int x = rr + kDiags - 1;
+              cfw[(8 * P + x) & 15] = col_fg(sm, base + x + (x >> 3));
+            }
+            const float4 rf = sm.r_fg[r0 + rr];
+            const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
+            {
+              const float ax = max3(cov[0].x, cov[1].x, cov[2].x);
+              const float ay = max3(cov[0].y, cov[1].y, cov[2].y);
+              const float cx3 = max3(cov[3].x, cov[4].x, cov[5].x);
+              const float cy3 = max3(cov[3].y, cov[4].y, cov[5].y);
+              bx = max3(bx, cov[6].x, cov[7].x);
+              by = max3(by, cov[6].y, cov[7].y);
+              bx = max3(bx, ax, cx3);
+              by = max3(by, ay, cy3);
+            }
 #pragma unroll
-          for (int k = 0; k < kDiags; k += 2) {
-            const float2 pa = mul2(cov[k], ciw[(8 * P + rr + k) & 15]);
-            const float2 pb = mul2(cov[k + 1], ciw[(8 * P + rr + k + 1) & 15]);
-            mx = max3(mx, pa.x, pb.x);
-            my = max3(my, pa.y, pb.y);
+            for (int k = 0; k < kDiags; ++k) {
+              const float4 c4 = cfw[(8 * P + rr + k) & 15];
+              cov[k] = fma2(make_float2(c4.x, c4.y), dgr, cov[k]);
+              cov[k] = fma2(dfr, make_float2(c4.z, c4.w), cov[k]);
+            }
           }
-          const float2 rm = mul2(make_float2(mx, my), ivr);
-          if (rr & 1) {
-            bx = max3(bx, rprev.x, rm.x);
-            by = max3(by, rprev.y, rm.y);
-          } else {
-            rprev = rm;
-          }
+          const float2 bnd = mul2(mul2(make_float2(fmaxf(bx, 0.f), fmaxf(by, 0.f)), icm), irm);
+          bx = bnd.x;
+          by = bnd.y;
+        } else {
+          float2 rprev;
 #pragma unroll
-          for (int k = 0; k < kDiags; ++k) {
-            const float4 c4 = cfw[(8 * P + rr + k) & 15];
-            cov[k] = fma2(make_float2(c4.x, c4.y), dgr, cov[k]);
-            cov[k] = fma2(dfr, make_float2(c4.z, c4.w), cov[k]);
+          for (int rr = 0; rr < kRows; ++rr) {
+            {
+              const int x = rr + kDiags - 1;
+              cfw[(8 * P + x) & 15] = col_fg(sm, base + x + (x >> 3));
+              ciw[(8 * P + x) & 15] = sm.u.s.c_iv[base + x + (x >> 3)];
+            }
+            const float4 rf = sm.r_fg[r0 + rr];
+            const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
+            const float2 ivr = sm.r_iv[r0 + rr];
+            // the row's largest cov * inv_c, times inv_r (> 0): the largest r
+            // of the row, rounded exactly as (cov * inv_c) * inv_r per cell
+            float mx = -3.f, my = -3.f;
+#pragma unroll
+            for (int k = 0; k < kDiags; k += 2) {
+              const float2 pa = mul2(cov[k], ciw[(8 * P + rr + k) & 15]);
+              const float2 pb = mul2(cov[k + 1], ciw[(8 * P + rr + k + 1) & 15]);
+              mx = max3(mx, pa.x, pb.x);
+              my = max3(my, pa.y, pb.y);
+            }
+            const float2 rm = mul2(make_float2(mx, my), ivr);
+            if (rr & 1) {
+              bx = max3(bx, rprev.x, rm.x);
+              by = max3(by, rprev.y, rm.y);
+            } else {
+              rprev = rm;
+            }
+#pragma unroll
+            for (int k = 0; k < kDiags; ++k) {
+              const float4 c4 = cfw[(8 * P + rr + k) & 15];
+              cov[k] = fma2(make_float2(c4.x, c4.y), dgr, cov[k]);
+              cov[k] = fma2(dfr, make_float2(c4.z, c4.w), cov[k]);
+            }
           }
         }
         const bool trig = bx > tx || by > ty;
@@ -932,7 +974,7 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
 #pragma unroll
           for (int x = 0; x < kDiags - 1; ++x) {
             cfw[x] = col_fg(sm, 9 * rb + x);  // padc(ring column 8 rb + x), x < 8
-            ciw[x] = sm.u.s.c_iv[9 * rb + x];
+            if constexpr (!kCoarse) ciw[x] = sm.u.s.c_iv[9 * rb + x];
           }
         }
         step(s, Parity<0>());
@@ -1004,11 +1046,19 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
 size_t mixed_1nn_smem_bytes() { return sizeof(Smem); }
 
 __global__ void __launch_bounds__(kThreads, 4) join_mixed_1nn_kernel(JoinParams P) {
-  band_body<false>(P);
+  band_body<false, false>(P);
 }
 
 __global__ void __launch_bounds__(kThreads, 4) join_mixed_sum_kernel(JoinParams P) {
-  band_body<true>(P);
+  band_body<true, false>(P);
+}
+
+__global__ void __launch_bounds__(kThreads, 4) join_mixed_1nn_coarse_kernel(JoinParams P) {
+  band_body<false, true>(P);
+}
+
+__global__ void __launch_bounds__(kThreads, 4) join_mixed_sum_coarse_kernel(JoinParams P) {
+  band_body<true, true>(P);
 }
 
 // Settles the verification requests of the band kernels, one warp per

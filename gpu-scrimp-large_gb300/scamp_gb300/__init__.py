@@ -56,7 +56,8 @@ def gpu_supported():
 
 def _args(a, b, m, profile, precision, computing_rows, computing_cols,
           keep_rows, aligned, threshold, start_row, start_col, max_tile_size,
-          anchor_interval, device, silent, max_matches=5, matrix_height=50, matrix_width=50):
+          anchor_interval, device, silent, max_matches=5, matrix_height=50, matrix_width=50,
+          filter_mode=0):
     ca = _lib.CArgs()
     ca.timeseries_a = a.ctypes.data if a is not None else None
     ca.len_a = len(a) if a is not None else 0
@@ -80,6 +81,7 @@ def _args(a, b, m, profile, precision, computing_rows, computing_cols,
     ca.max_matches_per_column = int(max_matches)
     ca.matrix_height = int(matrix_height)
     ca.matrix_width = int(matrix_width)
+    ca.filter_mode = int(filter_mode)
     return ca
 
 
@@ -123,7 +125,7 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
          aligned=False, threshold=0.0, start_row=-1, start_col=-1,
          max_tile_size=128000, anchor_interval=0, device=0, profile_a=None,
          profile_b=None, return_corr=False, silent=True, inplace=False, max_matches=5,
-         matrix_height=50, matrix_width=50):
+         matrix_height=50, matrix_width=50, filter_mode=0):
     """Run one join (the C ABI's scamp_gb300_join, host buffers; the
     reference's SCAMP::do_SCAMP, src/SCAMP.cpp:261-334, with the arguments
     of SCAMPArgs, src/common.h:164-188).
@@ -152,7 +154,7 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
     ca = _args(a, b, m, profile, precision, computing_rows, computing_cols,
                keep_rows, aligned, threshold, start_row, start_col,
                max_tile_size, anchor_interval, device, silent, max_matches,
-               matrix_height, matrix_width)
+               matrix_height, matrix_width, filter_mode)
     err = ctypes.create_string_buffer(1024)
     rc = lib.scamp_gb300_validate(ctypes.byref(ca), err, 1024)
     _check(rc, err)
@@ -234,7 +236,7 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
                 sum_b_ptr=None, corr_a_ptr=None, corr_b_ptr=None, stream=0,
                 anchor_interval=0, device=0, max_tile_size=128000, max_a_ptr=None,
                 max_b_ptr=None, knn_a_ptr=None, knn_b_ptr=None, matrix_ptr=None,
-                max_matches=5, matrix_height=50, matrix_width=50):
+                max_matches=5, matrix_height=50, matrix_width=50, filter_mode=0):
     """scamp_gb300_join_dev: every pointer is device memory (integers, e.g.
     ``tensor.data_ptr()``), results merged in place, ordered on ``stream``.
     ``max_a_ptr`` / ``max_b_ptr``: float32 profiles of the 1NN type;
@@ -243,7 +245,8 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
     lib = _lib.load()
     ca = _args(None, None, m, profile, precision, computing_rows, computing_cols,
                keep_rows, aligned, threshold, -1, -1, max_tile_size,
-               anchor_interval, device, True, max_matches, matrix_height, matrix_width)
+               anchor_interval, device, True, max_matches, matrix_height, matrix_width,
+               filter_mode)
     ca.timeseries_a = a_ptr
     ca.len_a = int(len_a)
     if b_ptr is not None:

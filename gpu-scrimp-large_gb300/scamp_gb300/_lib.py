@@ -74,7 +74,8 @@ class CArgs(ctypes.Structure):
         ("max_matches_per_column", ctypes.c_int32),
         ("matrix_height", ctypes.c_int32),
         ("matrix_width", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 3),
+        ("filter_mode", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
     ]
 
 

@@ -82,7 +82,12 @@ typedef struct scamp_c_args {
   int32_t max_matches_per_column;
   int32_t matrix_height;
   int32_t matrix_width;
-  int32_t reserved[3];
+  /* Mixed form's fast-path filter (tuning override, 0 = automatic): 1 = the
+   * largest per-cell correlation of each 8 x 8 block, 2 = a per-block bound
+   * (largest covariance times the largest inverse norms), cheaper where
+   * neighbouring windows' norms are close (long windows). */
+  int32_t filter_mode;
+  int32_t reserved[2];
 } scamp_c_args;
 
 /* Results.  Profiles are in/out: on entry they hold the best-so-far values

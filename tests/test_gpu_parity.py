@@ -20,9 +20,10 @@ def rw(rng, n):
 
 
 def run_1nn(engine, oracle, a, b, m, precision, tol, keep_rows=False, rows=True,
-            aligned=False, name="", brute=False, oracle_precision=3, **kw):
+            aligned=False, name="", brute=False, oracle_precision=3, filter_mode=0, **kw):
     got = engine.join(a, b, m, "1NN_INDEX", precision, computing_rows=rows,
-                      keep_rows=keep_rows, aligned=aligned, return_corr=True, **kw)
+                      keep_rows=keep_rows, aligned=aligned, return_corr=True,
+                      filter_mode=filter_mode, **kw)
     # exact_flat: flatness decided from an exact ssd (the engine's rule); the
     # reference's sequential ssd can leave flat windows "valid".
     want = oracle.join(a, b, m, "1NN_INDEX", computing_rows=rows, keep_rows=keep_rows,
@@ -386,3 +387,27 @@ def test_seeded_selfjoin(gpu_engine, oracle_mod):
     a = rw(rng, 1 << 17)
     got, _ = run_1nn(gpu_engine, oracle_mod, a, None, 128, "mixed", TOL_MIXED, name="seeded_self")
     assert got["gpu_launches"] > 8
+
+
+@pytest.mark.parametrize("filter_mode", [1, 2])
+def test_mixed_filters_both_forms(gpu_engine, oracle_mod, filter_mode):
+    """The mixed band kernel's two fast-path filters (per-cell r, and the
+    per-step covariance bound chosen for long windows) give the same
+    parity, at short and long windows, self and AB, 1NN_INDEX and
+    SUM_THRESH."""
+    rng = np.random.default_rng(31)
+    a = rw(rng, 6000)
+    b = rw(rng, 4500)
+    a[rng.choice(6000, 8, replace=False)] = np.nan
+    for m in (16, 100, 700):
+        run_1nn(gpu_engine, oracle_mod, a, None, m, "mixed", TOL_MIXED,
+                name="filter%d/self%d" % (filter_mode, m), filter_mode=filter_mode)
+        run_1nn(gpu_engine, oracle_mod, a, b, m, "mixed", TOL_MIXED, keep_rows=True,
+                name="filter%d/ab%d" % (filter_mode, m), filter_mode=filter_mode)
+        got = gpu_engine.join(a, b, m, "SUM_THRESH", "mixed", threshold=0.6, keep_rows=True,
+                              filter_mode=filter_mode)
+        want = oracle_mod.join(a, b, m, "SUM_THRESH", threshold=0.6, keep_rows=True)
+        check_sum("filter%d/sum%d/A" % (filter_mode, m), got["sum_a"], want["sum_a"], 0.6,
+                  2e-5, TOL_MIXED)
+        check_sum("filter%d/sum%d/B" % (filter_mode, m), got["sum_b"], want["sum_b"], 0.6,
+                  2e-5, TOL_MIXED)
