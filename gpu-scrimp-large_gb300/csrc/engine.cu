@@ -35,6 +35,9 @@ int mixed_1nn_band_width();
 int mixed_1nn_slab_rows();
 int mixed_1nn_threads();
 size_t mixed_1nn_smem_bytes();
+size_t anchor_gemm_smem_bytes();
+int anchor_tile_cols();
+int anchor_rows_per_tile();
 int measure_pipe_peak(int device, int kind, double* ops_per_s);
 
 namespace {
@@ -66,6 +69,18 @@ int64_t default_anchor_interval(int64_t m) {
 // noisy walk, m = 1024: 1430 / 1458 (1.5e8 / 9.0e6); a 2^21-sample walk
 // with NaN gaps, m = 4096: 368 / 412.
 constexpr int64_t kCoarseFilterMinWindow = 1024;
+
+// Windows from which the mixed form takes its anchors from the tensor-core
+// contraction (anchor_tc.cu) when the anchor interval allows it (a multiple
+// of 1024 rows): the CUDA-core anchors cost m FMAs per diagonal per K rows,
+// m / (2K) of the recurrence's work, 1/64 at K = 32 m but up to 1/8 where K
+// stops growing (m = 4096 at 16384 rows).
+constexpr int64_t kTcMinWindow = 512;
+// Budget of one chunk's anchor table (bytes); a chunk covers at least 16
+// unit rows (32 anchor rows, one tile of the contraction).
+constexpr double kTcTableBudget = 4.0 * (1 << 30);
+// Largest |anchor - FP64| inv_r inv_c the self-check accepts.
+constexpr double kTcCheckTol = 1e-5;
 
 // Anchor interval of joins that start cold (batched joins: diagonal seeds
 // only, the bests still rising through the first slabs): 8 m within [1024,
@@ -271,6 +286,12 @@ struct Workspace {
   // join's max_tie_margin (1NN) or max_abs_r_err (SUM_THRESH)
   bool tracked_tie_margin = false;
   bool tracked_sum_margin = false;
+  // Tensor-core anchors: 0 = not checked yet, 1 = checked (tc_desc_mode
+  // holds the descriptor orientation that matched FP64), 2 = unavailable;
+  // tc_check_err: the self-check's max |anchor - FP64| inv_r inv_c.
+  int tc_state = 0;
+  int tc_desc_mode = 0;
+  double tc_check_err = 0.0;
   // Verification requests of the mixed 1NN join: capacity of the buffer, and
   // the largest count a join asked for (the buffer grows to it on the next
   // join; requests beyond the capacity are verified inline, more slowly).
@@ -315,6 +336,7 @@ enum Slot {
   S_PREFIX, S_COUNTER, S_T32_A, S_T32_B, S_BHI_A, S_BLO_A, S_MUREL_A,
   S_BHI_B, S_BLO_B, S_MUREL_B, S_VREQ, S_PAA_A, S_PAA_B, S_SEED_A, S_SEED_B,
   S_BATCH, S_MAX_A, S_MAX_B, S_KNN_A, S_KNN_B, S_MAT,
+  S_TC_TAB, S_TC_W, S_TC_XS, S_TC_RAW, S_TC_OUT,
 };
 
 #define CUDA_TRY(expr)                                                     \
@@ -376,6 +398,119 @@ SeriesDev to_dev(const SeriesBufs& s, int64_t n, int64_t ns) {
   d.T32 = s.T32; d.bhi = s.bhi; d.blo = s.blo; d.mu_rel = s.mu_rel; d.bshift = s.bshift;
   d.n = n; d.ns = ns;
   return d;
+}
+
+// One problem's chunk of tensor-core anchors: anchor rows s0 .. s0 + nrows
+// - 1 of the row series against every diagonal of the problem, into `table`
+// (nrows x wp_pad floats, the layout of anchor_tc.cu).
+int tc_anchor_chunk(Workspace& ws, const Problem& pr, int64_t K, int64_t s0, int64_t nrows,
+                    int64_t wp_pad, float* table, int* error_flag, int desc_mode,
+                    cudaStream_t st, std::string* msg, AnchorArgs* out_args = nullptr) {
+  AnchorArgs A{};
+  A.R = pr.R;
+  A.C = pr.C;
+  A.m = pr.m;
+  A.m_pad = (pr.m + 15) / 16 * 16;
+  A.K = K;
+  A.d_lo = pr.d_lo;
+  A.s0 = s0;
+  A.nrows = nrows;
+  const int64_t rpt = anchor_rows_per_tile();
+  A.rows_pad = (nrows + rpt - 1) / rpt * rpt;
+  A.wp_pad = wp_pad;
+  A.col_tiles = ((rpt - 1) * K + wp_pad) / anchor_tile_cols();
+  A.table = table;
+  A.error_flag = error_flag;
+  A.desc_mode = desc_mode;
+  void* p;
+  int rc;
+  if ((rc = ensure(ws, S_TC_W, static_cast<size_t>(3 * A.rows_pad * A.m_pad) * 2, &p, msg))) return rc;
+  A.wsplit = static_cast<__nv_bfloat16*>(p);
+  if ((rc = ensure(ws, S_TC_XS, static_cast<size_t>(A.rows_pad) * 4, &p, msg))) return rc;
+  A.xsum = static_cast<float*>(p);
+  anchor_split_kernel<<<static_cast<unsigned>(A.rows_pad), 256, 0, st>>>(A);
+  const size_t smem = anchor_gemm_smem_bytes();
+  CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(anchor_gemm_kernel),
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  const int64_t tiles = (A.rows_pad / rpt) * A.col_tiles;
+  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(ws.sms, tiles));
+  anchor_gemm_kernel<<<static_cast<unsigned>(grid), 128, smem, st>>>(A);
+  CUDA_TRY(cudaGetLastError());
+  if (out_args) *out_args = A;
+  return SCAMP_OK;
+}
+
+// Self-check of the tensor-core anchors, once per device: a seeded random
+// walk (32768 samples, m = 512, anchor interval 1024) is joined's anchors
+// computed both ways; the descriptor orientation whose table matches FP64
+// direct dots to kTcCheckTol is kept, else the tensor-core path stays off
+// (the band kernel's own anchors serve every join).  Uses the series-A
+// slots (the join computes its statistics afterwards) and synchronises.
+int tc_self_check(Workspace& ws, cudaStream_t st, std::string* msg) {
+  constexpr int64_t n = 32768, m = 512, K = 1024;
+  std::vector<double> x(n);
+  uint64_t z = 0x9E3779B97F4A7C15ull;
+  double v = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    // xorshift increments, uniform in [-0.5, 0.5): a random walk
+    z ^= z << 13;
+    z ^= z >> 7;
+    z ^= z << 17;
+    v += static_cast<double>(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    x[static_cast<size_t>(i)] = v;
+  }
+  void* p;
+  int rc;
+  if ((rc = ensure(ws, S_TC_RAW, n * 8, &p, msg))) return rc;
+  double* raw = static_cast<double*>(p);
+  CUDA_TRY(cudaMemcpyAsync(raw, x.data(), n * 8, cudaMemcpyHostToDevice, st));
+  const int64_t ns = n - m + 1;
+  SeriesBufs sb{};
+  sb.bshift = block_shift(m);
+  if ((rc = alloc_series(ws, 0, n, ns, &sb, msg))) return rc;
+  const int chunk = 64;
+  stats_kernel<<<static_cast<unsigned>(((ns + chunk - 1) / chunk + 127) / 128), 128, 0, st>>>(
+      raw, n, m, 0, chunk, sb.bshift, sb.T, sb.T32, sb.bhi, sb.blo, sb.mu_rel, sb.mean, sb.inv,
+      sb.df, sb.dg, sb.inv32, sb.df32, sb.dg32);
+  CUDA_TRY(cudaGetLastError());
+  Problem pr{};
+  pr.R = pr.C = to_dev(sb, n, ns);
+  pr.d_lo = m / 4;
+  pr.d_hi = ns;
+  pr.m = m;
+  const int64_t nrows = 32;
+  const int64_t wp_pad = (ns - pr.d_lo + 1023) / 1024 * 1024;
+  if ((rc = ensure(ws, S_TC_TAB, static_cast<size_t>(nrows * wp_pad) * 4, &p, msg))) return rc;
+  float* table = static_cast<float*>(p);
+  if ((rc = ensure(ws, S_TC_OUT, 64, &p, msg))) return rc;
+  unsigned long long* out = static_cast<unsigned long long*>(p);
+  int* flag = reinterpret_cast<int*>(out + 4);
+  ws.tc_state = 2;
+  for (int mode = 0; mode < 2; ++mode) {
+    CUDA_TRY(cudaMemsetAsync(out, 0, 64, st));
+    CUDA_TRY(cudaMemsetAsync(table, 0, static_cast<size_t>(nrows * wp_pad) * 4, st));
+    AnchorArgs A{};
+    if ((rc = tc_anchor_chunk(ws, pr, K, 0, nrows, wp_pad, table, flag, mode, st, msg, &A))) return rc;
+    anchor_check_kernel<<<static_cast<unsigned>(ws.sms * 4), 256, 0, st>>>(A, 7, out);
+    CUDA_TRY(cudaGetLastError());
+    unsigned long long h[5] = {0, 0, 0, 0, 0};
+    CUDA_TRY(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    double err;
+    std::memcpy(&err, &h[0], 8);
+    if (static_cast<int>(h[4] & 0xFFFFFFFFull) != 0) {
+      *msg = "Error: tensor-core anchor self-check timed out on the device";
+      return SCAMP_ERR_DEVICE_TIMEOUT;
+    }
+    if (mode == 0 || err < ws.tc_check_err) ws.tc_check_err = h[1] > 1000 ? err : 1.0;
+    if (h[1] > 1000 && err <= kTcCheckTol) {
+      ws.tc_state = 1;
+      ws.tc_desc_mode = mode;
+      ws.tc_check_err = err;
+      break;
+    }
+  }
+  return SCAMP_OK;
 }
 
 // Runs a join whose inputs are device pointers; profile_a/b (packed entries)
@@ -498,6 +633,12 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   if (!nested) {
     ws.timed_kernel = false;
     ws.timed_verify = false;
+    // the tensor-core anchors' one-time self-check (before this join's own
+    // statistics, whose buffers it borrows)
+    if (mixed && !visit && ws.tc_state == 0 && a->anchor_mode != 1 &&
+        (a->anchor_mode == 2 || m >= kTcMinWindow)) {
+      if ((rc = tc_self_check(ws, st, msg))) return rc;
+    }
     CUDA_TRY(cudaEventRecord(ws.ev0, st));
   }
 
@@ -688,6 +829,10 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     const int64_t blk = 1ll << block_shift(m);
     if (K % blk) K = std::max<int64_t>(blk, (K / blk) * blk);
   }
+  // Tensor-core anchors need an anchor interval of whole 1024-column tiles.
+  const bool tc_eligible = kind == K_MIXED && !nested && ws.tc_state == 1 &&
+                           (a->anchor_mode == 2 || (a->anchor_mode == 0 && m >= kTcMinWindow));
+  if (tc_eligible && K >= 1024) K = K / 1024 * 1024;
 
   JoinParams P{};
   std::vector<int64_t> prefix;
@@ -726,10 +871,16 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   P.refresh_cols = (kind == K_MIXED && is_1nn && !seed_a) ? 1 : 0;
   P.threshold = a->distance_threshold;
   P.kl = kl;
+  // Tensor-core anchors (anchor_tc.cu): mixed joins of long windows whose
+  // anchor interval is a multiple of the contraction's 1024-column tiles.
+  const bool use_tc = tc_eligible && K % 1024 == 0;
   {
-    // FP32 anchor: blocks of up to 2^bshift terms, then the block sums.
+    // FP32 anchor: blocks of up to 2^bshift terms, then the block sums; the
+    // tensor-core contraction instead rounds its hi*hi accumulator m/16 times
+    // (the five small products go to a second accumulator).
     const double blk = static_cast<double>(1 << sa.bshift);
-    const double e = std::sqrt(std::min<double>(m, blk)) + std::sqrt(std::ceil(m / blk) + 1.0);
+    const double e = use_tc ? std::sqrt(m / 16.0 + 1.0) + std::sqrt(std::ceil(m / blk) + 1.0) + 1.0
+                            : std::sqrt(std::min<double>(m, blk)) + std::sqrt(std::ceil(m / blk) + 1.0);
     P.anchor_vcoef = static_cast<float>(e * e / 8.0);  // per 8-row step units
     for (int p = 0; p < P.nprob; ++p) P.prob[p].anchor_vcoef = P.anchor_vcoef;
   }
@@ -771,16 +922,74 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
       CUDA_TRY(cudaEventRecord(ws.evk0, st));
       ws.timed_kernel = true;
     }
-    if (kind == K_MIXED) {
+    auto launch_band = [&](const JoinParams& Q, int64_t g) {
       if (is_1nn && coarse)
-        join_mixed_1nn_coarse_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
+        join_mixed_1nn_coarse_kernel<<<static_cast<unsigned>(g), nthreads, smem, st>>>(Q);
       else if (is_1nn)
-        join_mixed_1nn_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
+        join_mixed_1nn_kernel<<<static_cast<unsigned>(g), nthreads, smem, st>>>(Q);
       else if (coarse)
-        join_mixed_sum_coarse_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
+        join_mixed_sum_coarse_kernel<<<static_cast<unsigned>(g), nthreads, smem, st>>>(Q);
       else
-        join_mixed_sum_kernel<<<static_cast<unsigned>(grid), nthreads, smem, st>>>(P);
+        join_mixed_sum_kernel<<<static_cast<unsigned>(g), nthreads, smem, st>>>(Q);
       ++launches;
+    };
+    if (kind == K_MIXED && use_tc) {
+      // Chunks of unit rows (every band's units ub in [u0, u0 + U)): the
+      // tensor-core contraction fills the chunk's anchor table (anchor rows
+      // 2 u0 .. 2 (u0 + U) - 1 of every problem), then one band-kernel launch
+      // runs the chunk's units with their anchors read from it.
+      int64_t wp[kMaxProblems] = {0, 0}, wsum = 0, urows = 0;
+      for (int p = 0; p < P.nprob; ++p) {
+        wp[p] = P.prob[p].nbands * W;
+        wsum += wp[p];
+        const int64_t rows0 = band_rows(P.prob[p].R.ns, P.prob[p].C.ns, P.prob[p].d_lo);
+        urows = std::max<int64_t>(urows, (rows0 + 2 * K - 1) / (2 * K));
+      }
+      int64_t U = static_cast<int64_t>(kTcTableBudget / (8.0 * static_cast<double>(wsum)));
+      U = std::max<int64_t>(16, U / 16 * 16);
+      void* tp;
+      if ((rc = ensure(ws, S_TC_TAB, static_cast<size_t>(2 * U * wsum) * 4, &tp, msg))) return rc;
+      float* tab = static_cast<float*>(tp);
+      std::vector<int64_t> cpre;
+      for (int64_t u0 = 0; u0 < urows; u0 += U) {
+        cpre.assign(1, 0);
+        for (int p = 0; p < P.nprob; ++p) {
+          const Problem& pr = P.prob[p];
+          for (int64_t b = 0; b < pr.nbands; ++b) {
+            const int64_t rows = band_rows(pr.R.ns, pr.C.ns, pr.d_lo + b * W);
+            const int64_t ub = (rows + 2 * K - 1) / (2 * K);
+            cpre.push_back(cpre.back() + std::max<int64_t>(0, std::min<int64_t>(ub - u0, U)));
+          }
+        }
+        const int64_t cunits = cpre.back();
+        if (cunits == 0) continue;
+        JoinParams Q = P;
+        Q.total_units = cunits;
+        Q.unit_row0 = u0;
+        float* tp_p = tab;
+        for (int p = 0; p < P.nprob; ++p) {
+          const int64_t s0 = 2 * u0;
+          const int64_t srows = std::max<int64_t>(
+              0, std::min<int64_t>(2 * U, (band_rows(P.prob[p].R.ns, P.prob[p].C.ns, P.prob[p].d_lo) +
+                                           K - 1) / K - s0));
+          Q.prob[p].anchor_tab = tp_p;
+          Q.prob[p].tab_wp = wp[p];
+          Q.prob[p].tab_s0 = s0;
+          if (srows > 0 && (rc = tc_anchor_chunk(ws, P.prob[p], K, s0, srows, wp[p], tp_p,
+                                                 P.error_flag, ws.tc_desc_mode, st, msg)))
+            return rc;
+          launches += srows > 0 ? 2 : 0;
+          tp_p += 2 * U * wp[p];
+        }
+        CUDA_TRY(cudaMemcpyAsync(dprefix, cpre.data(), cpre.size() * 8, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemsetAsync(P.unit_counter, 0, 8, st));
+        launch_band(Q, std::min<int64_t>(resident, cunits));
+      }
+      CUDA_TRY(cudaGetLastError());
+    } else if (kind == K_MIXED) {
+      launch_band(P, grid);
+    }
+    if (kind == K_MIXED) {
       if (!nested) {
         CUDA_TRY(cudaEventRecord(ws.evkv, st));
         ws.timed_verify = true;
@@ -875,10 +1084,13 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   return SCAMP_OK;
 }
 
-void read_times(Workspace& ws, scamp_c_result* res) {
+// Timing fields, work counters and the device error word of the last join
+// (SCAMP_ERR_DEVICE_TIMEOUT when a bounded wait on the device gave up).
+int read_times(Workspace& ws, scamp_c_result* res, std::string* msg = nullptr) {
   res->steps = res->slow_steps = res->verifications = 0;
+  int status = SCAMP_OK;
   if (ws.timed_kernel && ws.bufs.size() > S_COUNTER && ws.bufs[S_COUNTER].p) {
-    unsigned long long c[6] = {0, 0, 0, 0, 0, 0};
+    unsigned long long c[7] = {0, 0, 0, 0, 0, 0, 0};
     if (cudaMemcpy(c, ws.bufs[S_COUNTER].p, sizeof(c), cudaMemcpyDeviceToHost) == cudaSuccess) {
       res->steps = c[1];
       res->slow_steps = c[2];
@@ -889,6 +1101,10 @@ void read_times(Workspace& ws, scamp_c_result* res) {
       std::memcpy(&tm, &bits, 4);
       if (ws.tracked_tie_margin) res->max_tie_margin = tm;
       if (ws.tracked_sum_margin) res->max_abs_r_err = tm;
+      if (static_cast<uint32_t>(c[6]) != 0) {
+        status = SCAMP_ERR_DEVICE_TIMEOUT;
+        if (msg) *msg = "Error: a wait on the tensor cores timed out on the device";
+      }
     }
   }
   float ms = 0;
@@ -905,6 +1121,7 @@ void read_times(Workspace& ws, scamp_c_result* res) {
       res->verify_kernel_ms = k;
     }
   }
+  return status;
 }
 
 int init_workspace(int device, Workspace** out, std::string* msg) {
@@ -963,6 +1180,24 @@ extern "C" int scamp_gb300_gpu_supported(void) {
 
 extern "C" const char* scamp_gb300_version(void) { return "scamp_gb300 0.1.0 (sm_103a)"; }
 
+extern "C" int scamp_gb300_anchor_check(int device, double* max_err, int* available,
+                                        char* errbuf, size_t errlen) {
+  std::string msg;
+  Workspace* ws;
+  int rc = init_workspace(device, &ws, &msg);
+  if (rc == SCAMP_OK) {
+    std::lock_guard<std::mutex> lock(ws->mu);
+    ws->tc_state = 0;
+    rc = tc_self_check(*ws, ws->stream, &msg);
+    if (rc == SCAMP_OK) {
+      if (max_err) *max_err = ws->tc_check_err;
+      if (available) *available = ws->tc_state == 1 ? 1 : 0;
+    }
+  }
+  if (rc) set_err(errbuf, errlen, msg);
+  return rc;
+}
+
 extern "C" int scamp_gb300_pipe_peak(int device, int kind, double* ops_per_s) {
   if (!ops_per_s || (kind != 0 && kind != 1)) return SCAMP_ERR_INVALID_ARGS;
   return measure_pipe_peak(device, kind, ops_per_s) ? SCAMP_ERR_CUDA : SCAMP_OK;
@@ -990,7 +1225,7 @@ extern "C" int scamp_gb300_join_dev(const scamp_c_args* args, scamp_c_result* re
     cudaError_t e = cudaEventSynchronize(ws->ev1);
     if (e != cudaSuccess) { msg = std::string("CUDA error: ") + cudaGetErrorString(e); rc = SCAMP_ERR_CUDA; }
     else {
-      read_times(*ws, res);
+      rc = read_times(*ws, res, &msg);
     }
   }
   if (rc) set_err(errbuf, errlen, msg);
@@ -1104,7 +1339,7 @@ extern "C" int scamp_gb300_join(const scamp_c_args* args, scamp_c_result* res,
     }
   }
   HOST_CUDA(cudaStreamSynchronize(st));
-  read_times(*ws, res);
+  if ((rc = read_times(*ws, res, &msg))) return fail(rc);
   return SCAMP_OK;
 #undef HOST_CUDA
 }

@@ -7,8 +7,10 @@
 // (src/cpu_kernels.cpp:166-171, src/kernels_compute.h:425-435) and its Pearson
 // correlation is r = cov * invnorm_c[j] * invnorm_r[i].
 #pragma once
-#include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <cstdint>
 
 namespace scamp_gb300 {
 
@@ -118,6 +120,12 @@ struct Problem {
   int64_t m;            // window length
   int64_t seg_len;      // K: rows per segment (mixed 1NN kernel)
   float anchor_vcoef;   // initial drift estimate of an anchor / cov^2 (mixed 1NN)
+  // Tensor-core anchors (anchor_tc.cu), or null: row s - tab_s0 of the table
+  // holds the anchors cov(sK, sK + d) of the diagonals d_lo .. d_lo + tab_wp
+  // - 1, blocks of 1024 diagonals stored residue-major.
+  const float* anchor_tab;
+  int64_t tab_wp;
+  int64_t tab_s0;
 };
 
 constexpr int kMaxProblems = 2;
@@ -139,6 +147,7 @@ struct JoinParams {
   const Problem* batch;
   int64_t nbatch;
   const int64_t* band_unit_prefix;  // [total_bands + 1] unit offsets
+  int64_t unit_row0;                // first unit of every band in this launch (chunked joins)
   int64_t total_bands;
   int64_t total_units;
   unsigned long long* unit_counter; // persistent work queue head
@@ -195,7 +204,7 @@ __device__ __forceinline__ void decode_unit(const JoinParams& P, int64_t u,
     *band = lo - P.prob[p].band_begin;
   }
   *prob = p;
-  *unit_in_band = u - P.band_unit_prefix[lo];
+  *unit_in_band = u - P.band_unit_prefix[lo] + P.unit_row0;
 }
 
 __device__ __forceinline__ const Problem& problem_of(const JoinParams& P, int p) {
@@ -252,6 +261,28 @@ __global__ void join_mixed_sum_kernel(JoinParams P);  // mixed SUM_THRESH
 __global__ void join_mixed_1nn_coarse_kernel(JoinParams P);
 __global__ void join_mixed_sum_coarse_kernel(JoinParams P);
 __global__ void verify_requests_kernel(JoinParams P);
+
+// Tensor-core anchors of one problem's chunk of anchor rows (anchor_tc.cu).
+struct AnchorArgs {
+  SeriesDev R, C;          // row and column series
+  int64_t m, m_pad;        // window; terms padded to a multiple of 16
+  int64_t K;               // anchor interval (a multiple of 1024)
+  int64_t d_lo;            // first diagonal of the problem
+  int64_t s0, nrows;       // anchor rows s0 .. s0 + nrows - 1
+  int64_t rows_pad;        // nrows rounded up to the tile's 32 rows
+  int64_t wp_pad;          // diagonals per table row (multiple of 1024)
+  int64_t col_tiles;       // 1024-column tiles per group of 32 rows
+  __nv_bfloat16* wsplit;   // [3][rows_pad][m_pad] split centred anchor windows
+  float* xsum;             // [rows_pad] sums of the windows' values
+  float* table;            // [nrows][wp_pad]
+  int* error_flag;         // set when a wait on the tensor cores gives up
+  int desc_mode;           // shared-memory descriptor orientation (self-check)
+};
+__global__ void anchor_split_kernel(AnchorArgs A);
+__global__ void anchor_gemm_kernel(AnchorArgs A);
+// FP64 check of a table: every `stride`-th entry against a direct FP64 dot;
+// out[0] = max |table - cov| inv_r inv_c (as ordered bits), out[1] = count.
+__global__ void anchor_check_kernel(AnchorArgs A, int64_t stride, unsigned long long* out);
 
 // Seeds of the mixed 1NN join from a block-averaged pre-pass.
 struct SeedArgs {

@@ -564,7 +564,22 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
     const bool live1 = seg_len[1] > 0;
     const int64_t nblk_c = (pr.C.n + (int64_t{1} << sh) - 1) >> sh;
     int64_t span_b0 = 0;
-    for (int64_t t0 = 0; t0 < m; t0 += kAnchorChunk) {
+    // anchors from the tensor-core table (anchor_tc.cu) when the join has one
+    const bool tab = pr.anchor_tab != nullptr;
+    if (tab) {
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const bool live = g == 0 ? seg_len[0] > 0 : live1;
+        const float* rowp = pr.anchor_tab + (seg_row[g] / K - pr.tab_s0) * pr.tab_wp +
+                            band * kBand + t;
+#pragma unroll
+        for (int k = 0; k < kDiags; ++k) {
+          const float v = (live && jb[g] + k < pr.C.ns) ? rowp[k * 128] : 0.f;
+          if (g) acc2[k].y = v; else acc2[k].x = v;
+        }
+      }
+    }
+    for (int64_t t0 = 0; t0 < (tab ? 0 : m); t0 += kAnchorChunk) {
       const int chunk = static_cast<int>((m - t0) < kAnchorChunk ? (m - t0) : kAnchorChunk);
       {
         const int64_t i0 = seg_row[0], i1 = seg_row[1];
@@ -657,7 +672,7 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
 #pragma unroll
       for (int g = 0; g < 2; ++g) {
         const int64_t j = jb[g] + k;
-        if (j >= pr.C.ns || (g == 1 && !live1)) continue;
+        if (tab || j >= pr.C.ns || (g == 1 && !live1)) continue;
         const float ek = (pr.C.mu_rel[j] + block_delta(pr.C, j >> sh, b0s[g])) - mu0[g];
         if (g) acc2[k].y = fmaf(-ek, xsum2.y, acc2[k].y);
         else acc2[k].x = fmaf(-ek, xsum2.x, acc2[k].x);

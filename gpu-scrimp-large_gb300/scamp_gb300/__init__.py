@@ -57,7 +57,7 @@ def gpu_supported():
 def _args(a, b, m, profile, precision, computing_rows, computing_cols,
           keep_rows, aligned, threshold, start_row, start_col, max_tile_size,
           anchor_interval, device, silent, max_matches=5, matrix_height=50, matrix_width=50,
-          filter_mode=0):
+          filter_mode=0, anchor_mode=0):
     ca = _lib.CArgs()
     ca.timeseries_a = a.ctypes.data if a is not None else None
     ca.len_a = len(a) if a is not None else 0
@@ -82,6 +82,7 @@ def _args(a, b, m, profile, precision, computing_rows, computing_cols,
     ca.matrix_height = int(matrix_height)
     ca.matrix_width = int(matrix_width)
     ca.filter_mode = int(filter_mode)
+    ca.anchor_mode = int(anchor_mode)
     return ca
 
 
@@ -112,6 +113,19 @@ def pipe_peak(kind="fp32", device=0):
     return out.value
 
 
+def anchor_check(device=0):
+    """Self-check of the mixed form's tensor-core anchors (C ABI
+    scamp_gb300_anchor_check): (largest |anchor - FP64 cov| * invnorm_r *
+    invnorm_c on a seeded random walk, True when joins use them)."""
+    err = ctypes.c_double(0)
+    avail = ctypes.c_int(0)
+    buf = ctypes.create_string_buffer(1024)
+    rc = _lib.load().scamp_gb300_anchor_check(int(device), ctypes.byref(err), ctypes.byref(avail),
+                                              buf, 1024)
+    _check(rc, buf)
+    return err.value, bool(avail.value)
+
+
 def _check(rc, err):
     if rc != _lib.SCAMP_OK:
         msg = err.value.decode(errors="replace") or _lib.ERROR_NAMES.get(rc, str(rc))
@@ -125,7 +139,7 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
          aligned=False, threshold=0.0, start_row=-1, start_col=-1,
          max_tile_size=128000, anchor_interval=0, device=0, profile_a=None,
          profile_b=None, return_corr=False, silent=True, inplace=False, max_matches=5,
-         matrix_height=50, matrix_width=50, filter_mode=0):
+         matrix_height=50, matrix_width=50, filter_mode=0, anchor_mode=0):
     """Run one join (the C ABI's scamp_gb300_join, host buffers; the
     reference's SCAMP::do_SCAMP, src/SCAMP.cpp:261-334, with the arguments
     of SCAMPArgs, src/common.h:164-188).
@@ -154,7 +168,7 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
     ca = _args(a, b, m, profile, precision, computing_rows, computing_cols,
                keep_rows, aligned, threshold, start_row, start_col,
                max_tile_size, anchor_interval, device, silent, max_matches,
-               matrix_height, matrix_width, filter_mode)
+               matrix_height, matrix_width, filter_mode, anchor_mode)
     err = ctypes.create_string_buffer(1024)
     rc = lib.scamp_gb300_validate(ctypes.byref(ca), err, 1024)
     _check(rc, err)
@@ -236,7 +250,8 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
                 sum_b_ptr=None, corr_a_ptr=None, corr_b_ptr=None, stream=0,
                 anchor_interval=0, device=0, max_tile_size=128000, max_a_ptr=None,
                 max_b_ptr=None, knn_a_ptr=None, knn_b_ptr=None, matrix_ptr=None,
-                max_matches=5, matrix_height=50, matrix_width=50, filter_mode=0):
+                max_matches=5, matrix_height=50, matrix_width=50, filter_mode=0,
+                anchor_mode=0):
     """scamp_gb300_join_dev: every pointer is device memory (integers, e.g.
     ``tensor.data_ptr()``), results merged in place, ordered on ``stream``.
     ``max_a_ptr`` / ``max_b_ptr``: float32 profiles of the 1NN type;
@@ -246,7 +261,7 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
     ca = _args(None, None, m, profile, precision, computing_rows, computing_cols,
                keep_rows, aligned, threshold, -1, -1, max_tile_size,
                anchor_interval, device, True, max_matches, matrix_height, matrix_width,
-               filter_mode)
+               filter_mode, anchor_mode)
     ca.timeseries_a = a_ptr
     ca.len_a = int(len_a)
     if b_ptr is not None:

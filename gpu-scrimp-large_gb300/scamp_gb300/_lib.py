@@ -42,6 +42,7 @@ EXPORTED_SYMBOLS = (
     "scamp_gb300_count_cells",
     "scamp_gb300_gpu_supported",
     "scamp_gb300_pipe_peak",
+    "scamp_gb300_anchor_check",
     "scamp_gb300_version",
 )
 
@@ -75,7 +76,8 @@ class CArgs(ctypes.Structure):
         ("matrix_height", ctypes.c_int32),
         ("matrix_width", ctypes.c_int32),
         ("filter_mode", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 2),
+        ("anchor_mode", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 1),
     ]
 
 
@@ -153,6 +155,9 @@ def load():
     lib.scamp_gb300_gpu_supported.restype = ctypes.c_int
     lib.scamp_gb300_pipe_peak.argtypes = [ctypes.c_int, ctypes.c_int, _dp]
     lib.scamp_gb300_pipe_peak.restype = ctypes.c_int
+    lib.scamp_gb300_anchor_check.argtypes = [ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_int),
+                                             ctypes.c_char_p, ctypes.c_size_t]
+    lib.scamp_gb300_anchor_check.restype = ctypes.c_int
     lib.scamp_gb300_version.argtypes = []
     lib.scamp_gb300_version.restype = ctypes.c_char_p
     _lib = lib

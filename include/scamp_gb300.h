@@ -87,7 +87,11 @@ typedef struct scamp_c_args {
    * (largest covariance times the largest inverse norms), cheaper where
    * neighbouring windows' norms are close (long windows). */
   int32_t filter_mode;
-  int32_t reserved[2];
+  /* Mixed form's anchors (tuning override, 0 = automatic): 1 = FP32 dot
+   * products on the CUDA cores inside the band kernel, 2 = split-BF16x3
+   * contraction on the tensor cores into an anchor table. */
+  int32_t anchor_mode;
+  int32_t reserved[1];
 } scamp_c_args;
 
 /* Results.  Profiles are in/out: on entry they hold the best-so-far values
@@ -240,6 +244,17 @@ int scamp_gb300_gpu_supported(void);
  * kind 0 = FP32 FMA lane-ops/s (packed f32x2), 1 = FP64 FMA lane-ops/s.
  * Has no counterpart in the reference. */
 int scamp_gb300_pipe_peak(int device, int kind, double *ops_per_s);
+
+/* Self-check of the mixed form's tensor-core anchors on `device` (the
+ * check every process runs once before its first mixed join of long
+ * windows): anchors of a seeded random walk (32768 samples, m = 512) from the
+ * split-BF16x3 tcgen05 contraction against FP64 direct dot products.
+ * *max_err: the largest |anchor - cov| * invnorm_r * invnorm_c; *available:
+ * 1 when the joins use the tensor-core anchors (error within 1e-5), else 0
+ * (they use the band kernel's CUDA-core anchors).  Has no counterpart in
+ * the reference, whose seeds come from cuFFT (src/qt_helper.cpp:75-121). */
+int scamp_gb300_anchor_check(int device, double *max_err, int *available,
+                             char *errbuf, size_t errlen);
 
 /* Library version string. */
 const char *scamp_gb300_version(void);
