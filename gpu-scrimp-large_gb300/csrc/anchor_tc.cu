@@ -38,6 +38,19 @@
 // r from its stream.  Eight streams per split (one per residue) replace the
 // 1024 x m tile.
 //
+// Offset-free partial sums: the column operand is the series relative to
+// one offset per tile, y = T - y0, so a partial sum over part of a window
+// carries (local level - y0) * (sum of x over that part) -- much larger than
+// the covariance where the series wanders.  Each 64-term block of an anchor
+// window is therefore centred by its own mean xi_b before the split: with
+// x' = x - xi_b summing to zero over every block, the tensor cores only see
+// offset-free products, and the block means come back in the epilogue as
+//     sum_t x(t) y(j+t) = sum_t x'(t) y(j+t) + sum_b xi_b S_b(j),
+// S_b(j) the sum of y over block b of window j, from prefix sums of the tile's
+// span (double-float, in shared memory).  With S_b(j) - len_b (mu_j - y0) in
+// place of S_b(j) (the blocks' xi sum to the window's zero mean) every term
+// of the epilogue stays at the covariance's own scale.
+//
 // Anchor table layout (per problem): row s - s0 of the chunk holds the
 // anchors of diagonals d_lo .. d_lo + wp_pad - 1 in blocks of 1024
 // diagonals (the band width), each block stored residue-major: diagonal
@@ -65,6 +78,7 @@ constexpr int kSub = 64;                // terms per TMEM accumulation
 constexpr int kStreamLen = 8 * 127 + kKBlock;  // stream elements a pass reads
 constexpr int kStreamPad = kStreamLen + 8;      // padded (16-byte multiple)
 constexpr int kTmemCols = 256;          // 8 residues x 2 accumulators x 16 columns
+constexpr int kMaxPad = 8192;           // longest window (padded) the contraction serves
 
 // Shared memory of one CTA (dynamic): streams [3 splits][8 residues][kStreamPad]
 // bf16, the anchor-window operand [3 splits][kRowsPerTile x kKBlock] bf16 in
@@ -75,7 +89,17 @@ struct TcSmem {
   float xsum[kRowsPerTile];
   uint32_t tmem_base;
   unsigned long long mbar;
+  double part[kTcThreads];  // prefix-sum scan of the threads' span pieces
+  // followed in the dynamic allocation by: float2 pre[span + 1] (prefix sums
+  // of y as hi + lo) and float xi[kRowsPerTile][nsub]
 };
+
+// Dynamic shared memory of a contraction with m_pad window terms.
+__host__ __device__ inline size_t tc_smem_bytes(int64_t m_pad) {
+  const int64_t span = kTileCols + m_pad;
+  return sizeof(TcSmem) + static_cast<size_t>(span + 1) * sizeof(float2) +
+         static_cast<size_t>(kRowsPerTile * ((m_pad + 63) / 64)) * sizeof(float);
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -171,13 +195,16 @@ __device__ __forceinline__ float blk_delta(const SeriesDev& S, int64_t b, int64_
 
 }  // namespace
 
-// Centred anchor windows of one problem's chunk, split: out[split][row][t]
-// (rows padded to a multiple of kRowsPerTile, terms to m_pad; padding 0) and
-// xsum[row] = sum of the window's FP32 values (the split is exact).  Row
-// `row` is anchor row s = s0 + row, window sK of the row series, centred by
-// its FP64 mean from the same block-relative FP32 data the CUDA-core anchors
-// use.  One block per row.
+// Anchor windows of one problem's chunk, split: row `row` is anchor row
+// s = s0 + row, window sK of the row series centred by its FP64 mean, from
+// the same block-relative FP32 data the CUDA-core anchors use.  Each 64-term
+// block b is centred by its own mean: xi[row][b] = that mean, out[split][row]
+// [t] = the split of x(t) - xi_b (rows padded to a multiple of kRowsPerTile,
+// terms to m_pad; padding 0), xsum[row] = the sum of x(t) - xi_b (the split
+// is exact).  One block per row.
 __global__ void __launch_bounds__(256) anchor_split_kernel(AnchorArgs A) {
+  __shared__ float xs[kMaxPad];
+  __shared__ float red[256];
   const int64_t row = blockIdx.x;
   const int64_t s = A.s0 + row;
   const int64_t i = s * A.K;
@@ -186,10 +213,20 @@ __global__ void __launch_bounds__(256) anchor_split_kernel(AnchorArgs A) {
   const int sh = R.bshift;
   const int64_t bi = live ? (i >> sh) : 0;
   const float mr = live ? R.mu_rel[i] : 0.f;
+  for (int64_t t = threadIdx.x; t < A.m_pad; t += blockDim.x)
+    xs[t] = (live && t < A.m) ? R.T32[i + t] + (blk_delta(R, (i + t) >> sh, bi) - mr) : 0.f;
+  __syncthreads();
+  // block means (one thread per 64-term block)
+  for (int64_t b = threadIdx.x; b < A.nsub; b += blockDim.x) {
+    const int64_t t0 = 64 * b, t1 = (t0 + 64 < A.m) ? t0 + 64 : A.m;
+    float sum = 0.f;
+    for (int64_t t = t0; t < t1; ++t) sum += xs[t];
+    A.xi[row * A.nsub + b] = t1 > t0 ? sum / static_cast<float>(t1 - t0) : 0.f;
+  }
+  __syncthreads();
   float part = 0.f;
   for (int64_t t = threadIdx.x; t < A.m_pad; t += blockDim.x) {
-    float v = 0.f;
-    if (live && t < A.m) v = R.T32[i + t] + (blk_delta(R, (i + t) >> sh, bi) - mr);
+    const float v = t < A.m ? xs[t] - A.xi[row * A.nsub + (t >> 6)] : 0.f;
     __nv_bfloat16 h, md, l;
     split3(v, h, md, l);
     const int64_t o = row * A.m_pad + t;
@@ -198,7 +235,6 @@ __global__ void __launch_bounds__(256) anchor_split_kernel(AnchorArgs A) {
     A.wsplit[2 * A.rows_pad * A.m_pad + o] = l;
     part += v;
   }
-  __shared__ float red[256];
   red[threadIdx.x] = part;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
@@ -249,6 +285,43 @@ __global__ void __launch_bounds__(kTcThreads, 1) anchor_gemm_kernel(AnchorArgs A
     const int64_t J0 = s_first * A.K + A.d_lo + ct * kTileCols;
     if (J0 >= C.ns) continue;  // no column window of the tile exists (uniform)
     const int64_t bJ0 = (J0 < C.n ? J0 : C.n - 1) >> sh;  // offset block of the tile
+    // ---- prefix sums of the span y(J0 + p), p < span, as hi + lo floats ----
+    float2* pre = reinterpret_cast<float2*>(tc_raw + sizeof(TcSmem));
+    float* xi_s = reinterpret_cast<float*>(pre + (kTileCols + A.m_pad + 1));
+    {
+      const int64_t span = kTileCols + A.m_pad;
+      const int64_t per = (span + kTcThreads - 1) / kTcThreads;
+      const int64_t p0 = t * per, p1 = (p0 + per < span) ? p0 + per : span;
+      double run = 0.0;
+      for (int64_t p = p0; p < p1; ++p) {
+        const int64_t g = J0 + p;
+        if (g < C.n) run += static_cast<double>(C.T32[g] + blk_delta(C, g >> sh, bJ0));
+      }
+      sm.part[t] = run;
+      __syncthreads();
+      if (t == 0) {
+        double acc_p = 0.0;
+        for (int k = 0; k < kTcThreads; ++k) {
+          const double v = sm.part[k];
+          sm.part[k] = acc_p;
+          acc_p += v;
+        }
+      }
+      __syncthreads();
+      run = sm.part[t];
+      for (int64_t p = p0; p < p1; ++p) {
+        const float hi = static_cast<float>(run);
+        pre[p] = make_float2(hi, static_cast<float>(run - hi));
+        const int64_t g = J0 + p;
+        if (g < C.n) run += static_cast<double>(C.T32[g] + blk_delta(C, g >> sh, bJ0));
+      }
+      if (p1 == span && p0 < p1) {
+        const float hi = static_cast<float>(run);
+        pre[span] = make_float2(hi, static_cast<float>(run - hi));
+      }
+      for (int64_t q = t; q < kRowsPerTile * A.nsub; q += kTcThreads)
+        xi_s[q] = A.xi[(grp * kRowsPerTile) * A.nsub + q];
+    }
     float acc[8][kRowsPerTile];  // lane q's columns J0 + 8q + r, one per anchor row
 #pragma unroll
     for (int r = 0; r < 8; ++r)
@@ -350,17 +423,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) anchor_gemm_kernel(AnchorArgs A
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int64_t j = J0 + 8 * q + r;
-      // sum_t x (y(j + t) - y0) = cov + (mu_j - y0) sum_t x, with y0 the
-      // tile's offset block
+      const int o = 8 * q + r;  // j - J0
+      // cov = sum_t x'(y(j+t) - y0) + sum_b xi_b (S_b(j) - len_b ej) - ej sum x'
+      // with ej = mu_j - y0 (y0: the tile's offset block)
       float ej = 0.f;
       if (j < C.ns) ej = C.mu_rel[j] + blk_delta(C, j >> sh, bJ0);
+      float corr[kRowsPerTile];
+#pragma unroll
+      for (int n = 0; n < kRowsPerTile; ++n) corr[n] = -ej * sm.xsum[n];
+      for (int64_t b = 0; b < A.nsub; ++b) {
+        const int64_t t0 = 64 * b, t1 = (t0 + 64 < A.m) ? t0 + 64 : A.m;
+        const float2 pa = pre[o + t0], pb = pre[o + t1];
+        const float sbj = ((pb.x - pa.x) + (pb.y - pa.y)) - static_cast<float>(t1 - t0) * ej;
+#pragma unroll
+        for (int n = 0; n < kRowsPerTile; ++n) corr[n] = fmaf(xi_s[n * A.nsub + b], sbj, corr[n]);
+      }
 #pragma unroll
       for (int n = 0; n < kRowsPerTile; ++n) {
         const int64_t row = grp * kRowsPerTile + n;
         const int64_t s = A.s0 + row;
         const int64_t b = ct - (s - s_first) * kpb;  // diagonal block of row s
         if (row < A.nrows && b >= 0 && b < A.wp_pad / kTileCols)
-          A.table[row * A.wp_pad + b * kTileCols + r * 128 + q] = acc[r][n] - ej * sm.xsum[n];
+          A.table[row * A.wp_pad + b * kTileCols + r * 128 + q] = acc[r][n] + corr[n];
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -380,7 +464,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) anchor_gemm_kernel(AnchorArgs A
                  : "memory");
 }
 
-size_t anchor_gemm_smem_bytes() { return sizeof(TcSmem); }
+size_t anchor_gemm_smem_bytes(int64_t m_pad) { return tc_smem_bytes(m_pad); }
+int64_t anchor_max_window() { return kMaxPad; }
 int anchor_tile_cols() { return kTileCols; }
 int anchor_rows_per_tile() { return kRowsPerTile; }
 int anchor_kblock() { return kKBlock; }

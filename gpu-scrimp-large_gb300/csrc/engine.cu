@@ -35,7 +35,8 @@ int mixed_1nn_band_width();
 int mixed_1nn_slab_rows();
 int mixed_1nn_threads();
 size_t mixed_1nn_smem_bytes();
-size_t anchor_gemm_smem_bytes();
+size_t anchor_gemm_smem_bytes(int64_t m_pad);
+int64_t anchor_max_window();
 int anchor_tile_cols();
 int anchor_rows_per_tile();
 int measure_pipe_peak(int device, int kind, double* ops_per_s);
@@ -336,7 +337,7 @@ enum Slot {
   S_PREFIX, S_COUNTER, S_T32_A, S_T32_B, S_BHI_A, S_BLO_A, S_MUREL_A,
   S_BHI_B, S_BLO_B, S_MUREL_B, S_VREQ, S_PAA_A, S_PAA_B, S_SEED_A, S_SEED_B,
   S_BATCH, S_MAX_A, S_MAX_B, S_KNN_A, S_KNN_B, S_MAT,
-  S_TC_TAB, S_TC_W, S_TC_XS, S_TC_RAW, S_TC_OUT,
+  S_TC_TAB, S_TC_W, S_TC_XS, S_TC_RAW, S_TC_OUT, S_TC_XI,
 };
 
 #define CUDA_TRY(expr)                                                     \
@@ -422,14 +423,17 @@ int tc_anchor_chunk(Workspace& ws, const Problem& pr, int64_t K, int64_t s0, int
   A.table = table;
   A.error_flag = error_flag;
   A.desc_mode = desc_mode;
+  A.nsub = (A.m_pad + 63) / 64;
   void* p;
   int rc;
+  if ((rc = ensure(ws, S_TC_XI, static_cast<size_t>(A.rows_pad * A.nsub) * 4, &p, msg))) return rc;
+  A.xi = static_cast<float*>(p);
   if ((rc = ensure(ws, S_TC_W, static_cast<size_t>(3 * A.rows_pad * A.m_pad) * 2, &p, msg))) return rc;
   A.wsplit = static_cast<__nv_bfloat16*>(p);
   if ((rc = ensure(ws, S_TC_XS, static_cast<size_t>(A.rows_pad) * 4, &p, msg))) return rc;
   A.xsum = static_cast<float*>(p);
   anchor_split_kernel<<<static_cast<unsigned>(A.rows_pad), 256, 0, st>>>(A);
-  const size_t smem = anchor_gemm_smem_bytes();
+  const size_t smem = anchor_gemm_smem_bytes(A.m_pad);
   CUDA_TRY(cudaFuncSetAttribute(reinterpret_cast<const void*>(anchor_gemm_kernel),
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   const int64_t tiles = (A.rows_pad / rpt) * A.col_tiles;
@@ -831,6 +835,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   }
   // Tensor-core anchors need an anchor interval of whole 1024-column tiles.
   const bool tc_eligible = kind == K_MIXED && !nested && ws.tc_state == 1 &&
+                           (m + 15) / 16 * 16 <= anchor_max_window() &&
                            (a->anchor_mode == 2 || (a->anchor_mode == 0 && m >= kTcMinWindow));
   if (tc_eligible && K >= 1024) K = K / 1024 * 1024;
 

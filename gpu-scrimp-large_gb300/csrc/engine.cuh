@@ -272,8 +272,11 @@ struct AnchorArgs {
   int64_t rows_pad;        // nrows rounded up to the tile's 32 rows
   int64_t wp_pad;          // diagonals per table row (multiple of 1024)
   int64_t col_tiles;       // 1024-column tiles per group of 32 rows
-  __nv_bfloat16* wsplit;   // [3][rows_pad][m_pad] split centred anchor windows
-  float* xsum;             // [rows_pad] sums of the windows' values
+  __nv_bfloat16* wsplit;   // [3][rows_pad][m_pad] split anchor windows, each
+                           // 64-term block centred by its own mean
+  float* xsum;             // [rows_pad] sums of those block-centred values
+  float* xi;               // [rows_pad][nsub] the block means
+  int64_t nsub;            // 64-term blocks per window (m_pad / 64, rounded up)
   float* table;            // [nrows][wp_pad]
   int* error_flag;         // set when a wait on the tensor cores gives up
   int desc_mode;           // shared-memory descriptor orientation (self-check)
