@@ -389,10 +389,11 @@ def run_batch_workload(args, world, rank, local):
 
 
 # DRAM bytes (read + write) of one band-kernel launch on the 2^24-point
-# self-join, from a one-launch ncu capture of a smaller self-join of the same
-# distribution scaled by comparisons (join_mixed_1nn_selfjoin summary under
-# profiles/); None until measured.
-SELF_DRAM_BYTES_PER_LAUNCH = None
+# self-join: a one-launch ncu capture of the first 2^20 samples (190.7 MB
+# read + 572.8 MB written, profiles/join_mixed_1nn_coarse_selfjoin_2e20_m1024
+# .txt), scaled by the window count (x16), since the bytes are mostly the
+# 16-byte verification requests, whose number grows with the windows.
+SELF_DRAM_BYTES_PER_LAUNCH = (190.7e6 + 572.8e6) * 16
 
 
 def run_self_headline(args, world, rank, local):

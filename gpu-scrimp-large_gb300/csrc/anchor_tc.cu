@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) anchor_gemm_kernel(AnchorArgs A
       const int kend = static_cast<int>((A.m_pad - k0) < kKBlock ? (A.m_pad - k0) : kKBlock);
       for (int sb = 0; sb < kend && ok; sb += kSub) {
         // ---- MMAs of 64 terms (one thread) into fresh accumulators ----
-        if (t == 0) {
+        if (t == 0 && !A.wait_test) {
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           // A (Hankel): K step 16 B, M step 128 B; B (windows): K step 128 B,
           // N step (kKBlock / 8) * 128 B

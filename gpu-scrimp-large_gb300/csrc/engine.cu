@@ -406,8 +406,10 @@ SeriesDev to_dev(const SeriesBufs& s, int64_t n, int64_t ns) {
 // (nrows x wp_pad floats, the layout of anchor_tc.cu).
 int tc_anchor_chunk(Workspace& ws, const Problem& pr, int64_t K, int64_t s0, int64_t nrows,
                     int64_t wp_pad, float* table, int* error_flag, int desc_mode,
-                    cudaStream_t st, std::string* msg, AnchorArgs* out_args = nullptr) {
+                    cudaStream_t st, std::string* msg, AnchorArgs* out_args = nullptr,
+                    int wait_test = 0) {
   AnchorArgs A{};
+  A.wait_test = wait_test;
   A.R = pr.R;
   A.C = pr.C;
   A.m = pr.m;
@@ -450,7 +452,7 @@ int tc_anchor_chunk(Workspace& ws, const Problem& pr, int64_t K, int64_t s0, int
 // direct dots to kTcCheckTol is kept, else the tensor-core path stays off
 // (the band kernel's own anchors serve every join).  Uses the series-A
 // slots (the join computes its statistics afterwards) and synchronises.
-int tc_self_check(Workspace& ws, cudaStream_t st, std::string* msg) {
+int tc_self_check(Workspace& ws, cudaStream_t st, std::string* msg, bool wait_test = false) {
   constexpr int64_t n = 32768, m = 512, K = 1024;
   std::vector<double> x(n);
   uint64_t z = 0x9E3779B97F4A7C15ull;
@@ -489,6 +491,23 @@ int tc_self_check(Workspace& ws, cudaStream_t st, std::string* msg) {
   if ((rc = ensure(ws, S_TC_OUT, 64, &p, msg))) return rc;
   unsigned long long* out = static_cast<unsigned long long*>(p);
   int* flag = reinterpret_cast<int*>(out + 4);
+  if (wait_test) {
+    // the contraction with no MMA issued: its first bounded wait must give
+    // up, set the error word and return
+    CUDA_TRY(cudaMemsetAsync(out, 0, 64, st));
+    if ((rc = tc_anchor_chunk(ws, pr, K, 0, nrows, wp_pad, table, flag, ws.tc_desc_mode, st, msg,
+                              nullptr, 1)))
+      return rc;
+    int h = 0;
+    CUDA_TRY(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (h != 0) {
+      *msg = "Error: a wait on the tensor cores timed out on the device (wait-limit self-test)";
+      return SCAMP_ERR_DEVICE_TIMEOUT;
+    }
+    *msg = "Error: the wait-limit self-test finished without its wait running out";
+    return SCAMP_ERR_CUDA;
+  }
   ws.tc_state = 2;
   for (int mode = 0; mode < 2; ++mode) {
     CUDA_TRY(cudaMemsetAsync(out, 0, 64, st));
@@ -1198,6 +1217,18 @@ extern "C" int scamp_gb300_anchor_check(int device, double* max_err, int* availa
       if (max_err) *max_err = ws->tc_check_err;
       if (available) *available = ws->tc_state == 1 ? 1 : 0;
     }
+  }
+  if (rc) set_err(errbuf, errlen, msg);
+  return rc;
+}
+
+extern "C" int scamp_gb300_wait_limit_check(int device, char* errbuf, size_t errlen) {
+  std::string msg;
+  Workspace* ws;
+  int rc = init_workspace(device, &ws, &msg);
+  if (rc == SCAMP_OK) {
+    std::lock_guard<std::mutex> lock(ws->mu);
+    rc = tc_self_check(*ws, ws->stream, &msg, true);
   }
   if (rc) set_err(errbuf, errlen, msg);
   return rc;

@@ -280,6 +280,8 @@ struct AnchorArgs {
   float* table;            // [nrows][wp_pad]
   int* error_flag;         // set when a wait on the tensor cores gives up
   int desc_mode;           // shared-memory descriptor orientation (self-check)
+  int wait_test;           // 1: issue no MMA, so every bounded wait runs out
+                           // (the wait-limit self-test)
 };
 __global__ void anchor_split_kernel(AnchorArgs A);
 __global__ void anchor_gemm_kernel(AnchorArgs A);

@@ -43,6 +43,7 @@ EXPORTED_SYMBOLS = (
     "scamp_gb300_gpu_supported",
     "scamp_gb300_pipe_peak",
     "scamp_gb300_anchor_check",
+    "scamp_gb300_wait_limit_check",
     "scamp_gb300_version",
 )
 
@@ -158,6 +159,8 @@ def load():
     lib.scamp_gb300_anchor_check.argtypes = [ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_int),
                                              ctypes.c_char_p, ctypes.c_size_t]
     lib.scamp_gb300_anchor_check.restype = ctypes.c_int
+    lib.scamp_gb300_wait_limit_check.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
+    lib.scamp_gb300_wait_limit_check.restype = ctypes.c_int
     lib.scamp_gb300_version.argtypes = []
     lib.scamp_gb300_version.restype = ctypes.c_char_p
     _lib = lib

@@ -109,9 +109,10 @@ typedef struct scamp_c_result {
   double *corr_b;       /* optional */
   /* Filled by the engine. */
   double elapsed_ms;    /* device time of the join (stats .. final profile) */
-  double join_kernel_ms;/* device time of the join kernels (the band kernel,
-                         * then, in the mixed 1NN form, the verification of
-                         * deferred candidates) */
+  double join_kernel_ms;/* device time of the join kernels (the tensor-core
+                         * anchors where the mixed form uses them, the band
+                         * kernel, then, in the mixed forms, the
+                         * verification of deferred candidates) */
   uint64_t comparisons; /* distance-matrix cells evaluated */
   uint32_t gpu_launches;/* kernels launched by this call */
   uint32_t reserved0;
@@ -255,6 +256,15 @@ int scamp_gb300_pipe_peak(int device, int kind, double *ops_per_s);
  * the reference, whose seeds come from cuFFT (src/qt_helper.cpp:75-121). */
 int scamp_gb300_anchor_check(int device, double *max_err, int *available,
                              char *errbuf, size_t errlen);
+
+/* Self-test of the device wait limits on `device`: runs the tensor-core
+ * anchor kernel with no MMA issued, so that its bounded wait on the MMA
+ * completion barrier (about two seconds) runs out; the kernel sets the
+ * error word, waits once more (bounded), frees its tensor memory and
+ * returns.  Returns SCAMP_ERR_DEVICE_TIMEOUT when the limit worked (the
+ * context stays usable); any other code is a failure.  No counterpart in
+ * the reference. */
+int scamp_gb300_wait_limit_check(int device, char *errbuf, size_t errlen);
 
 /* Library version string. */
 const char *scamp_gb300_version(void);

@@ -74,3 +74,21 @@ def test_tc_anchors_sum_thresh(gpu_engine, oracle_mod, thr):
     got = gpu_engine.join(a, None, 512, "SUM_THRESH", "mixed", threshold=thr, anchor_mode=2,
                           anchor_interval=2048)
     check_sum("tc-sum", got["sum_a"], want["sum_a"], thr, 2e-5, TOL_MIXED)
+
+
+def test_device_wait_limit_returns_timeout(gpu_engine):
+    """The tensor-core kernel's bounded wait on its MMA barrier, made to run
+    out (no MMA issued): the host gets SCAMP_ERR_DEVICE_TIMEOUT and the
+    context stays usable for the next join."""
+    import ctypes
+
+    from scamp_gb300 import _lib
+
+    lib = _lib.load()
+    err = ctypes.create_string_buffer(512)
+    rc = lib.scamp_gb300_wait_limit_check(0, err, 512)
+    assert rc == 103, (rc, err.value)  # SCAMP_ERR_DEVICE_TIMEOUT
+    assert b"timed out" in err.value
+    a = _walk(9, 5000)
+    r = gpu_engine.join(a, None, 100, "1NN_INDEX", "mixed", return_corr=True)
+    assert r["comparisons"] > 0 and np.all(r["corr_a"] >= -1)
