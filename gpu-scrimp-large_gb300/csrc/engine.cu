@@ -1008,6 +1008,14 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
         CUDA_TRY(cudaMemcpyAsync(dprefix, cpre.data(), cpre.size() * 8, cudaMemcpyHostToDevice, st));
         CUDA_TRY(cudaMemsetAsync(P.unit_counter, 0, 8, st));
         launch_band(Q, std::min<int64_t>(resident, cunits));
+        if (u0 + U < urows) {
+          // the chunk's deferred verifications now, so that the request
+          // buffer only ever holds one chunk's requests (a long join's would
+          // overflow it); the last chunk's go to the verification below
+          verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
+          CUDA_TRY(cudaMemsetAsync(P.counters + 3, 0, 8, st));
+          ++launches;
+        }
       }
       CUDA_TRY(cudaGetLastError());
     } else if (kind == K_MIXED) {

@@ -122,7 +122,9 @@ typedef struct scamp_c_result {
   uint64_t steps;
   uint64_t slow_steps;
   uint64_t verifications;
-  double verify_kernel_ms; /* part of join_kernel_ms: deferred verification */
+  double verify_kernel_ms; /* part of join_kernel_ms: the last deferred
+                            * verification pass (joins anchored on the tensor
+                            * cores verify each chunk's requests after it) */
   /* 1NN (SCAMP_PROFILE_1NN): the best correlation per window as float32,
    * -2.0f = none (the reference's float profile, src/common.cpp:290-292);
    * in/out like profile_a / profile_b. */
