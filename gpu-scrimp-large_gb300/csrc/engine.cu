@@ -812,8 +812,11 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   // threshold is the sum threshold and every cell above it is accumulated).
   // The k-best and matrix-summary types run the FP64 visit kernel.
   enum { K_FP64, K_MIXED, K_VISIT } kind = visit ? K_VISIT : !mixed ? K_FP64 : K_MIXED;
+  // (SUM_THRESH keeps the per-cell filter unless asked: its fast path adds
+  // the blocks that lie wholly above the threshold, which needs per-cell r)
   const bool coarse = kind == K_MIXED && (a->filter_mode == 2 ||
-                                          (a->filter_mode == 0 && m >= kCoarseFilterMinWindow));
+                                          (a->filter_mode == 0 && is_1nn &&
+                                           m >= kCoarseFilterMinWindow));
   const void* kfn = kind == K_VISIT ? reinterpret_cast<const void*>(join_visit_kernel)
                   : kind == K_FP64 ? reinterpret_cast<const void*>(join_fp64_kernel)
                   : is_1nn ? (coarse ? reinterpret_cast<const void*>(join_mixed_1nn_coarse_kernel)

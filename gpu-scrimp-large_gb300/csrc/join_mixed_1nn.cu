@@ -108,6 +108,11 @@ __device__ __forceinline__ float max3(float a, float b, float c) {
   asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
   return d;
 }
+__device__ __forceinline__ float min3(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
 // PTX sqrt.approx.f32: an approximate square root (a few ulp); sqrt(0) = 0.
 __device__ __forceinline__ float sqrt_approx(float x) {
   float r;
@@ -481,6 +486,83 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
   return nreq;
 }
 
+// SUM_THRESH fast path of one thread-step whose cells all lie above the
+// threshold by more than the step's margin (fx, fy per segment): the block
+// is rewound from the covariances at the step's end (as the exact path
+// rewinds) and walked again; every valid cell adds its FP32 r to its row's
+// and its column's slab sums.  Rows are reduced over the warp (every lane
+// calls this, adding nothing where its flags are off), columns over
+// neighbouring threads: thread t's columns 8..14 are thread t + 1's 0..6.
+__device__ __noinline__ void fast_add_block(Smem& sm, const float2 (&cov_end)[kDiags], int s,
+                                            int t, int lane, bool fx, bool fy) {
+  const SlowCtx& cx = sm.cx;
+  const int r0 = s * kRows;
+  const int cb0 = 8 * (s + t);  // slab-relative column of (row 0, diagonal 0)
+  float2 c[kDiags];
+#pragma unroll
+  for (int k = 0; k < kDiags; ++k) c[k] = cov_end[k];
+#pragma unroll 1
+  for (int rr = kRows - 1; rr >= 0; --rr) {
+    const float4 rf = sm.r_fg[r0 + rr];
+#pragma unroll
+    for (int k = 0; k < kDiags; ++k) {
+      const float4 cf = col_fg(sm, padc(ringc(cx.ring0, cb0 + rr + k)));
+      c[k] = fma2(make_float2(-rf.x, -rf.y), make_float2(cf.z, cf.w), c[k]);
+      c[k] = fma2(make_float2(-cf.x, -cf.y), make_float2(rf.z, rf.w), c[k]);
+    }
+  }
+  float2 cacc[15];
+#pragma unroll
+  for (int x = 0; x < 15; ++x) cacc[x] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int rr = 0; rr < kRows; ++rr) {
+    const float4 rf = sm.r_fg[r0 + rr];
+    const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
+    const float2 ivr = sm.r_iv[r0 + rr];
+    float2 rs = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < kDiags; ++k) {
+      const int slot = padc(ringc(cx.ring0, cb0 + rr + k));
+      const float2 r2 = mul2(mul2(c[k], sm.u.s.c_iv[slot]), ivr);
+      const float vx = (fx && r2.x == r2.x) ? r2.x : 0.f;  // NaN cells add nothing
+      const float vy = (fy && r2.y == r2.y) ? r2.y : 0.f;
+      rs.x += vx;
+      rs.y += vy;
+      cacc[rr + k].x += vx;
+      cacc[rr + k].y += vy;
+      const float4 cf = col_fg(sm, slot);
+      c[k] = fma2(make_float2(cf.x, cf.y), dgr, c[k]);
+      c[k] = fma2(dfr, make_float2(cf.z, cf.w), c[k]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      rs.x += __shfl_xor_sync(0xffffffffu, rs.x, o);
+      rs.y += __shfl_xor_sync(0xffffffffu, rs.y, o);
+    }
+    if (lane == 0) {
+      if (rs.x != 0.f) atomicAdd(&sm.r_best[r0 + rr].x, rs.x);
+      if (rs.y != 0.f) atomicAdd(&sm.r_best[r0 + rr].y, rs.y);
+    }
+  }
+#pragma unroll
+  for (int x = 0; x < 7; ++x) {
+    const float ux = __shfl_up_sync(0xffffffffu, cacc[8 + x].x, 1);
+    const float uy = __shfl_up_sync(0xffffffffu, cacc[8 + x].y, 1);
+    if (lane > 0) {
+      cacc[x].x += ux;
+      cacc[x].y += uy;
+    }
+  }
+#pragma unroll
+  for (int x = 0; x < 15; ++x) {
+    if (x < 8 || lane == 31) {
+      const int rcx = ringc(cx.ring0, cb0 + x);
+      if (cacc[x].x != 0.f) atomicAdd(&sm.c_best[rcx].x, cacc[x].x);
+      if (cacc[x].y != 0.f) atomicAdd(&sm.c_best[rcx].y, cacc[x].y);
+    }
+  }
+}
+
 // The band kernel's body; kSum selects SUM_THRESH (separate instantiations,
 // so the 1NN_INDEX form carries none of the sum bookkeeping).  kCoarse
 // selects the fast path's filter:
@@ -502,6 +584,7 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
   const float thr = static_cast<float>(P.threshold);
   unsigned long long n_steps = 0, n_slow = 0, n_verify = 0;
   int qn = 0;  // queued blocks of this warp (warp-uniform)
+  float tfast = 0.f;  // SUM_THRESH: largest margin of a block added on the fast path
 
   for (;;) {
     if (t == 0) {
@@ -889,8 +972,9 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
         const float2 tt = fma2(make_float2(-kStepMarginC, -kStepMarginC), mg, tb);
         const float tx = tt.x, ty = tt.y;
 
-        // fast path: recurrence + block maximum
+        // fast path: recurrence + block maximum (SUM_THRESH: and minimum)
         float bx = -3.f, by = -3.f;
+        float lx = 3.f, ly = 3.f;
         if constexpr (kCoarse) {
           // largest covariance of the block (NaN diagonals ignored), then
           // the bound max(cov, 0) * max inv_c * max inv_r of every r in it
@@ -923,7 +1007,7 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
           bx = bnd.x;
           by = bnd.y;
         } else {
-          float2 rprev;
+          float2 rprev, lprev;
 #pragma unroll
           for (int rr = 0; rr < kRows; ++rr) {
             {
@@ -937,12 +1021,17 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
             // the row's largest cov * inv_c, times inv_r (> 0): the largest r
             // of the row, rounded exactly as (cov * inv_c) * inv_r per cell
             float mx = -3.f, my = -3.f;
+            float nx = 3.f, ny = 3.f;  // SUM_THRESH: the row's smallest as well
 #pragma unroll
             for (int k = 0; k < kDiags; k += 2) {
               const float2 pa = mul2(cov[k], ciw[(8 * P + rr + k) & 15]);
               const float2 pb = mul2(cov[k + 1], ciw[(8 * P + rr + k + 1) & 15]);
               mx = max3(mx, pa.x, pb.x);
               my = max3(my, pa.y, pb.y);
+              if constexpr (kSum) {
+                nx = min3(nx, pa.x, pb.x);
+                ny = min3(ny, pa.y, pb.y);
+              }
             }
             const float2 rm = mul2(make_float2(mx, my), ivr);
             if (rr & 1) {
@@ -950,6 +1039,15 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
               by = max3(by, rprev.y, rm.y);
             } else {
               rprev = rm;
+            }
+            if constexpr (kSum) {
+              const float2 rn = mul2(make_float2(nx, ny), ivr);
+              if (rr & 1) {
+                lx = min3(lx, lprev.x, rn.x);
+                ly = min3(ly, lprev.y, rn.y);
+              } else {
+                lprev = rn;
+              }
             }
 #pragma unroll
             for (int k = 0; k < kDiags; ++k) {
@@ -959,7 +1057,26 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
             }
           }
         }
-        const bool trig = bx > tx || by > ty;
+        bool trig = bx > tx || by > ty;
+        if constexpr (kSum && !kCoarse) {
+          // A segment whose every valid cell is above the threshold by more
+          // than the step's margin needs no exact path: each of its cells
+          // adds its FP32 r, as the exact path would add it (its per-cell
+          // margin is never larger).  The block is walked again from the
+          // step's start, the rows' sums reduced over the warp and the
+          // columns' sums over neighbouring threads (thread t's columns 8..14
+          // are thread t + 1's 0..6) before the shared-memory atomics.
+          const float2 ut = fma2(make_float2(kStepMarginC, kStepMarginC), mg, tb);
+          const bool ax = lx > ut.x && bx > tx, ay = ly > ut.y && by > ty;
+          trig = (bx > tx && !ax) || (by > ty && !ay);
+          const bool fx = ax && !trig, fy = ay && !trig;
+          if (__any_sync(0xffffffffu, fx || fy)) {
+            fast_add_block(sm, cov, s, t, lane, fx, fy);
+            const float2 smg = mul2(make_float2(kStepMarginC, kStepMarginC), mg);
+            if (fx) tfast = fmaxf(tfast, smg.x);
+            if (fy) tfast = fmaxf(tfast, smg.y);
+          }
+        }
         const unsigned tmask = __ballot_sync(0xffffffffu, trig);
         if (tmask) {
           // queue the triggered lanes in rank order while there is room
@@ -1053,6 +1170,12 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
     atomicAdd(P.counters + 0, n_steps);
     atomicAdd(P.counters + 1, n_slow);
     atomicAdd(P.counters + 2, n_verify);
+  }
+  if constexpr (kSum) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tfast = fmaxf(tfast, __shfl_xor_sync(0xffffffffu, tfast, o));
+    if (lane == 0 && P.counters && tfast > 0.f)
+      atomicMax(P.counters + 4, static_cast<unsigned long long>(__float_as_uint(tfast)));
   }
 }
 
