@@ -21,10 +21,23 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "engine.cuh"
 #include "scamp_gb300.h"
 
 namespace scamp_gb300 {
+
+// NVTX range over a phase of a join's host-side enqueueing (header-only
+// NVTX3: free unless a profiler is attached), so that a timeline shows the
+// statistics, seeding, anchors and band kernel, verification, re-evaluation
+// and the copies of every join.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 int fp64_band_width();
 int fp64_slab_rows();
@@ -666,6 +679,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   }
 
   // ---- seeds: block-averaged pre-pass (mixed 1NN joins that pay for it) ----
+  NvtxRange nvtx_join(nested ? "seeding pre-pass join" : "join");
   uint64_t *seed_a = nullptr, *seed_b = nullptr;
   int64_t seed_ns_a = 0, seed_ns_b = 0;
   if (!nested && mixed && is_1nn && seedable(a, plan)) {
@@ -675,6 +689,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   }
 
   // ---- statistics ----
+  nvtxRangePushA("statistics");
   SeriesBufs sa{}, sb{};
   sa.bshift = sb.bshift = block_shift(m);
   if ((rc = alloc_series(ws, 0, na, plan.ns_a, &sa, msg))) return rc;
@@ -719,6 +734,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     ++launches;
   }
   CUDA_TRY(cudaGetLastError());
+  nvtxRangePop();
   SeriesDev devA = to_dev(sa, na, plan.ns_a);
   SeriesDev devB = to_dev(sb, nb, plan.ns_b);
   SeriesDev devArows = devA;  // series A in the row role
@@ -921,6 +937,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   }
 
   if (P.total_units > 0) {
+    NvtxRange nvtx_band("anchors, band kernel, verification");
     void* p;
     if ((rc = ensure(ws, S_PREFIX, prefix.size() * 8, &p, msg))) return rc;
     int64_t* dprefix = static_cast<int64_t*>(p);
@@ -1055,6 +1072,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
 
   // ---- FP64 re-evaluation of every reported cell (1NN types) ----
   if (is_1nn) {
+    NvtxRange nvtx_eval("FP64 re-evaluation");
     EvalPair E{};
     E.m = m;
     E.kl = kl;
@@ -1306,6 +1324,7 @@ extern "C" int scamp_gb300_join(const scamp_c_args* args, scamp_c_result* res,
       return fail(SCAMP_ERR_CUDA);                                            \
     }                                                                         \
   } while (0)
+  NvtxRange nvtx_call("scamp_gb300_join");
   void *pa, *pb = nullptr;
   if ((rc = ensure(*ws, S_RAW_A, na * 8, &pa, &msg))) return fail(rc);
   HOST_CUDA(cudaMemcpyAsync(pa, args->timeseries_a, na * 8, cudaMemcpyHostToDevice, st));
