@@ -1263,6 +1263,56 @@ extern "C" int scamp_gb300_wait_limit_check(int device, char* errbuf, size_t err
   return rc;
 }
 
+namespace scamp_gb300 {
+// The statistics kernel of the joins on one host series, results copied back.
+int window_stats(Workspace& ws, const double* series, int64_t n, int64_t m, int ultra,
+                 double* mean, double* invnorm, double* df, double* dg, std::string* msg) {
+  cudaStream_t st = ws.stream;
+  const int64_t ns = n - m + 1;
+  void* p;
+  int rc;
+  if ((rc = ensure(ws, S_RAW_A, n * 8, &p, msg))) return rc;
+  double* raw = static_cast<double*>(p);
+  CUDA_TRY(cudaMemcpyAsync(raw, series, n * 8, cudaMemcpyHostToDevice, st));
+  SeriesBufs sb{};
+  sb.bshift = block_shift(m);
+  if ((rc = alloc_series(ws, 0, n, ns, &sb, msg))) return rc;
+  const int chunk = 64;
+  const int64_t threads = (ns + chunk - 1) / chunk;
+  stats_kernel<<<static_cast<unsigned>((threads + 127) / 128), 128, 0, st>>>(
+      raw, n, m, ultra, chunk, sb.bshift, sb.T, sb.T32, sb.bhi, sb.blo, sb.mu_rel, sb.mean,
+      sb.inv, sb.df, sb.dg, sb.inv32, sb.df32, sb.dg32);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(mean, sb.mean, ns * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(invnorm, sb.inv, ns * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(df, sb.df, ns * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(dg, sb.dg, ns * 8, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return SCAMP_OK;
+}
+}  // namespace scamp_gb300
+
+extern "C" int scamp_gb300_window_stats(int device, const double* series, int64_t n,
+                                        int64_t window, int high_precision_norms,
+                                        double* mean, double* invnorm, double* df, double* dg,
+                                        char* errbuf, size_t errlen) {
+  std::string msg;
+  if (!series || !mean || !invnorm || !df || !dg || window < 3 || n < window) {
+    set_err(errbuf, errlen, "Error: window statistics need a series of at least `window` >= 3 "
+                            "samples and four output arrays");
+    return SCAMP_ERR_INVALID_ARGS;
+  }
+  Workspace* ws;
+  int rc = init_workspace(device, &ws, &msg);
+  if (rc == SCAMP_OK) {
+    std::lock_guard<std::mutex> lock(ws->mu);
+    rc = window_stats(*ws, series, n, window, high_precision_norms ? 1 : 0, mean, invnorm, df,
+                      dg, &msg);
+  }
+  if (rc) set_err(errbuf, errlen, msg);
+  return rc;
+}
+
 extern "C" int scamp_gb300_pipe_peak(int device, int kind, double* ops_per_s) {
   if (!ops_per_s || (kind != 0 && kind != 1)) return SCAMP_ERR_INVALID_ARGS;
   return measure_pipe_peak(device, kind, ops_per_s) ? SCAMP_ERR_CUDA : SCAMP_OK;

@@ -167,9 +167,11 @@ __device__ __forceinline__ void stats_body(int64_t tid, const double* __restrict
       ss = s2;
       sc = c2;
     } else {
+      // With the means' low parts, so that a large offset's rounded mean
+      // does not leave a per-step residue (b - a)(delta_w + delta_w+1).
       const double a = clean(T_raw[w]);
       const double b = clean(T_raw[w + m]);
-      acc2(ss, sc, ((a - mu) + (b - mu_next)) * (b - a));
+      acc2(ss, sc, (((a - mu) - mu_lo) + ((b - mu_next) - mu_next_lo)) * (b - a));
     }
     ps = ps_n;
     pc = pc_n;

@@ -126,6 +126,25 @@ def anchor_check(device=0):
     return err.value, bool(avail.value)
 
 
+def window_stats(series, m, high_precision_norms=False, device=0):
+    """Window statistics as the joins compute them on the device (C ABI
+    scamp_gb300_window_stats; the reference's compute_statistics_cpu,
+    src/cpu_stats.cpp:123-160): (mean, invnorm, df, dg), FP64 arrays of
+    len(series) - m + 1 windows."""
+    x = np.ascontiguousarray(series, dtype=np.float64)
+    ns = len(x) - int(m) + 1
+    if int(m) < 3 or ns < 1:
+        raise ValueError("window statistics need a window >= 3 and a series at least that long")
+    out = [np.empty(ns, dtype=np.float64) for _ in range(4)]
+    buf = ctypes.create_string_buffer(1024)
+    ptr = lambda a: a.ctypes.data_as(_lib._dp)
+    rc = _lib.load().scamp_gb300_window_stats(int(device), ptr(x), len(x), int(m),
+                                              1 if high_precision_norms else 0,
+                                              *[ptr(o) for o in out], buf, 1024)
+    _check(rc, buf)
+    return tuple(out)
+
+
 def _check(rc, err):
     if rc != _lib.SCAMP_OK:
         msg = err.value.decode(errors="replace") or _lib.ERROR_NAMES.get(rc, str(rc))

@@ -44,6 +44,7 @@ EXPORTED_SYMBOLS = (
     "scamp_gb300_pipe_peak",
     "scamp_gb300_anchor_check",
     "scamp_gb300_wait_limit_check",
+    "scamp_gb300_window_stats",
     "scamp_gb300_version",
 )
 
@@ -161,6 +162,10 @@ def load():
     lib.scamp_gb300_anchor_check.restype = ctypes.c_int
     lib.scamp_gb300_wait_limit_check.argtypes = [ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
     lib.scamp_gb300_wait_limit_check.restype = ctypes.c_int
+    lib.scamp_gb300_window_stats.argtypes = [ctypes.c_int, _dp, ctypes.c_int64, ctypes.c_int64,
+                                             ctypes.c_int, _dp, _dp, _dp, _dp,
+                                             ctypes.c_char_p, ctypes.c_size_t]
+    lib.scamp_gb300_window_stats.restype = ctypes.c_int
     lib.scamp_gb300_version.argtypes = []
     lib.scamp_gb300_version.restype = ctypes.c_char_p
     _lib = lib

@@ -248,6 +248,19 @@ int scamp_gb300_gpu_supported(void);
  * Has no counterpart in the reference. */
 int scamp_gb300_pipe_peak(int device, int kind, double *ops_per_s);
 
+/* Window statistics of one series, as every join computes them on the
+ * device (compensated FP64): for each of the n - window + 1 windows its mean,
+ * inverse norm 1/sqrt(sum of squared differences from the mean), NaN when
+ * the window holds a non-finite sample or is flat, and the update terms
+ * df[i] = (T[i+m] - T[i]) / 2, dg[i] = (T[i+m] - mean[i+1]) + (T[i] - mean[i])
+ * (0 at the last window), non-finite samples counted as 0.
+ * high_precision_norms = 1 sums every window directly (ULTRA).  Replaces
+ * compute_statistics_cpu (src/cpu_stats.cpp:123-160); host arrays. */
+int scamp_gb300_window_stats(int device, const double *series, int64_t n,
+                             int64_t window, int high_precision_norms,
+                             double *mean, double *invnorm, double *df, double *dg,
+                             char *errbuf, size_t errlen);
+
 /* Self-check of the mixed form's tensor-core anchors on `device` (the
  * check every process runs once before its first mixed join of long
  * windows): anchors of a seeded random walk (32768 samples, m = 512) from the
