@@ -313,8 +313,16 @@ def run_batch_workload(args, world, rank, local):
 
     torch.cuda.set_device(local)
     batch = workloads.cfg4_batch()
+    if args.batch_series:
+        batch = batch[: args.batch_series]  # a smaller batch, for profiling captures
     series = [x for x, _ in batch]
     windows = [m for _, m in batch]
+    if args.profile_only:
+        # the batched calls alone, at the tile-height rule (ncu captures)
+        for _ in range(args.warmup + args.steps):
+            scamp_gb300.join_batch(series, windows, "mixed", device=local)
+        torch.cuda.synchronize(local)
+        return
     # tile height per window, tuned once (kept for every later call)
     t0 = time.perf_counter()
     seg = scamp_gb300.tune_batch(series, windows, "mixed", device=local)
@@ -553,6 +561,8 @@ def main():
                    help="--workload gaps: profile types to run, comma-separated")
     p.add_argument("--na-log2", type=int, default=None,
                    help="log2 length of A (B is half); smaller only for profiling captures")
+    p.add_argument("--batch-series", type=int, default=0,
+                   help="--workload batch: only the first N series (profiling captures)")
     p.add_argument("--profile-form", default="mixed", choices=["mixed", "double"],
                    help="form run by --profile-only")
     p.add_argument("--anchor-study", action="store_true",

@@ -93,6 +93,10 @@ constexpr int64_t kTcMinWindow = 512;
 // Budget of one chunk's anchor table (bytes); a chunk covers at least 16
 // unit rows (32 anchor rows, one tile of the contraction).
 constexpr double kTcTableBudget = 4.0 * (1 << 30);
+// Unit rows of a chunk of the anchor table: at least this many (a chunk's
+// anchor rows fill whole 16-row tiles), down to half of it when a chunk's
+// verification requests approach the buffer's capacity.
+constexpr int64_t kTcMinChunkRows = 16;
 // Largest |anchor - FP64| inv_r inv_c the self-check accepts.
 constexpr double kTcCheckTol = 1e-5;
 
@@ -319,7 +323,7 @@ struct Workspace {
 };
 
 constexpr int64_t kMinVerifyReqs = int64_t{1} << 22;
-constexpr int64_t kMaxVerifyReqs = int64_t{1} << 28;  // 4 GiB of requests
+constexpr int64_t kMaxVerifyReqs = int64_t{1} << 30;  // 16 GiB of requests
 
 Workspace g_ws[64];
 
@@ -554,6 +558,9 @@ int tc_self_check(Workspace& ws, cudaStream_t st, std::string* msg, bool wait_te
 // Seeding pre-pass of the mixed 1NN join: when and how.  The block-averaged
 // join costs ~1/64 of the join's cells; below a few 1e9 cells it does not pay.
 constexpr float kSeedFloor = 0.8f;  // partners below it are not worth a seed
+// Smallest averaged window of a batch's pre-pass (shorter ones pair blocks
+// at random).
+constexpr int64_t kBatchSeedMinWindow = 8;
 constexpr int64_t kSeedMinWindow = 64;
 
 // Block size of the pre-pass: the largest power of two <= m / 16 within
@@ -990,19 +997,19 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
         urows = std::max<int64_t>(urows, (rows0 + 2 * K - 1) / (2 * K));
       }
       int64_t U = static_cast<int64_t>(kTcTableBudget / (8.0 * static_cast<double>(wsum)));
-      U = std::max<int64_t>(16, U / 16 * 16);
+      U = std::max<int64_t>(kTcMinChunkRows, U / kTcMinChunkRows * kTcMinChunkRows);
       void* tp;
       if ((rc = ensure(ws, S_TC_TAB, static_cast<size_t>(2 * U * wsum) * 4, &tp, msg))) return rc;
       float* tab = static_cast<float*>(tp);
       std::vector<int64_t> cpre;
-      for (int64_t u0 = 0; u0 < urows; u0 += U) {
+      for (int64_t u0 = 0, Uc = U; u0 < urows; u0 += Uc, Uc = U) {
         cpre.assign(1, 0);
         for (int p = 0; p < P.nprob; ++p) {
           const Problem& pr = P.prob[p];
           for (int64_t b = 0; b < pr.nbands; ++b) {
             const int64_t rows = band_rows(pr.R.ns, pr.C.ns, pr.d_lo + b * W);
             const int64_t ub = (rows + 2 * K - 1) / (2 * K);
-            cpre.push_back(cpre.back() + std::max<int64_t>(0, std::min<int64_t>(ub - u0, U)));
+            cpre.push_back(cpre.back() + std::max<int64_t>(0, std::min<int64_t>(ub - u0, Uc)));
           }
         }
         const int64_t cunits = cpre.back();
@@ -1014,7 +1021,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
         for (int p = 0; p < P.nprob; ++p) {
           const int64_t s0 = 2 * u0;
           const int64_t srows = std::max<int64_t>(
-              0, std::min<int64_t>(2 * U, (band_rows(P.prob[p].R.ns, P.prob[p].C.ns, P.prob[p].d_lo) +
+              0, std::min<int64_t>(2 * Uc, (band_rows(P.prob[p].R.ns, P.prob[p].C.ns, P.prob[p].d_lo) +
                                            K - 1) / K - s0));
           Q.prob[p].anchor_tab = tp_p;
           Q.prob[p].tab_wp = wp[p];
@@ -1023,18 +1030,28 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
                                                  P.error_flag, ws.tc_desc_mode, st, msg)))
             return rc;
           launches += srows > 0 ? 2 : 0;
-          tp_p += 2 * U * wp[p];
+          tp_p += 2 * Uc * wp[p];
         }
         CUDA_TRY(cudaMemcpyAsync(dprefix, cpre.data(), cpre.size() * 8, cudaMemcpyHostToDevice, st));
         CUDA_TRY(cudaMemsetAsync(P.unit_counter, 0, 8, st));
         launch_band(Q, std::min<int64_t>(resident, cunits));
-        if (u0 + U < urows) {
+        if (u0 + Uc < urows) {
           // the chunk's deferred verifications now, so that the request
           // buffer only ever holds one chunk's requests (a long join's would
           // overflow it); the last chunk's go to the verification below
           verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
-          CUDA_TRY(cudaMemsetAsync(P.counters + 3, 0, 8, st));
           ++launches;
+          // a chunk that filled more than half of the buffer: later chunks
+          // take fewer unit rows (their tables fit the one allocated)
+          unsigned long long nreq = 0;
+          CUDA_TRY(cudaMemcpyAsync(&nreq, P.counters + 3, 8, cudaMemcpyDeviceToHost, st));
+          CUDA_TRY(cudaStreamSynchronize(st));
+          ws.vreq_seen = std::max<int64_t>(ws.vreq_seen, static_cast<int64_t>(nreq));
+          while (2 * static_cast<int64_t>(nreq) > P.vreq_cap && U > kTcMinChunkRows / 2) {
+            U /= 2;
+            nreq /= 2;
+          }
+          CUDA_TRY(cudaMemsetAsync(P.counters + 3, 0, 8, st));
         }
       }
       CUDA_TRY(cudaGetLastError());
@@ -1838,7 +1855,80 @@ struct BatchSeries {
   int bshift;
   int64_t off_n, off_ns, off_blk;
   uint64_t cells;
+  // block-averaged pre-pass (f = 0: not seeded): f samples per block, the
+  // averaged series' length, window, windows, exclusion, segment length
+  int f;
+  int64_t n2, m2, ns2, excl2, K2;
+  int bshift2;
+  int64_t off_n2, off_ns2, off_blk2;
 };
+
+// Device arrays of a batch's concatenated series.
+struct BatchArrays {
+  double *raw, *T, *mean, *inv, *df, *dg;
+  float *inv32, *df32, *dg32, *T32, *bhi, *blo, *murel;
+  uint64_t* keys;
+};
+
+// One series' view of the concatenated arrays.
+SeriesDev batch_series_dev(const BatchArrays& A, int64_t off_n, int64_t off_ns, int64_t off_blk,
+                           int bshift, int64_t n, int64_t ns) {
+  SeriesDev sd;
+  sd.T = A.T + off_n; sd.mean = A.mean + off_ns; sd.inv = A.inv + off_ns;
+  sd.df = A.df + off_ns; sd.dg = A.dg + off_ns;
+  sd.inv32 = A.inv32 + off_ns; sd.df32 = A.df32 + off_ns; sd.dg32 = A.dg32 + off_ns;
+  sd.T32 = A.T32 + off_n; sd.bhi = A.bhi + off_blk; sd.blo = A.blo + off_blk;
+  sd.mu_rel = A.murel + off_ns; sd.bshift = bshift; sd.n = n; sd.ns = ns;
+  return sd;
+}
+
+StatsJob batch_stats_job(const BatchArrays& A, int64_t off_n, int64_t off_ns, int64_t off_blk,
+                         int bshift, int64_t n, int64_t m) {
+  StatsJob j;
+  j.T_raw = A.raw + off_n;
+  j.n = n;
+  j.m = m;
+  j.bshift = bshift;
+  j.T_clean = A.T + off_n;
+  j.mean = A.mean + off_ns;
+  j.inv = A.inv + off_ns;
+  j.df = A.df + off_ns;
+  j.dg = A.dg + off_ns;
+  j.T32 = A.T32 + off_n;
+  j.bhi = A.bhi + off_blk;
+  j.blo = A.blo + off_blk;
+  j.mu_rel = A.murel + off_ns;
+  j.inv32 = A.inv32 + off_ns;
+  j.df32 = A.df32 + off_ns;
+  j.dg32 = A.dg32 + off_ns;
+  return j;
+}
+
+// Band problem of one series of a batch (a self-join into its keys) and its
+// band unit prefix entries.
+Problem batch_problem(const SeriesDev& sd, uint64_t* keys, int64_t excl, int64_t m, int64_t K,
+                      int64_t band_begin, int W, std::vector<int64_t>* bpre) {
+  Problem pr{};
+  pr.R = sd;
+  pr.C = sd;
+  pr.d_lo = excl;
+  pr.d_hi = sd.ns;
+  pr.x_lo = pr.x_hi = 0;
+  pr.key_col = pr.key_row = keys;  // self-join: rows and columns into one profile
+  pr.band_begin = band_begin;
+  pr.nbands = (pr.d_hi - pr.d_lo + W - 1) / W;
+  pr.m = m;
+  pr.seg_len = K;
+  const double blk = static_cast<double>(1 << sd.bshift);
+  const double e = std::sqrt(std::min<double>(m, blk)) + std::sqrt(std::ceil(m / blk) + 1.0);
+  pr.anchor_vcoef = static_cast<float>(e * e / 8.0);
+  for (int64_t g = 0; g < pr.nbands; ++g) {
+    const int64_t D0 = pr.d_lo + g * W;
+    const int64_t rows = band_rows(sd.ns, sd.ns, D0);
+    bpre->push_back(bpre->back() + (rows + 2 * K - 1) / (2 * K));
+  }
+  return pr;
+}
 
 // Segment length of one series of a batch: `pref` (the autotuned value for
 // its window, 0 = none) or the cold-start anchor interval, reduced for short
@@ -1869,6 +1959,8 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   ws.tracked_tie_margin = ws.tracked_sum_margin = false;
   std::vector<BatchSeries> ser(count);
   int64_t Nn = 0, Nns = 0, Nblk = 0, ns_max = 1;
+  int64_t N2n = 0, N2ns = 0, N2blk = 0;  // the pre-pass's series
+  int nseed = 0;
   bool want_corr = false;
   for (int k = 0; k < count; ++k) {
     const scamp_c_args* a = &args[k];
@@ -1892,6 +1984,29 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     Nns += b.ns;
     Nblk += (b.n >> b.bshift) + 1;
     ns_max = std::max(ns_max, b.ns);
+    // the pre-pass: series averaged over blocks of f samples, window m / f
+    b.f = 0;
+    if (b.cells > 0) {
+      const int f = seed_factor(b.m);
+      const int64_t n2 = b.n / f, m2 = b.m / f;
+      const int64_t ns2 = n2 - m2 + 1, excl2 = m2 / 4;
+      if (m2 >= kBatchSeedMinWindow && ns2 > excl2 && diag_cells(ns2, ns2, excl2, ns2) > 0) {
+        b.f = f;
+        b.n2 = n2;
+        b.m2 = m2;
+        b.ns2 = ns2;
+        b.excl2 = excl2;
+        b.bshift2 = block_shift(m2);
+        b.K2 = batch_segment(m2, ns2, mixed_1nn_slab_rows(), 0);
+        b.off_n2 = N2n;
+        b.off_ns2 = N2ns;
+        b.off_blk2 = N2blk;
+        N2n += n2;
+        N2ns += ns2;
+        N2blk += (n2 >> b.bshift2) + 1;
+        ++nseed;
+      }
+    }
     want_corr = want_corr || res[k].corr_a != nullptr;
   }
   // ---- arena ----
@@ -1906,9 +2021,22 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
                b_counter = sz(64), b_wpre = sz(8 * (count + 1)),
                b_eval = sz(sizeof(EvalSide) * count);
   // band prefix: sized after the problems are known
-  int64_t bands_max = 0;
-  for (const auto& b : ser) bands_max += (b.ns + mixed_1nn_band_width() - 1) / mixed_1nn_band_width();
+  int64_t bands_max = 0, bands2_max = 0;
+  for (const auto& b : ser) {
+    bands_max += (b.ns + mixed_1nn_band_width() - 1) / mixed_1nn_band_width();
+    if (b.f) bands2_max += (b.ns2 + mixed_1nn_band_width() - 1) / mixed_1nn_band_width();
+  }
   const size_t b_bpre = sz(8 * (bands_max + 1));
+  // the pre-pass's arrays
+  const size_t s_raw = sz(8 * N2n), s_T = sz(8 * N2n), s_mean = sz(8 * N2ns), s_inv = sz(8 * N2ns),
+               s_df = sz(8 * N2ns), s_dg = sz(8 * N2ns), s_inv32 = sz(4 * N2ns),
+               s_df32 = sz(4 * N2ns), s_dg32 = sz(4 * N2ns), s_T32 = sz(4 * N2n),
+               s_bhi = sz(4 * N2blk), s_blo = sz(4 * N2blk), s_murel = sz(4 * N2ns),
+               s_keys = sz(8 * N2ns), s_jobs = sz(sizeof(StatsJob) * nseed),
+               s_jpre = sz(8 * (nseed + 1)), s_probs = sz(sizeof(Problem) * nseed),
+               s_counter = sz(64), s_wpre = sz(8 * (nseed + 1)), s_bpre = sz(8 * (bands2_max + 1)),
+               s_paa = sz(sizeof(PaaJob) * nseed), s_paapre = sz(8 * (nseed + 1)),
+               s_seed = sz(sizeof(BatchSeedJob) * nseed);
   void* arena;
   if ((rc = ensure(ws, S_BATCH, total, &arena, msg))) return rc;
   unsigned char* cur = static_cast<unsigned char*>(arena);
@@ -1936,6 +2064,32 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   int64_t* d_bpre = reinterpret_cast<int64_t*>(take(b_bpre));
   int64_t* d_wpre = reinterpret_cast<int64_t*>(take(b_wpre));
   EvalSide* d_eval = reinterpret_cast<EvalSide*>(take(b_eval));
+  BatchArrays A2;
+  A2.raw = reinterpret_cast<double*>(take(s_raw));
+  A2.T = reinterpret_cast<double*>(take(s_T));
+  A2.mean = reinterpret_cast<double*>(take(s_mean));
+  A2.inv = reinterpret_cast<double*>(take(s_inv));
+  A2.df = reinterpret_cast<double*>(take(s_df));
+  A2.dg = reinterpret_cast<double*>(take(s_dg));
+  A2.inv32 = reinterpret_cast<float*>(take(s_inv32));
+  A2.df32 = reinterpret_cast<float*>(take(s_df32));
+  A2.dg32 = reinterpret_cast<float*>(take(s_dg32));
+  A2.T32 = reinterpret_cast<float*>(take(s_T32));
+  A2.bhi = reinterpret_cast<float*>(take(s_bhi));
+  A2.blo = reinterpret_cast<float*>(take(s_blo));
+  A2.murel = reinterpret_cast<float*>(take(s_murel));
+  A2.keys = reinterpret_cast<uint64_t*>(take(s_keys));
+  StatsJob* d_jobs2 = reinterpret_cast<StatsJob*>(take(s_jobs));
+  int64_t* d_jpre2 = reinterpret_cast<int64_t*>(take(s_jpre));
+  Problem* d_probs2 = reinterpret_cast<Problem*>(take(s_probs));
+  unsigned long long* d_counter2 = reinterpret_cast<unsigned long long*>(take(s_counter));
+  int64_t* d_wpre2 = reinterpret_cast<int64_t*>(take(s_wpre));
+  int64_t* d_bpre2 = reinterpret_cast<int64_t*>(take(s_bpre));
+  PaaJob* d_paa = reinterpret_cast<PaaJob*>(take(s_paa));
+  int64_t* d_paapre = reinterpret_cast<int64_t*>(take(s_paapre));
+  BatchSeedJob* d_seed = reinterpret_cast<BatchSeedJob*>(take(s_seed));
+  BatchArrays A1{d_raw, d_T, d_mean, d_inv, d_df, d_dg, d_inv32, d_df32, d_dg32, d_T32,
+                 d_bhi, d_blo, d_murel, d_keys};
 
   // ---- host side: inputs gathered, every launch's arguments built ----
   std::vector<double> h_raw(static_cast<size_t>(Nn));
@@ -1949,23 +2103,7 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   std::vector<int64_t> jpre(count + 1, 0);
   for (int k = 0; k < count; ++k) {
     const BatchSeries& b = ser[k];
-    StatsJob& j = jobs[k];
-    j.T_raw = d_raw + b.off_n;
-    j.n = b.n;
-    j.m = b.m;
-    j.bshift = b.bshift;
-    j.T_clean = d_T + b.off_n;
-    j.mean = d_mean + b.off_ns;
-    j.inv = d_inv + b.off_ns;
-    j.df = d_df + b.off_ns;
-    j.dg = d_dg + b.off_ns;
-    j.T32 = d_T32 + b.off_n;
-    j.bhi = d_bhi + b.off_blk;
-    j.blo = d_blo + b.off_blk;
-    j.mu_rel = d_murel + b.off_ns;
-    j.inv32 = d_inv32 + b.off_ns;
-    j.df32 = d_df32 + b.off_ns;
-    j.dg32 = d_dg32 + b.off_ns;
+    jobs[k] = batch_stats_job(A1, b.off_n, b.off_ns, b.off_blk, b.bshift, b.n, b.m);
     const int64_t threads = (b.ns + chunk - 1) / chunk;
     jpre[k + 1] = jpre[k] + (threads + 127) / 128;
   }
@@ -1979,35 +2117,42 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   for (int k = 0; k < count; ++k) {
     const BatchSeries& b = ser[k];
     if (b.cells == 0) continue;
-    SeriesDev sd;
-    sd.T = d_T + b.off_n; sd.mean = d_mean + b.off_ns; sd.inv = d_inv + b.off_ns;
-    sd.df = d_df + b.off_ns; sd.dg = d_dg + b.off_ns;
-    sd.inv32 = d_inv32 + b.off_ns; sd.df32 = d_df32 + b.off_ns; sd.dg32 = d_dg32 + b.off_ns;
-    sd.T32 = d_T32 + b.off_n; sd.bhi = d_bhi + b.off_blk; sd.blo = d_blo + b.off_blk;
-    sd.mu_rel = d_murel + b.off_ns; sd.bshift = b.bshift; sd.n = b.n; sd.ns = b.ns;
-    Problem pr{};
-    pr.R = sd;
-    pr.C = sd;
-    pr.d_lo = b.excl;
-    pr.d_hi = b.ns;
-    pr.x_lo = pr.x_hi = 0;
-    pr.key_col = pr.key_row = d_keys + b.off_ns;  // self-join: rows and columns into profile A
-    pr.band_begin = band_total;
-    pr.nbands = (pr.d_hi - pr.d_lo + W - 1) / W;
-    pr.m = b.m;
-    pr.seg_len = b.K;
-    {
-      const double blk = static_cast<double>(1 << b.bshift);
-      const double e = std::sqrt(std::min<double>(b.m, blk)) + std::sqrt(std::ceil(b.m / blk) + 1.0);
-      pr.anchor_vcoef = static_cast<float>(e * e / 8.0);
-    }
-    for (int64_t g = 0; g < pr.nbands; ++g) {
-      const int64_t D0 = pr.d_lo + g * W;
-      const int64_t rows = band_rows(b.ns, b.ns, D0);
-      bpre.push_back(bpre.back() + (rows + 2 * b.K - 1) / (2 * b.K));
-    }
+    const SeriesDev sd = batch_series_dev(A1, b.off_n, b.off_ns, b.off_blk, b.bshift, b.n, b.ns);
+    const Problem pr = batch_problem(sd, d_keys + b.off_ns, b.excl, b.m, b.K, band_total, W, &bpre);
     band_total += pr.nbands;
     probs.push_back(pr);
+  }
+  // the pre-pass: averaged copies, their statistics jobs, band problems, and
+  // the seeding jobs that carry its partners back to the series' keys
+  std::vector<PaaJob> paa_jobs;
+  std::vector<StatsJob> jobs2;
+  std::vector<Problem> probs2;
+  std::vector<BatchSeedJob> seed_jobs;
+  // wpre2: the averaged windows' prefix (diagonal seeds and seeding jobs)
+  std::vector<int64_t> paapre(1, 0), jpre2(1, 0), wpre2(1, 0), bpre2(1, 0);
+  int64_t band_total2 = 0;
+  for (int k = 0; k < count; ++k) {
+    const BatchSeries& b = ser[k];
+    if (!b.f) continue;
+    paa_jobs.push_back(PaaJob{d_raw + b.off_n, A2.raw + b.off_n2, b.n2, b.f});
+    paapre.push_back(paapre.back() + b.n2);
+    jobs2.push_back(batch_stats_job(A2, b.off_n2, b.off_ns2, b.off_blk2, b.bshift2, b.n2, b.m2));
+    jpre2.push_back(jpre2.back() + ((b.ns2 + chunk - 1) / chunk + 127) / 128);
+    const SeriesDev sd2 = batch_series_dev(A2, b.off_n2, b.off_ns2, b.off_blk2, b.bshift2, b.n2, b.ns2);
+    const Problem pr2 = batch_problem(sd2, A2.keys + b.off_ns2, b.excl2, b.m2, b.K2, band_total2, W,
+                                      &bpre2);
+    band_total2 += pr2.nbands;
+    probs2.push_back(pr2);
+    wpre2.push_back(wpre2.back() + b.ns2);
+    BatchSeedJob sj;
+    sj.X = batch_series_dev(A1, b.off_n, b.off_ns, b.off_blk, b.bshift, b.n, b.ns);
+    sj.key = d_keys + b.off_ns;
+    sj.paa_key = A2.keys + b.off_ns2;
+    sj.ns_paa = b.ns2;
+    sj.excl = b.excl;
+    sj.m = b.m;
+    sj.f = b.f;
+    seed_jobs.push_back(sj);
   }
   // seeds from each series' nearest allowed diagonal (diag_seed_kernel),
   // and the FP64 re-evaluation of every reported cell (final_eval_batch_kernel)
@@ -2057,9 +2202,52 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, mixed_1nn_threads(), smem));
     grid = std::min<int64_t>(static_cast<int64_t>(ws.sms) * std::max(occ, 1), P.total_units);
   }
+  // the pre-pass join: the same kernel over the averaged series, into their
+  // own keys (started at the seed floor); its unverified candidates keep
+  // their lower bounds, which is all a seed needs (the partner), so it has
+  // no verification launch.  It shares the request buffer: the main join's
+  // requests are counted from 0 after it.
+  JoinParams P2{};
+  int64_t grid2 = 0;
+  const int64_t nseed_jobs = static_cast<int64_t>(seed_jobs.size());
+  if (nseed_jobs > 0 && !probs.empty()) {
+    P2 = P;
+    P2.batch = d_probs2;
+    P2.nbatch = static_cast<int64_t>(probs2.size());
+    P2.band_unit_prefix = d_bpre2;
+    P2.total_bands = band_total2;
+    P2.total_units = bpre2.back();
+    P2.unit_counter = d_counter2;
+    P2.counters = d_counter2 + 1;
+    P2.error_flag = reinterpret_cast<int*>(d_counter2 + 6);
+    grid2 = std::min<int64_t>(grid > 0 ? grid : 1, std::max<int64_t>(P2.total_units, 1));
+  }
+  const bool seeded = grid2 > 0 && P2.total_units > 0;
+  const int64_t paa_blocks = std::max<int64_t>(
+      std::min<int64_t>((paapre.back() + 255) / 256, static_cast<int64_t>(ws.sms) * 16), 1);
+  const int64_t fill2_blocks = std::max<int64_t>(
+      std::min<int64_t>((N2ns + 255) / 256, static_cast<int64_t>(ws.sms) * 16), 1);
+  const int64_t seed2_blocks = std::max<int64_t>(
+      std::min<int64_t>((wpre2.back() + 255) / 256, static_cast<int64_t>(ws.sms) * 32), 1);
+  const int64_t bseed_blocks = std::max<int64_t>(
+      std::min<int64_t>((wpre2.back() + 7) / 8, static_cast<int64_t>(ws.sms) * 16), 1);
 
   // ---- copies in ----
   CUDA_TRY(cudaEventRecord(ws.ev0, st));
+  if (seeded) {
+    CUDA_TRY(cudaMemcpyAsync(d_paa, paa_jobs.data(), sizeof(PaaJob) * nseed_jobs,
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_paapre, paapre.data(), 8 * paapre.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_jobs2, jobs2.data(), sizeof(StatsJob) * nseed_jobs,
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_jpre2, jpre2.data(), 8 * jpre2.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_probs2, probs2.data(), sizeof(Problem) * probs2.size(),
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_wpre2, wpre2.data(), 8 * wpre2.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_bpre2, bpre2.data(), 8 * bpre2.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_seed, seed_jobs.data(), sizeof(BatchSeedJob) * nseed_jobs,
+                             cudaMemcpyHostToDevice, st));
+  }
   CUDA_TRY(cudaMemcpyAsync(d_raw, h_raw.data(), Nn * 8, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(d_prof, h_prof.data(), Nns * 8, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(StatsJob) * count, cudaMemcpyHostToDevice, st));
@@ -2074,12 +2262,13 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   }
 
   // ---- device part: one graph ----
-  uint32_t launches = probs.empty() ? 3 : 7;
+  uint32_t launches = probs.empty() ? 3 : (seeded ? 13 : 7);
   const std::vector<int64_t> key = {
       reinterpret_cast<int64_t>(arena), Nn, Nns, Nblk, count, want_corr ? 1 : 0, bands_max,
       jpre[count], kl.idx_bits, static_cast<int64_t>(probs.size()), seed_blocks, band_total,
       P.total_units, grid, reinterpret_cast<int64_t>(P.vreq), P.vreq_cap,
-      static_cast<int64_t>(smem), reinterpret_cast<int64_t>(st)};
+      static_cast<int64_t>(smem), reinterpret_cast<int64_t>(st), seeded ? 1 : 0, N2n, N2ns, N2blk,
+      nseed_jobs, bands2_max, band_total2, P2.total_units, grid2};
   if (!ws.batch_exec || ws.batch_key != key) {
     auto enqueue = [&]() -> cudaError_t {
       cudaError_t e;
@@ -2088,6 +2277,20 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
       profile_to_keys_kernel<<<static_cast<unsigned>((Nns + 255) / 256), 256, 0, st>>>(d_prof, d_keys,
                                                                                        Nns, kl);
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      if (seeded) {
+        const int nj = static_cast<int>(nseed_jobs);
+        paa_batch_kernel<<<static_cast<unsigned>(paa_blocks), 256, 0, st>>>(d_paa, d_paapre, nj);
+        stats_batch_kernel<<<static_cast<unsigned>(jpre2.back()), 128, 0, st>>>(d_jobs2, d_jpre2, nj, 0,
+                                                                                 chunk);
+        fill_key_floor_kernel<<<static_cast<unsigned>(fill2_blocks), 256, 0, st>>>(A2.keys, N2ns,
+                                                                                    kSeedFloor, kl);
+        diag_seed_kernel<<<static_cast<unsigned>(seed2_blocks), 256, 0, st>>>(d_probs2, d_wpre2, nj, kl);
+        if ((e = cudaMemsetAsync(d_counter2, 0, 64, st)) != cudaSuccess) return e;
+        join_mixed_1nn_kernel<<<static_cast<unsigned>(grid2), mixed_1nn_threads(), smem, st>>>(P2);
+        batch_seed_kernel<<<static_cast<unsigned>(bseed_blocks), 256, 0, st>>>(d_seed, d_wpre2, nj,
+                                                                                kl, kSeedFloor);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      }
       if (!probs.empty()) {
         diag_seed_kernel<<<static_cast<unsigned>(seed_blocks), 256, 0, st>>>(
             d_probs, d_wpre, static_cast<int>(probs.size()), kl);

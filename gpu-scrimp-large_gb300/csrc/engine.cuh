@@ -310,6 +310,33 @@ __global__ void seed_kernel(SeedArgs S);
 __global__ void diag_seed_kernel(const Problem* __restrict__ probs,
                                  const int64_t* __restrict__ win_prefix, int nprob, KeyLayout kl);
 
+// Block-averaged pre-pass of a batch: one series' averaged copy.
+struct PaaJob {
+  const double* src;      // the series (raw samples)
+  double* dst;            // n_out block means (NaN where a block holds a non-finite sample)
+  int64_t n_out;
+  int f;                  // samples per block
+};
+// Output sample t of the launch belongs to job p, out_prefix[p] <= t < out_prefix[p + 1].
+__global__ void paa_batch_kernel(const PaaJob* __restrict__ jobs,
+                                 const int64_t* __restrict__ out_prefix, int njobs);
+// Keys {r = floor, index 0}: the pre-pass only looks for partners above floor.
+__global__ void fill_key_floor_kernel(uint64_t* __restrict__ keys, int64_t n, float floor,
+                                      KeyLayout kl);
+// Seeds of one series of a batch from its pre-pass (self-join).
+struct BatchSeedJob {
+  SeriesDev X;               // the series' windows
+  uint64_t* key;             // its profile keys
+  const uint64_t* paa_key;   // keys of its block-averaged windows
+  int64_t ns_paa;
+  int64_t excl, m;
+  int f;
+};
+// Warp w of the launch seeds averaged window w - paa_prefix[p] of job p.
+__global__ void batch_seed_kernel(const BatchSeedJob* __restrict__ jobs,
+                                  const int64_t* __restrict__ paa_prefix, int njobs,
+                                  KeyLayout kl, float floor);
+
 // FP64 re-evaluation of the reported 1NN cells (final_eval.cu): one side is
 // one profile's keys, with the series of its windows (X) and of its
 // partners (Y).  prof_in / max_in: the profile given on input (its entries

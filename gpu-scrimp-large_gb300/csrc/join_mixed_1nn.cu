@@ -342,7 +342,7 @@ __device__ __forceinline__ float verify_cov_warp(const SeriesDev& R, const Serie
   return a;
 }
 
-// The whole covariance, one lane (used when the request buffer is full).
+// The whole covariance, one lane (the diagonal seeds).
 __device__ __noinline__ float verify_cov_lane(const SeriesDev& R, const SeriesDev& C,
                                               int64_t i, int64_t j, int64_t m) {
   return cov_part(R, C, i, j, 0, m);
@@ -449,9 +449,12 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
             q.ub = rv + mk;
             cx.vreq[slot] = q;
           } else {
-            const float ev = verify_cov_lane(pr.R, pr.C, i, j, cx.m) * ivc * ivr;
-            if (cx.sum_mode) add = ev > cx.thr ? ev : 0.f;
-            else publish(sm, cx, ev, i, j, r0 + rr, rcs, g);
+            // request buffer full: the FP32 value decides, and its margin
+            // enters the join's accuracy statement (a lane-serial direct dot
+            // here would stall the warp for every such cell)
+            if (cx.sum_mode) add = rv > cx.thr ? rv : 0.f;
+            else publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
+            tmax = fmaxf(tmax, mk);
           }
         } else if (cx.sum_mode) {
           add = rv > cx.thr ? rv : 0.f;
@@ -1338,6 +1341,105 @@ __global__ void __launch_bounds__(256) diag_seed_kernel(const Problem* __restric
       best = kr > best ? kr : best;
     }
     if (pr.key_row && best) atomicMax(reinterpret_cast<u64*>(pr.key_row + i), best);
+  }
+}
+
+// Largest p with prefix[p] <= t (prefix[0] = 0, p < n).
+__device__ __forceinline__ int job_of(const int64_t* __restrict__ prefix, int n, int64_t t) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void paa_batch_kernel(const PaaJob* __restrict__ jobs,
+                                 const int64_t* __restrict__ out_prefix, int njobs) {
+  const int64_t total = out_prefix[njobs];
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < total;
+       t += stride) {
+    const int p = job_of(out_prefix, njobs, t);
+    const PaaJob& J = jobs[p];
+    const int64_t k = t - out_prefix[p];
+    double sum = 0.0;
+    bool finite = true;
+    for (int u = 0; u < J.f; ++u) {
+      const double v = J.src[static_cast<int64_t>(J.f) * k + u];
+      finite = finite && isfinite(v);
+      sum += v;
+    }
+    J.dst[k] = finite ? sum / J.f : __longlong_as_double(0x7FF8000000000000ll);
+  }
+}
+
+__global__ void fill_key_floor_kernel(uint64_t* __restrict__ keys, int64_t n, float floor,
+                                      KeyLayout kl) {
+  const uint64_t key = make_key(q_from_float_bits(__float_as_uint(floor), kl.frac_bits), 0, kl);
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride)
+    keys[k] = key;
+}
+
+// One warp per block-averaged window i' of a series (PreSCRIMP-style seeds
+// with a neighbourhood refinement): its pre-pass partner j' puts the windows
+// i = f i' + o (o < f) near diagonal D = f (j' - i'); lane l takes diagonal
+// D + l - 15 (|l - 15| < f), computes its first cell's covariance directly
+// (FP32, centred) and walks the block's rows with the FP32 recurrence; per
+// row the warp keeps the best of its cells, merged into that window's key.
+// Every seed is a real cell's r, so the join's result does not depend on
+// them; good seeds only spare the join's exact path the records a cold start
+// sets (a short series' best improves about ln(n) times as the bands sweep
+// outward).
+__global__ void __launch_bounds__(256) batch_seed_kernel(const BatchSeedJob* __restrict__ jobs,
+                                                         const int64_t* __restrict__ paa_prefix,
+                                                         int njobs, KeyLayout kl, float floor) {
+  const int lane = threadIdx.x & 31;
+  const int64_t total = paa_prefix[njobs];
+  const int64_t nwarps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  const uint64_t q_floor = q_from_float_bits(__float_as_uint(floor), kl.frac_bits);
+  for (int64_t w = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; w < total;
+       w += nwarps) {
+    const int p = job_of(paa_prefix, njobs, w);
+    const BatchSeedJob& J = jobs[p];
+    const int64_t ip = w - paa_prefix[p];
+    const uint64_t pk = J.paa_key[ip];
+    if ((pk >> kl.idx_bits) <= q_floor) continue;  // no partner above the floor (warp-uniform)
+    const int64_t jp = static_cast<int64_t>(kl.idx_mask - (pk & kl.idx_mask));
+    const int f = J.f;
+    const int64_t ns = J.X.ns;
+    const int64_t i0 = static_cast<int64_t>(f) * ip;
+    const int delta = lane - 15;
+    const int64_t d = static_cast<int64_t>(f) * (jp - ip) + delta;
+    // rows o in [o_lo, o_hi) of this lane's diagonal are cells of the join
+    int64_t o_lo = 0, o_hi = 0;
+    if (lane < 31 && (delta < f && -delta < f) && (d >= J.excl || -d >= J.excl)) {
+      o_lo = -(i0 + d) > 0 ? -(i0 + d) : 0;
+      o_hi = f;
+      if (ns - i0 < o_hi) o_hi = ns - i0;
+      if (ns - i0 - d < o_hi) o_hi = ns - i0 - d;
+    }
+    float cov = 0.f;
+    if (o_lo < o_hi) cov = cov_part(J.X, J.X, i0 + o_lo, i0 + o_lo + d, 0, J.m);
+    for (int o = 0; o < f; ++o) {
+      const int64_t i = i0 + o, j = i + d;
+      const bool valid = o >= o_lo && o < o_hi;
+      uint64_t key = 0;
+      if (valid) {
+        const float ivi = J.X.inv32[i], ivj = J.X.inv32[j];
+        if (!isnan(ivi) && !isnan(ivj))
+          key = make_key(q_from_float_bits(__float_as_uint((cov * ivj) * ivi), kl.frac_bits), j, kl);
+        if (o + 1 < o_hi)
+          cov = fmaf(J.X.df32[i], J.X.dg32[j], fmaf(J.X.df32[j], J.X.dg32[i], cov));
+      }
+#pragma unroll
+      for (int s = 16; s > 0; s >>= 1) {
+        const uint64_t other = __shfl_xor_sync(0xffffffffu, key, s);
+        key = other > key ? other : key;
+      }
+      if (lane == 0 && key && i < ns) atomicMax(reinterpret_cast<u64*>(J.key + i), key);
+    }
   }
 }
 

@@ -34,7 +34,9 @@ def test_batch_matches_oracle(gpu_engine, oracle_mod):
         _, gi = gpu_engine.unpack_profile(r["profile_a"])
         check_1nn("batch%d" % k, r["corr_a"], gi, want["corr_a"], want["idx_a"], TOL_MIXED,
                   x, x, m)
-    assert out[0]["gpu_launches"] <= 8  # one launch per stage for the whole batch
+    # one launch per stage for the whole batch (the block-averaged pre-pass
+    # that seeds it adds six)
+    assert out[0]["gpu_launches"] <= 13
 
 
 def test_batch_equals_single_joins(gpu_engine):
