@@ -97,6 +97,9 @@ constexpr double kTcTableBudget = 4.0 * (1 << 30);
 // anchor rows fill whole 16-row tiles), down to half of it when a chunk's
 // verification requests approach the buffer's capacity.
 constexpr int64_t kTcMinChunkRows = 16;
+// Mixed MATRIX_SUMMARY: the least windows per grid row and column (a band
+// kernel block spans 8 rows and 15 columns).
+constexpr int64_t kMatMixedMinSpan = 64;
 // Largest |anchor - FP64| inv_r inv_c the self-check accepts.
 constexpr double kTcCheckTol = 1e-5;
 
@@ -662,10 +665,19 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   // the k-best and matrix-summary types run the FP64 visit kernel
   const bool max_only = a->profile_type == SCAMP_PROFILE_1NN;
   const bool is_1nn = a->profile_type == SCAMP_PROFILE_1NN_INDEX || max_only;
-  const bool visit = a->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS ||
-                     a->profile_type == SCAMP_PROFILE_MATRIX_SUMMARY;
   const bool mixed = a->precision_type == SCAMP_PRECISION_MIXED ||
                      a->precision_type == SCAMP_PRECISION_SINGLE;
+  // MATRIX_SUMMARY grid: rows are windows of B (of A in a self-join),
+  // columns windows of A.  The mixed form takes the band kernel's per-cell
+  // maxima when grid entries span enough windows that most of its 8 x 15
+  // blocks fall inside one; else (and in FP64) the visit kernel serves it.
+  const bool is_mat = a->profile_type == SCAMP_PROFILE_MATRIX_SUMMARY;
+  const int64_t mat_rpc = is_mat ? (plan.ns_b + a->matrix_height - 1) / a->matrix_height : 1;
+  const int64_t mat_cpc = is_mat ? (plan.ns_a + a->matrix_width - 1) / a->matrix_width : 1;
+  const bool mat_mixed = is_mat && mixed && mat_rpc >= kMatMixedMinSpan &&
+                         mat_cpc >= kMatMixedMinSpan && std::max(plan.ns_a, plan.ns_b) < (int64_t{1} << 31) &&
+                         static_cast<int64_t>(a->matrix_height) * a->matrix_width < (int64_t{1} << 31);
+  const bool visit = a->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS || (is_mat && !mat_mixed);
   const bool ultra = a->precision_type == SCAMP_PRECISION_ULTRA;
   const int64_t m = plan.m;
   const int64_t na = static_cast<int64_t>(a->len_a);
@@ -777,7 +789,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
           ex->knn[s], reinterpret_cast<uint64_t*>(vkeys[s]), nsz[s] * knn_k, kl);
       ++launches;
     }
-  } else if (visit) {
+  } else if (is_mat) {
     if (!ex || !ex->matrix) { *msg = "Error: profile buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
     void* p;
     if ((rc = ensure(ws, S_MAT, mat_n * 4, &p, msg))) return rc;
@@ -837,11 +849,12 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   enum { K_FP64, K_MIXED, K_VISIT } kind = visit ? K_VISIT : !mixed ? K_FP64 : K_MIXED;
   // (SUM_THRESH keeps the per-cell filter unless asked: its fast path adds
   // the blocks that lie wholly above the threshold, which needs per-cell r)
-  const bool coarse = kind == K_MIXED && (a->filter_mode == 2 ||
-                                          (a->filter_mode == 0 && is_1nn &&
-                                           m >= kCoarseFilterMinWindow));
+  const bool coarse = kind == K_MIXED && !is_mat &&
+                      (a->filter_mode == 2 ||
+                       (a->filter_mode == 0 && is_1nn && m >= kCoarseFilterMinWindow));
   const void* kfn = kind == K_VISIT ? reinterpret_cast<const void*>(join_visit_kernel)
                   : kind == K_FP64 ? reinterpret_cast<const void*>(join_fp64_kernel)
+                  : is_mat ? reinterpret_cast<const void*>(join_mixed_mat_kernel)
                   : is_1nn ? (coarse ? reinterpret_cast<const void*>(join_mixed_1nn_coarse_kernel)
                                      : reinterpret_cast<const void*>(join_mixed_1nn_kernel))
                            : (coarse ? reinterpret_cast<const void*>(join_mixed_sum_coarse_kernel)
@@ -921,6 +934,19 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   P.refresh_cols = (kind == K_MIXED && is_1nn && !seed_a) ? 1 : 0;
   P.threshold = a->distance_threshold;
   P.kl = kl;
+  if (mat_mixed) {
+    P.mat = vmat;
+    P.mat_w = a->matrix_width;
+    P.rows_per_cell = mat_rpc;
+    P.cols_per_cell = mat_cpc;
+    // ceil(2^64 / d) for d >= 2
+    P.rpc_magic = UINT64_MAX / static_cast<uint64_t>(mat_rpc) + 1;
+    P.cpc_magic = UINT64_MAX / static_cast<uint64_t>(mat_cpc) + 1;
+    for (int p = 0; p < P.nprob; ++p) {
+      P.mat_col[p] = plan.probs[p].col_target == 0 ? 1 : 0;
+      P.mat_row[p] = plan.probs[p].row_target == 0 ? 1 : 0;
+    }
+  }
   // Tensor-core anchors (anchor_tc.cu): mixed joins of long windows whose
   // anchor interval is a multiple of the contraction's 1024-column tiles.
   const bool use_tc = tc_eligible && K % 1024 == 0;
@@ -974,7 +1000,9 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
       ws.timed_kernel = true;
     }
     auto launch_band = [&](const JoinParams& Q, int64_t g) {
-      if (is_1nn && coarse)
+      if (is_mat)
+        join_mixed_mat_kernel<<<static_cast<unsigned>(g), nthreads, smem, st>>>(Q);
+      else if (is_1nn && coarse)
         join_mixed_1nn_coarse_kernel<<<static_cast<unsigned>(g), nthreads, smem, st>>>(Q);
       else if (is_1nn)
         join_mixed_1nn_kernel<<<static_cast<unsigned>(g), nthreads, smem, st>>>(Q);
@@ -1035,7 +1063,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
         CUDA_TRY(cudaMemcpyAsync(dprefix, cpre.data(), cpre.size() * 8, cudaMemcpyHostToDevice, st));
         CUDA_TRY(cudaMemsetAsync(P.unit_counter, 0, 8, st));
         launch_band(Q, std::min<int64_t>(resident, cunits));
-        if (u0 + Uc < urows) {
+        if (u0 + Uc < urows && !is_mat) {
           // the chunk's deferred verifications now, so that the request
           // buffer only ever holds one chunk's requests (a long join's would
           // overflow it); the last chunk's go to the verification below
@@ -1063,7 +1091,11 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
         CUDA_TRY(cudaEventRecord(ws.evkv, st));
         ws.timed_verify = true;
       }
-      verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
+      // (the matrix form makes no requests: it publishes its maxima directly)
+      if (!is_mat) {
+        verify_requests_kernel<<<static_cast<unsigned>(ws.sms * 8), 256, 0, st>>>(P);
+        ++launches;
+      }
     } else if (kind == K_VISIT) {
       VisitArgs V{};
       V.mode = a->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS ? 0 : 1;
@@ -1080,9 +1112,11 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
         V.row_target[p] = plan.probs[p].row_target;
       }
       join_visit_kernel<<<static_cast<unsigned>(grid), nthreads, 0, st>>>(P, V);
-    } else
+      ++launches;
+    } else {
       join_fp64_kernel<<<static_cast<unsigned>(grid), nthreads, 0, st>>>(P);
-    ++launches;
+      ++launches;
+    }
     CUDA_TRY(cudaGetLastError());
     if (!nested) CUDA_TRY(cudaEventRecord(ws.evk1, st));
   }

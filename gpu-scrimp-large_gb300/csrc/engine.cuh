@@ -165,6 +165,16 @@ struct JoinParams {
   KeyLayout kl;
   float anchor_vcoef;               // initial drift estimate of an anchor / cov^2
   int refresh_cols;                 // mixed 1NN: refresh kept ring columns' bests per slab
+  // MATRIX_SUMMARY, mixed form: the grid (order-preserving images of
+  // floats, mat_w entries per grid row), windows per grid row and column
+  // with their division magics ceil(2^64 / d), and per problem whether its
+  // column results (cell (i, j) -> grid (i / rpc, j / cpc)) and its row
+  // results (-> grid (j / rpc, i / cpc)) enter the grid.
+  unsigned* mat;
+  int64_t mat_w;
+  int64_t rows_per_cell, cols_per_cell;
+  uint64_t rpc_magic, cpc_magic;
+  int mat_col[kMaxProblems], mat_row[kMaxProblems];
 };
 
 // Outputs of the two experimental profile types (join_visit.cu).
@@ -260,6 +270,7 @@ __global__ void join_mixed_sum_kernel(JoinParams P);  // mixed SUM_THRESH
 // the same with the per-step covariance bound as the fast path's filter
 __global__ void join_mixed_1nn_coarse_kernel(JoinParams P);
 __global__ void join_mixed_sum_coarse_kernel(JoinParams P);
+__global__ void join_mixed_mat_kernel(JoinParams P);  // mixed MATRIX_SUMMARY
 __global__ void verify_requests_kernel(JoinParams P);
 
 // Tensor-core anchors of one problem's chunk of anchor rows (anchor_tc.cu).

@@ -172,6 +172,13 @@ struct SlowCtx {
   unsigned long long* vcount;      // their count (may exceed vcap)
   int64_t vcap;
   unsigned long long* tmargin;     // largest drift margin of a trusted FP32 value (float bits)
+  // MATRIX_SUMMARY: the grid and its geometry (JoinParams), the current
+  // problem's targets
+  unsigned* mat;
+  int64_t mat_w;
+  int64_t rpc, cpc;
+  uint64_t rpc_magic, cpc_magic;
+  bool mcol, mrow;
 };
 
 struct Smem {
@@ -566,6 +573,76 @@ __device__ __noinline__ void fast_add_block(Smem& sm, const float2 (&cov_end)[kD
   }
 }
 
+// MATRIX_SUMMARY: a thread's running maxima (per segment and target).
+struct MatRun {
+  int cell[2][2];
+  float mx[2][2];
+};
+
+// Order-preserving uint32 image of a float (not NaN).
+__device__ __forceinline__ unsigned ord_float(float x) {
+  const unsigned b = __float_as_uint(x);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+// n / d for n < 2^32 and d >= 2 from M = ceil(2^64 / d): exact while
+// n d < 2^64 (floor(n M / 2^64) = n / d + n e / (d 2^64), e = M d - 2^64 < d).
+__device__ __forceinline__ int64_t div_magic(int64_t n, uint64_t M) {
+  return static_cast<int64_t>(__umul64hi(static_cast<uint64_t>(n), M));
+}
+
+// MATRIX_SUMMARY: a thread-step whose block crosses a grid boundary (flags
+// fx, fy per segment) is walked again from the step's start (rewound from
+// the covariances at its end, as the exact path rewinds), and every cell
+// above the threshold goes to its own grid entry.
+__device__ __noinline__ void mat_cells_block(Smem& sm, const float2 (&cov_end)[kDiags], int s,
+                                             int t, bool fx, bool fy) {
+  const SlowCtx& cx = sm.cx;
+  const int r0 = s * kRows;
+  const int cb0 = 8 * (s + t);
+  float2 c[kDiags];
+#pragma unroll
+  for (int k = 0; k < kDiags; ++k) c[k] = cov_end[k];
+#pragma unroll 1
+  for (int rr = kRows - 1; rr >= 0; --rr) {
+    const float4 rf = sm.r_fg[r0 + rr];
+#pragma unroll
+    for (int k = 0; k < kDiags; ++k) {
+      const float4 cf = col_fg(sm, padc(ringc(cx.ring0, cb0 + rr + k)));
+      c[k] = fma2(make_float2(-rf.x, -rf.y), make_float2(cf.z, cf.w), c[k]);
+      c[k] = fma2(make_float2(-cf.x, -cf.y), make_float2(rf.z, rf.w), c[k]);
+    }
+  }
+#pragma unroll 1
+  for (int rr = 0; rr < kRows; ++rr) {
+    const float4 rf = sm.r_fg[r0 + rr];
+    const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
+    const float2 ivr = sm.r_iv[r0 + rr];
+#pragma unroll
+    for (int k = 0; k < kDiags; ++k) {
+      const int slot = padc(ringc(cx.ring0, cb0 + rr + k));
+      const float2 r2 = mul2(mul2(c[k], sm.u.s.c_iv[slot]), ivr);
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const float r = g ? r2.y : r2.x;
+        if ((g ? fy : fx) && r > cx.thr) {  // false for NaN
+          const int64_t i = cx.rbase[g] + r0 + rr;
+          const int64_t j = i + cx.D0 + t * kDiags + k;
+          if (cx.mcol)
+            atomicMax(cx.mat + div_magic(i, cx.rpc_magic) * cx.mat_w + div_magic(j, cx.cpc_magic),
+                      ord_float(r));
+          if (cx.mrow)
+            atomicMax(cx.mat + div_magic(j, cx.rpc_magic) * cx.mat_w + div_magic(i, cx.cpc_magic),
+                      ord_float(r));
+        }
+      }
+      const float4 cf = col_fg(sm, slot);
+      c[k] = fma2(make_float2(cf.x, cf.y), dgr, c[k]);
+      c[k] = fma2(dfr, make_float2(cf.z, cf.w), c[k]);
+    }
+  }
+}
+
 // The band kernel's body; kSum selects SUM_THRESH (separate instantiations,
 // so the 1NN_INDEX form carries none of the sum bookkeeping).  kCoarse
 // selects the fast path's filter:
@@ -577,8 +654,9 @@ __device__ __noinline__ void fast_add_block(Smem& sm, const float2 (&cov_end)[kD
 //          tight where the inverse norms of neighbouring windows are close
 //          (long windows); a block it flags goes to the exact path, which
 //          checks every cell with its own r.
-template <bool kSum, bool kCoarse>
+template <bool kSum, bool kCoarse, bool kMat = false>
 __device__ __forceinline__ void band_body(const JoinParams& P) {
+  static_assert(!(kMat && (kSum || kCoarse)), "the matrix form takes per-cell maxima");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   const int t = threadIdx.x;
@@ -588,6 +666,21 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
   unsigned long long n_steps = 0, n_slow = 0, n_verify = 0;
   int qn = 0;  // queued blocks of this warp (warp-uniform)
   float tfast = 0.f;  // SUM_THRESH: largest margin of a block added on the fast path
+  // MATRIX_SUMMARY: per segment (x, y) and target (column, row results) the
+  // grid entry the thread's recent blocks fell in and their largest r, kept
+  // in the exact path's queue space (the matrix form queues nothing)
+  static_assert(sizeof(MatRun) * kThreads <= sizeof(SlowItem) * kWarps * kQueue,
+                "matrix state exceeds the queue space");
+  MatRun& mrun = reinterpret_cast<MatRun*>(&sm.queue[0][0])[t];
+  if constexpr (kMat) {
+#pragma unroll
+    for (int g = 0; g < 2; ++g)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        mrun.cell[g][h] = -1;
+        mrun.mx[g][h] = -3.f;
+      }
+  }
 
   for (;;) {
     if (t == 0) {
@@ -797,6 +890,16 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
       cx.tmargin = P.counters + 4;
       cx.sum_mode = kSum;
       cx.thr = static_cast<float>(P.threshold);
+      if constexpr (kMat) {
+        cx.mat = P.mat;
+        cx.mat_w = P.mat_w;
+        cx.rpc = P.rows_per_cell;
+        cx.cpc = P.cols_per_cell;
+        cx.rpc_magic = P.rpc_magic;
+        cx.cpc_magic = P.cpc_magic;
+        cx.mcol = P.mat_col[sm.prob_index] != 0;
+        cx.mrow = P.mat_row[sm.prob_index] != 0;
+      }
     }
 
     // ---------------- slabs ----------------
@@ -1061,6 +1164,53 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
           }
         }
         bool trig = bx > tx || by > ty;
+        if constexpr (kMat) {
+          // a block inside one grid entry (per target) raises the thread's
+          // running maximum of that entry, published when the thread's
+          // blocks move on; a block across a grid boundary routes each cell
+          trig = false;
+          const float2 smg = mul2(make_float2(kStepMarginC, kStepMarginC), mg);
+          bool nonuni[2] = {false, false};
+#pragma unroll
+          for (int g = 0; g < 2; ++g) {
+            const float bm = g ? by : bx;
+            if (!(bm > thr)) continue;
+            tfast = fmaxf(tfast, g ? smg.y : smg.x);
+            const int64_t i0 = rbase[g] + r0, j0 = i0 + d_my;
+            const int64_t rpc = sm.cx.rpc, cpc = sm.cx.cpc;
+            int cell[2] = {-1, -1};
+            bool uni = true;
+            if (sm.cx.mcol) {
+              const int64_t qa = div_magic(i0, sm.cx.rpc_magic), qb = div_magic(j0, sm.cx.cpc_magic);
+              uni = uni && i0 - qa * rpc + (kRows - 1) < rpc &&
+                    j0 - qb * cpc + (kRows + kDiags - 2) < cpc;
+              cell[0] = static_cast<int>(qa * sm.cx.mat_w + qb);
+            }
+            if (sm.cx.mrow) {
+              const int64_t qa = div_magic(j0, sm.cx.rpc_magic), qb = div_magic(i0, sm.cx.cpc_magic);
+              uni = uni && j0 - qa * rpc + (kRows + kDiags - 2) < rpc &&
+                    i0 - qb * cpc + (kRows - 1) < cpc;
+              cell[1] = static_cast<int>(qa * sm.cx.mat_w + qb);
+            }
+            if (!uni) {
+              nonuni[g] = true;
+              continue;
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              if (cell[h] < 0) continue;
+              const int cur = mrun.cell[g][h];
+              if (cell[h] != cur) {
+                if (cur >= 0) atomicMax(sm.cx.mat + cur, ord_float(mrun.mx[g][h]));
+                mrun.cell[g][h] = cell[h];
+                mrun.mx[g][h] = bm;
+              } else {
+                mrun.mx[g][h] = fmaxf(mrun.mx[g][h], bm);
+              }
+            }
+          }
+          if (nonuni[0] || nonuni[1]) mat_cells_block(sm, cov, s, t, nonuni[0], nonuni[1]);
+        }
         if constexpr (kSum && !kCoarse) {
           // A segment whose every valid cell is above the threshold by more
           // than the step's margin needs no exact path: each of its cells
@@ -1174,7 +1324,14 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
     atomicAdd(P.counters + 1, n_slow);
     atomicAdd(P.counters + 2, n_verify);
   }
-  if constexpr (kSum) {
+  if constexpr (kMat) {
+#pragma unroll
+    for (int g = 0; g < 2; ++g)
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+        if (mrun.cell[g][h] >= 0) atomicMax(P.mat + mrun.cell[g][h], ord_float(mrun.mx[g][h]));
+  }
+  if constexpr (kSum || kMat) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) tfast = fmaxf(tfast, __shfl_xor_sync(0xffffffffu, tfast, o));
     if (lane == 0 && P.counters && tfast > 0.f)
@@ -1192,6 +1349,10 @@ __global__ void __launch_bounds__(kThreads, 4) join_mixed_1nn_kernel(JoinParams 
 
 __global__ void __launch_bounds__(kThreads, 4) join_mixed_sum_kernel(JoinParams P) {
   band_body<true, false>(P);
+}
+
+__global__ void __launch_bounds__(kThreads, 4) join_mixed_mat_kernel(JoinParams P) {
+  band_body<false, false, true>(P);
 }
 
 __global__ void __launch_bounds__(kThreads, 4) join_mixed_1nn_coarse_kernel(JoinParams P) {

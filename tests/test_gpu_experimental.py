@@ -7,7 +7,7 @@ per window must be the true k best up to near-ties."""
 import numpy as np
 import pytest
 
-from parity import window_stats
+from parity import TOL_MIXED, window_stats
 
 pytestmark = pytest.mark.gpu
 
@@ -85,19 +85,27 @@ def test_knn_abjoin_and_pyscamp_surface(gpu_engine):
     assert abs(v - np.sqrt(max(2 * m * (1 - C[row, c]), 0))) < 1e-3
 
 
-def check_matrix(mat, C, h, w, thr):
+def check_matrix(mat, C, h, w, thr, tol=TOL):
+    """Grid entries against the brute-force maxima above `thr`; with the
+    mixed form's tolerance an entry whose largest cell lies within `tol` of
+    the threshold may be either side of it."""
     rpc = -(-C.shape[0] // h)
     cpc = -(-C.shape[1] // w)
     want = np.full((h, w), -2.0)
+    top = np.full((h, w), -2.0)
     for y in range(h):
         for x in range(w):
             blk = C[y * rpc:(y + 1) * rpc, x * cpc:(x + 1) * cpc]
+            if np.any(blk == blk):
+                top[y, x] = np.nanmax(blk)
             v = blk[blk > thr]
             if v.size:
                 want[y, x] = v.max()
-    assert np.array_equal(mat < -1, want < -1)
-    ok = want >= -1
-    assert np.max(np.abs(mat[ok] - want[ok]), initial=0.0) <= TOL
+    edge = np.abs(top - thr) <= tol
+    assert np.array_equal((mat < -1)[~edge], (want < -1)[~edge])
+    ok = (want >= -1) & (mat >= -1)
+    assert np.max(np.abs(mat[ok] - want[ok]), initial=0.0) <= tol
+    assert np.all(mat[(mat >= -1) & (want < -1)] <= thr + tol)
 
 
 @pytest.mark.parametrize("precision", ["double", "mixed"])
@@ -106,16 +114,21 @@ def test_matrix_summary(gpu_engine, precision):
     a, b = rw(rng, 3000), rw(rng, 2000)
     m = 64
     # self-join: columns only, so the cells with j - i >= m/4 (upper triangle)
+    tol = TOL if precision == "double" else TOL_MIXED
     r = gpu_engine.join(a, None, m, "MATRIX_SUMMARY", precision, threshold=0.2,
                         matrix_height=20, matrix_width=30)
     C = corr_matrix(a, a, m)
     ii, jj = np.indices(C.shape)
     C[jj - ii < m // 4] = np.nan
-    check_matrix(r["matrix"].astype(np.float64), C, 20, 30, 0.2)
+    check_matrix(r["matrix"].astype(np.float64), C, 20, 30, 0.2, tol)
+    if precision == "mixed":
+        # the band kernel's form (grid entries of >= 64 windows each), with
+        # its error statement
+        assert 0 <= r["max_abs_r_err"] <= TOL_MIXED
     # AB-join: every (window of b, window of a) cell
     r = gpu_engine.join(a, b, m, "MATRIX_SUMMARY", precision, computing_rows=False,
                         matrix_height=17, matrix_width=23)
-    check_matrix(r["matrix"].astype(np.float64), corr_matrix(b, a, m), 17, 23, 0.0)
+    check_matrix(r["matrix"].astype(np.float64), corr_matrix(b, a, m), 17, 23, 0.0, tol)
     # pyscamp surface: distances (NaN where none), shape (mheight, mwidth)
     d = gpu_engine.abjoin_matrix(a, b, m, mheight=17, mwidth=23)
     assert d.shape == (17, 23)
@@ -124,6 +137,32 @@ def test_matrix_summary(gpu_engine, precision):
     np.testing.assert_allclose(d, want, rtol=1e-5, atol=1e-4)
     p = gpu_engine.selfjoin_matrix(a, m, pearson=True, mheight=5, mwidth=5)
     assert p.shape == (5, 5)
+
+
+@pytest.mark.parametrize("shape", [(7, 5), (3, 64), (50, 2)])
+def test_matrix_summary_mixed_vs_fp64(gpu_engine, shape):
+    """The mixed form (band kernel, grid entries crossing its blocks at
+    uneven boundaries, NaN windows) against the FP64 visit kernel on a larger
+    self-join and an AB-join with both profiles' transposed halves."""
+    rng = np.random.default_rng(66)
+    a, b = rw(rng, 40000), rw(rng, 30000)
+    a[5000:5040] = np.nan
+    m = 100
+    h, w = shape
+    for bb in (None, b):
+        kw = dict(threshold=0.5, matrix_height=h, matrix_width=w)
+        if bb is not None:
+            kw["computing_rows"] = False
+        f = gpu_engine.join(a, bb, m, "MATRIX_SUMMARY", "double", **kw)
+        x = gpu_engine.join(a, bb, m, "MATRIX_SUMMARY", "mixed", **kw)
+        fm, xm = f["matrix"].astype(np.float64), x["matrix"].astype(np.float64)
+        both = (fm >= -1) & (xm >= -1)
+        assert both.sum() >= 0.9 * max((fm >= -1).sum(), 1)
+        assert np.max(np.abs(fm[both] - xm[both]), initial=0.0) <= TOL_MIXED
+        # an entry on one side only lies at the threshold's edge
+        assert np.all(fm[(fm >= -1) & (xm < -1)] <= 0.5 + TOL_MIXED)
+        assert np.all(xm[(xm >= -1) & (fm < -1)] <= 0.5 + TOL_MIXED)
+        assert 0 < x["max_abs_r_err"] <= TOL_MIXED
 
 
 def test_matrix_merges_into_given_matrix(gpu_engine):
