@@ -677,7 +677,12 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   const bool mat_mixed = is_mat && mixed && mat_rpc >= kMatMixedMinSpan &&
                          mat_cpc >= kMatMixedMinSpan && std::max(plan.ns_a, plan.ns_b) < (int64_t{1} << 31) &&
                          static_cast<int64_t>(a->matrix_height) * a->matrix_width < (int64_t{1} << 31);
-  const bool visit = a->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS || (is_mat && !mat_mixed);
+  // APPROX_ALL_NEIGHBORS in the mixed form: the band kernel with k-best
+  // lists (up to knn_mixed_max_k() entries); else the visit kernel
+  const bool is_knn = a->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS;
+  const bool knn_mixed = is_knn && mixed && a->max_matches_per_column >= 1 &&
+                         a->max_matches_per_column <= static_cast<uint64_t>(knn_mixed_max_k());
+  const bool visit = (is_knn && !knn_mixed) || (is_mat && !mat_mixed);
   const bool ultra = a->precision_type == SCAMP_PRECISION_ULTRA;
   const int64_t m = plan.m;
   const int64_t na = static_cast<int64_t>(a->len_a);
@@ -778,7 +783,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   unsigned* vmat = nullptr;
   const int64_t knn_k = a->max_matches_per_column;
   const int64_t mat_n = static_cast<int64_t>(a->matrix_height) * a->matrix_width;
-  if (visit && a->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS) {
+  if (is_knn) {
     for (int s = 0; s < 2; ++s) {
       if (!used[s]) continue;
       if (!ex || !ex->knn[s]) { *msg = "Error: profile buffer missing"; return SCAMP_ERR_INVALID_ARGS; }
@@ -849,12 +854,13 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   enum { K_FP64, K_MIXED, K_VISIT } kind = visit ? K_VISIT : !mixed ? K_FP64 : K_MIXED;
   // (SUM_THRESH keeps the per-cell filter unless asked: its fast path adds
   // the blocks that lie wholly above the threshold, which needs per-cell r)
-  const bool coarse = kind == K_MIXED && !is_mat &&
+  const bool coarse = kind == K_MIXED && !is_mat && !is_knn &&
                       (a->filter_mode == 2 ||
                        (a->filter_mode == 0 && is_1nn && m >= kCoarseFilterMinWindow));
   const void* kfn = kind == K_VISIT ? reinterpret_cast<const void*>(join_visit_kernel)
                   : kind == K_FP64 ? reinterpret_cast<const void*>(join_fp64_kernel)
                   : is_mat ? reinterpret_cast<const void*>(join_mixed_mat_kernel)
+                  : is_knn ? reinterpret_cast<const void*>(join_mixed_knn_kernel)
                   : is_1nn ? (coarse ? reinterpret_cast<const void*>(join_mixed_1nn_coarse_kernel)
                                      : reinterpret_cast<const void*>(join_mixed_1nn_kernel))
                            : (coarse ? reinterpret_cast<const void*>(join_mixed_sum_coarse_kernel)
@@ -909,6 +915,10 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     pr.d_lo = q.d_lo; pr.d_hi = q.d_hi; pr.x_lo = q.x_lo; pr.x_hi = q.x_hi;
     pr.key_col = is_1nn && q.col_target >= 0 ? keys[q.col_target] : nullptr;
     pr.key_row = is_1nn && q.row_target >= 0 ? keys[q.row_target] : nullptr;
+    if (knn_mixed) {
+      pr.key_col = q.col_target >= 0 ? reinterpret_cast<uint64_t*>(vkeys[q.col_target]) : nullptr;
+      pr.key_row = q.row_target >= 0 ? reinterpret_cast<uint64_t*>(vkeys[q.row_target]) : nullptr;
+    }
     pr.sum_col = !is_1nn && q.col_target >= 0 ? sums[q.col_target] : nullptr;
     pr.sum_row = !is_1nn && q.row_target >= 0 ? sums[q.row_target] : nullptr;
     pr.band_begin = band_total;
@@ -931,7 +941,8 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   P.profile_type = is_1nn ? SCAMP_PROFILE_1NN_INDEX : a->profile_type;
   // a join without seeds starts cold: the band kernel refreshes its ring
   // columns' bests every slab (seeded joins start near their final bests)
-  P.refresh_cols = (kind == K_MIXED && is_1nn && !seed_a) ? 1 : 0;
+  P.refresh_cols = (kind == K_MIXED && ((is_1nn && !seed_a) || knn_mixed)) ? 1 : 0;
+  P.knn_k = knn_mixed ? static_cast<int>(knn_k) : 0;
   P.threshold = a->distance_threshold;
   P.kl = kl;
   if (mat_mixed) {
@@ -1002,6 +1013,8 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     auto launch_band = [&](const JoinParams& Q, int64_t g) {
       if (is_mat)
         join_mixed_mat_kernel<<<static_cast<unsigned>(g), nthreads, smem, st>>>(Q);
+      else if (is_knn)
+        join_mixed_knn_kernel<<<static_cast<unsigned>(g), nthreads, smem, st>>>(Q);
       else if (is_1nn && coarse)
         join_mixed_1nn_coarse_kernel<<<static_cast<unsigned>(g), nthreads, smem, st>>>(Q);
       else if (is_1nn)
@@ -1146,6 +1159,25 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     }
   }
 
+  // ---- FP64 re-evaluation of the mixed form's k-best lists ----
+  if (knn_mixed) {
+    NvtxRange nvtx_eval("FP64 re-evaluation");
+    for (int s = 0; s < 2; ++s) {
+      if (!vkeys[s] || nsz[s] == 0) continue;
+      EvalSide es{};
+      es.keys = reinterpret_cast<uint64_t*>(vkeys[s]);
+      es.prof_in = ex->knn[s];
+      es.X = s == 0 ? devA : devB;
+      es.Y = plan.self_join ? devA : (s == 0 ? devB : devA);
+      es.ns = nsz[s];
+      es.m = m;
+      const int64_t blocks = std::min<int64_t>((nsz[s] + 31) / 32, static_cast<int64_t>(ws.sms) * 16);
+      knn_final_eval_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(
+          es, static_cast<int>(knn_k), a->distance_threshold, kl);
+      ++launches;
+    }
+  }
+
   // ---- keys -> packed entries (+ optional double correlations) ----
   for (int s = 0; s < 2; ++s) {
     if (!vkeys[s]) continue;
@@ -1178,12 +1210,13 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     res->gpu_launches = launches;
     // accuracy fields; the mixed form's tracked margin is read with the
     // work counters (read_times)
-    res->max_abs_r_err = is_1nn ? final_eval_bound(m, kl.frac_bits) : (kind == K_MIXED ? 0.0 : -1.0);
-    res->max_tie_margin = (is_1nn && kind == K_MIXED) ? 0.0 : -1.0;
+    const bool fp64_final = is_1nn || knn_mixed;  // values recomputed in FP64
+    res->max_abs_r_err = fp64_final ? final_eval_bound(m, kl.frac_bits) : (kind == K_MIXED ? 0.0 : -1.0);
+    res->max_tie_margin = (fp64_final && kind == K_MIXED) ? 0.0 : -1.0;
   }
   if (!nested) {
-    ws.tracked_sum_margin = !is_1nn && kind == K_MIXED;
-    ws.tracked_tie_margin = is_1nn && kind == K_MIXED;
+    ws.tracked_sum_margin = !is_1nn && !knn_mixed && kind == K_MIXED;
+    ws.tracked_tie_margin = (is_1nn || knn_mixed) && kind == K_MIXED;
   }
   return SCAMP_OK;
 }

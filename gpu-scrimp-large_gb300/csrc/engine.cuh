@@ -170,6 +170,9 @@ struct JoinParams {
   // with their division magics ceil(2^64 / d), and per problem whether its
   // column results (cell (i, j) -> grid (i / rpc, j / cpc)) and its row
   // results (-> grid (j / rpc, i / cpc)) enter the grid.
+  // APPROX_ALL_NEIGHBORS, mixed form: k > 0 makes key_row / key_col lists
+  // of k keys per window (largest first) instead of one key
+  int knn_k;
   unsigned* mat;
   int64_t mat_w;
   int64_t rows_per_cell, cols_per_cell;
@@ -271,6 +274,7 @@ __global__ void join_mixed_sum_kernel(JoinParams P);  // mixed SUM_THRESH
 __global__ void join_mixed_1nn_coarse_kernel(JoinParams P);
 __global__ void join_mixed_sum_coarse_kernel(JoinParams P);
 __global__ void join_mixed_mat_kernel(JoinParams P);  // mixed MATRIX_SUMMARY
+__global__ void join_mixed_knn_kernel(JoinParams P);  // mixed APPROX_ALL_NEIGHBORS
 __global__ void verify_requests_kernel(JoinParams P);
 
 // Tensor-core anchors of one problem's chunk of anchor rows (anchor_tc.cu).
@@ -365,6 +369,12 @@ struct EvalPair {
   KeyLayout kl;
 };
 __global__ void final_eval_kernel(EvalPair E);
+// The k-best lists of one side (k keys per window): every entry the join
+// made is recomputed in FP64 and each list re-sorted; entries of the input
+// list (prof_in, k packed entries per window) are kept as they are, entries
+// whose FP64 value is not above `thr` dropped.
+__global__ void knn_final_eval_kernel(EvalSide S, int k, double thr, KeyLayout kl);
+int knn_mixed_max_k();  // longest list the mixed k-best form keeps
 __global__ void final_eval_batch_kernel(const EvalSide* __restrict__ sides,
                                         const int64_t* __restrict__ win_prefix, int nsides,
                                         KeyLayout kl);

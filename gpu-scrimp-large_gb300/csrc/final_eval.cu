@@ -111,7 +111,72 @@ __device__ __forceinline__ void eval_window(const EvalSide& s, int64_t w, int64_
   }
 }
 
+// The key entry `e` of an input k-best list turns into: 0 when empty.
+__device__ __forceinline__ uint64_t list_entry_key(uint64_t e, const KeyLayout& kl) {
+  const uint32_t cbits = static_cast<uint32_t>(e);
+  const uint32_t idx = static_cast<uint32_t>(e >> 32);
+  if (!(__uint_as_float(cbits) >= -1.0f) || static_cast<uint64_t>(idx) > kl.idx_mask) return 0;
+  return make_key(q_from_float_bits(cbits, kl.frac_bits), idx, kl);
+}
+
+constexpr int kKnnMaxK = 64;  // longest list the mixed k-best form keeps
+
 }  // namespace
+
+int knn_mixed_max_k() { return kKnnMaxK; }
+
+// k-best lists: kLanes lanes per window, its k entries in turn (the slot loop
+// is warp-uniform, so the shuffle tree always has its lanes), then the
+// group's first lane re-sorts the list, largest key first (ties: the smaller
+// index, which the key's index field orders first).
+__global__ void __launch_bounds__(256) knn_final_eval_kernel(EvalSide S, int k, double thr,
+                                                             KeyLayout kl) {
+  const int lane = threadIdx.x & 31;
+  const int sub = lane & (kLanes - 1);
+  const int64_t nwarps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  constexpr int kGroups = 32 / kLanes;
+  for (int64_t g0 = ((static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * kGroups;
+       g0 < S.ns; g0 += nwarps * kGroups) {
+    const int64_t w = g0 + lane / kLanes;
+    const bool active = w < S.ns;
+    uint64_t* list = S.keys + (active ? w : 0) * k;
+    for (int s = 0; s < k; ++s) {
+      uint64_t key = active ? list[s] : 0;
+      if (key != 0 && S.prof_in) {
+        // an entry of the given list stays as it is
+        for (int t = 0; t < k; ++t)
+          if (list_entry_key(S.prof_in[w * k + t], kl) == key) {
+            key = 0;
+            break;
+          }
+      }
+      const int64_t j = key ? key_to_index(key, kl) : 0;
+      const bool work = key != 0 && j >= 0 && j < S.Y.ns;
+      const double r = corr_group_fp64(S.X, S.Y, work ? w : 0, work ? j : 0, work ? S.m : 0, sub,
+                                       sub == 0);
+      if (sub == 0 && work) {
+        const double rc = r > 1.0 ? 1.0 : (r < -1.0 ? -1.0 : r);
+        list[s] = (!isnan(r) && r > thr)
+                      ? make_key(q_from_double_bits(__double_as_longlong(rc), kl.frac_bits), j, kl)
+                      : 0;
+      }
+    }
+    if (sub == 0 && active) {
+      uint64_t v[kKnnMaxK];
+      const int kc = k < kKnnMaxK ? k : kKnnMaxK;
+      for (int s = 0; s < kc; ++s) {
+        const uint64_t x = list[s];
+        int p = s;
+        while (p > 0 && v[p - 1] < x) {
+          v[p] = v[p - 1];
+          --p;
+        }
+        v[p] = x;
+      }
+      for (int s = 0; s < kc; ++s) list[s] = v[s];
+    }
+  }
+}
 
 // Groups of kLanes lanes, one window each, over up to two profile sides (a
 // single join).  The loop bound is warp-uniform: a warp's four groups stay

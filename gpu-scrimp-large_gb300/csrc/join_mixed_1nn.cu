@@ -174,6 +174,7 @@ struct SlowCtx {
   unsigned long long* tmargin;     // largest drift margin of a trusted FP32 value (float bits)
   // MATRIX_SUMMARY: the grid and its geometry (JoinParams), the current
   // problem's targets
+  int knn_k;  // APPROX_ALL_NEIGHBORS: list length (0 otherwise)
   unsigned* mat;
   int64_t mat_w;
   int64_t rpc, cpc;
@@ -375,6 +376,47 @@ __device__ __forceinline__ void publish(Smem& sm, const SlowCtx& cx, float rv, i
   }
 }
 
+// Inserts `key` into a list of k keys kept largest first: each slot keeps
+// the larger of its key and the incoming one and passes the smaller on, so
+// after every insertion slot s holds the (s+1)-th largest key inserted.
+__device__ __forceinline__ void topk_insert(u64* slots, int k, u64 key) {
+  for (int s = 0; s < k && key != 0; ++s) {
+    const u64 old = atomicMax(slots + s, key);
+    if (old < key) key = old;
+  }
+}
+
+// A list's filter value: its k-th best (rounded down), at least the threshold.
+__device__ __forceinline__ float knn_floor(const uint64_t* list, int k, float thr,
+                                           const KeyLayout& kl) {
+  return fmaxf(key_corr_floor(list[k - 1], kl), thr);
+}
+
+// APPROX_ALL_NEIGHBORS counterpart of publish(): a cell above its row's
+// (column's) k-th best enters that window's list; the shared filter value
+// then follows the list's new k-th entry.
+__device__ __noinline__ void knn_publish(Smem& sm, const SlowCtx& cx, float rv, int64_t i,
+                                         int64_t j, int rslot, int cslot, int g) {
+  if (!(rv > cx.thr)) return;
+  const Problem& pr = *cx.pr;
+  const int k = cx.knn_k;
+  const float rb = g ? sm.r_best[rslot].y : sm.r_best[rslot].x;
+  const float cb = g ? sm.c_best[cslot].y : sm.c_best[cslot].x;
+  const uint64_t q = q_from_float_bits(__float_as_uint(rv), cx.kl.frac_bits);
+  if (rv > rb && pr.key_row) {
+    u64* list = reinterpret_cast<u64*>(pr.key_row + i * k);
+    topk_insert(list, k, make_key(q, j, cx.kl));
+    const float nb = knn_floor(pr.key_row + i * k, k, cx.thr, cx.kl);
+    if (g) sm.r_best[rslot].y = nb; else sm.r_best[rslot].x = nb;
+  }
+  if (rv > cb && pr.key_col) {
+    u64* list = reinterpret_cast<u64*>(pr.key_col + j * k);
+    topk_insert(list, k, make_key(q, i, cx.kl));
+    const float nb = knn_floor(pr.key_col + j * k, k, cx.thr, cx.kl);
+    if (g) sm.c_best[cslot].y = nb; else sm.c_best[cslot].x = nb;
+  }
+}
+
 // Exact path of queued blocks, 16 lanes per block: lane (k, g) rewinds the
 // covariance of diagonal k, segment g to the start of the block's first
 // step, then walks the block's rows (8 per step); every cell that may improve its row or column is
@@ -449,7 +491,9 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
         if (req) {
           ++nreq;
           if (slot < static_cast<unsigned long long>(cx.vcap)) {
-            if (!cx.sum_mode) publish(sm, cx, rv - mk, i, j, r0 + rr, rcs, g);
+            // (1NN: the lower bound raises the filters at once; a k-best
+            // list would keep it beside the verified value)
+            if (!cx.sum_mode && !cx.knn_k) publish(sm, cx, rv - mk, i, j, r0 + rr, rcs, g);
             VerifyReq q;
             q.i = static_cast<uint64_t>(i) | (static_cast<uint64_t>(cx.prob) << 40);
             q.d = static_cast<uint32_t>(j - i);
@@ -460,6 +504,7 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
             // enters the join's accuracy statement (a lane-serial direct dot
             // here would stall the warp for every such cell)
             if (cx.sum_mode) add = rv > cx.thr ? rv : 0.f;
+            else if (cx.knn_k) knn_publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
             else publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
             tmax = fmaxf(tmax, mk);
           }
@@ -467,7 +512,8 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
           add = rv > cx.thr ? rv : 0.f;
           if (add != 0.f) tmax = fmaxf(tmax, mk);
         } else {
-          publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
+          if (cx.knn_k) knn_publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
+          else publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
           tmax = fmaxf(tmax, mk);
         }
       }
@@ -654,15 +700,23 @@ __device__ __noinline__ void mat_cells_block(Smem& sm, const float2 (&cov_end)[k
 //          tight where the inverse norms of neighbouring windows are close
 //          (long windows); a block it flags goes to the exact path, which
 //          checks every cell with its own r.
-template <bool kSum, bool kCoarse, bool kMat = false>
+template <bool kSum, bool kCoarse, bool kMat = false, bool kKnn = false>
 __device__ __forceinline__ void band_body(const JoinParams& P) {
   static_assert(!(kMat && (kSum || kCoarse)), "the matrix form takes per-cell maxima");
+  static_assert(!(kKnn && (kSum || kCoarse || kMat)), "the k-best form is a 1NN variant");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
   const int t = threadIdx.x;
   const int lane = t & 31, warp = t >> 5;
   constexpr bool sum_mode = kSum;
   const float thr = static_cast<float>(P.threshold);
+  // a window's filter value: its best (1NN), or its list's k-th best, at
+  // least the threshold (k-best lists of kk keys per window)
+  const int kk = kKnn ? P.knn_k : 1;
+  auto best_floor = [&](const uint64_t* keys, int64_t w) -> float {
+    const float v = key_corr_floor(keys[w * kk + (kk - 1)], P.kl);
+    return kKnn ? fmaxf(v, thr) : v;
+  };
   unsigned long long n_steps = 0, n_slow = 0, n_verify = 0;
   int qn = 0;  // queued blocks of this warp (warp-uniform)
   float tfast = 0.f;  // SUM_THRESH: largest margin of a block added on the fast path
@@ -890,6 +944,7 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
       cx.tmargin = P.counters + 4;
       cx.sum_mode = kSum;
       cx.thr = static_cast<float>(P.threshold);
+      cx.knn_k = kKnn ? P.knn_k : 0;
       if constexpr (kMat) {
         cx.mat = P.mat;
         cx.mat_w = P.mat_w;
@@ -930,8 +985,8 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
         for (int c = t; c < kCols - kSlab; c += kThreads) {
           const int rc = ringc(ring0, c);
           float2 cb = sm.c_best[rc];
-          if (cb.x != kNoTarget) cb.x = fmaxf(cb.x, key_corr_floor(pr.key_col[cbase_g[0] + c], P.kl));
-          if (cb.y != kNoTarget) cb.y = fmaxf(cb.y, key_corr_floor(pr.key_col[cbase_g[1] + c], P.kl));
+          if (cb.x != kNoTarget) cb.x = fmaxf(cb.x, best_floor(pr.key_col, cbase_g[0] + c));
+          if (cb.y != kNoTarget) cb.y = fmaxf(cb.y, best_floor(pr.key_col, cbase_g[1] + c));
           sm.c_best[rc] = cb;
           float2 mn = cb;
 #pragma unroll
@@ -972,8 +1027,8 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
           }
           cbv = make_float2(0.f, 0.f);
         } else {
-          cbv.x = (pr.key_col && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_col[j0], P.kl) : kNoTarget;
-          cbv.y = (pr.key_col && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_col[j1], P.kl) : kNoTarget;
+          cbv.x = (pr.key_col && ok0 && !isnan(iv.x)) ? best_floor(pr.key_col, j0) : kNoTarget;
+          cbv.y = (pr.key_col && ok1 && !isnan(iv.y)) ? best_floor(pr.key_col, j1) : kNoTarget;
         }
         sm.u.s.c_df[padc(rc)] = make_float2(f.x, f.y);
         sm.u.s.c_dg[padc(rc)] = make_float2(f.z, f.w);
@@ -1012,8 +1067,8 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
         if (sum_mode) {
           rbv = make_float2(0.f, 0.f);
         } else {
-          rbv.x = (pr.key_row && ok0 && !isnan(iv.x)) ? key_corr_floor(pr.key_row[i0], P.kl) : kNoTarget;
-          rbv.y = (pr.key_row && ok1 && !isnan(iv.y)) ? key_corr_floor(pr.key_row[i1], P.kl) : kNoTarget;
+          rbv.x = (pr.key_row && ok0 && !isnan(iv.x)) ? best_floor(pr.key_row, i0) : kNoTarget;
+          rbv.y = (pr.key_row && ok1 && !isnan(iv.y)) ? best_floor(pr.key_row, i1) : kNoTarget;
         }
         sm.r_fg[r] = f;
         sm.r_iv[r] = iv;
@@ -1355,6 +1410,10 @@ __global__ void __launch_bounds__(kThreads, 4) join_mixed_mat_kernel(JoinParams 
   band_body<false, false, true>(P);
 }
 
+__global__ void __launch_bounds__(kThreads, 4) join_mixed_knn_kernel(JoinParams P) {
+  band_body<false, false, false, true>(P);
+}
+
 __global__ void __launch_bounds__(kThreads, 4) join_mixed_1nn_coarse_kernel(JoinParams P) {
   band_body<false, true>(P);
 }
@@ -1389,6 +1448,25 @@ verify_requests_kernel(JoinParams P) {
       if (lane == 0 && rv > static_cast<float>(P.threshold)) {
         if (pr.sum_row) atomicAdd(pr.sum_row + i, static_cast<double>(rv));
         if (pr.sum_col) atomicAdd(pr.sum_col + j, static_cast<double>(rv));
+      }
+      continue;
+    }
+    if (P.knn_k > 0) {  // APPROX_ALL_NEIGHBORS: into the k-best lists
+      const int k = P.knn_k;
+      const float thr = static_cast<float>(P.threshold);
+      const bool ro = pr.key_row && rq.ub > knn_floor(pr.key_row + i * k, k, thr, P.kl);
+      const bool co = pr.key_col && rq.ub > knn_floor(pr.key_col + j * k, k, thr, P.kl);
+      if (!ro && !co) continue;
+      const float cv = verify_cov_warp(pr.R, pr.C, i, j, pr.m, lane);
+      if (lane == 0) {
+        const float rv = (cv * pr.C.inv32[j]) * pr.R.inv32[i];
+        if (rv > thr) {
+          const uint64_t q = q_from_float_bits(__float_as_uint(rv), P.kl.frac_bits);
+          if (ro && rv > knn_floor(pr.key_row + i * k, k, thr, P.kl))
+            topk_insert(reinterpret_cast<u64*>(pr.key_row + i * k), k, make_key(q, j, P.kl));
+          if (co && rv > knn_floor(pr.key_col + j * k, k, thr, P.kl))
+            topk_insert(reinterpret_cast<u64*>(pr.key_col + j * k), k, make_key(q, i, P.kl));
+        }
       }
       continue;
     }
