@@ -108,11 +108,6 @@ __device__ __forceinline__ float max3(float a, float b, float c) {
   asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
   return d;
 }
-__device__ __forceinline__ float min3(float a, float b, float c) {
-  float d;
-  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-  return d;
-}
 // PTX sqrt.approx.f32: an approximate square root (a few ulp); sqrt(0) = 0.
 __device__ __forceinline__ float sqrt_approx(float x) {
   float r;
@@ -417,33 +412,70 @@ __device__ __noinline__ void knn_publish(Smem& sm, const SlowCtx& cx, float rv, 
   }
 }
 
-// Exact path of queued blocks, 16 lanes per block: lane (k, g) rewinds the
-// covariance of diagonal k, segment g to the start of the block's first
-// step, then walks the block's rows (8 per step); every cell that may improve its row or column is
-// published with its FP32 value when its margin is within kTrust.  A cell
-// with a larger margin is published with the lower bound rv - margin (so the
-// filters rise at once) and appended to the verification requests, which
-// verify_requests_kernel settles after the join.  Two blocks per pass.
-// Returns the lane's number of requests.
+// One cell of the exact path: publish (or add) its FP32 value when that is
+// safe, else queue a verification request at `slot`.
+__device__ __forceinline__ void exact_cell(Smem& sm, const SlowCtx& cx, float rv, float mk,
+                                           bool cand, bool req, unsigned long long slot,
+                                           int64_t i, int64_t j, int rslot, int cslot, int g,
+                                           float& add, float& tmax, int& nreq) {
+  if (!cand) return;
+  if (req) {
+    ++nreq;
+    if (slot < static_cast<unsigned long long>(cx.vcap)) {
+      // (1NN: the lower bound raises the filters at once; a k-best list
+      // would keep it beside the verified value)
+      if (!cx.sum_mode && !cx.knn_k) publish(sm, cx, rv - mk, i, j, rslot, cslot, g);
+      VerifyReq q;
+      q.i = static_cast<uint64_t>(i) | (static_cast<uint64_t>(cx.prob) << 40);
+      q.d = static_cast<uint32_t>(j - i);
+      q.ub = rv + mk;
+      cx.vreq[slot] = q;
+    } else {
+      // request buffer full: the FP32 value decides, and its margin enters
+      // the join's accuracy statement (a lane-serial direct dot here would
+      // stall the warp for every such cell)
+      if (cx.sum_mode) add = rv > cx.thr ? rv : 0.f;
+      else if (cx.knn_k) knn_publish(sm, cx, rv, i, j, rslot, cslot, g);
+      else publish(sm, cx, rv, i, j, rslot, cslot, g);
+      tmax = fmaxf(tmax, mk);
+    }
+  } else if (cx.sum_mode) {
+    add = rv > cx.thr ? rv : 0.f;
+    if (add != 0.f) tmax = fmaxf(tmax, mk);
+  } else {
+    if (cx.knn_k) knn_publish(sm, cx, rv, i, j, rslot, cslot, g);
+    else publish(sm, cx, rv, i, j, rslot, cslot, g);
+    tmax = fmaxf(tmax, mk);
+  }
+}
+
+// Exact path of queued blocks, 8 lanes per block (four blocks per pass):
+// lane k rewinds the covariances of diagonal k in both segments (an f32x2
+// pair, as the fast path holds them) to the start of the block's first step,
+// then walks the block's rows (8 per step); every cell that may improve its
+// row or column is published with its FP32 value when its margin is within
+// kTrust.  A cell with a larger margin is published with the lower bound
+// rv - margin (so the filters rise at once) and appended to the
+// verification requests, which verify_requests_kernel settles after the
+// join.  Returns the lane's number of requests.
 __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane) {
   __syncwarp();  // the queue was written by other lanes
   const SlowCtx& cx = sm.cx;
-  const Problem& pr = *cx.pr;
-  const int k = (lane & 15) >> 1, g = lane & 1;
+  const int k = lane & 7;
   int nreq = 0;
   float tmax = 0.f;  // largest margin of a value published or added unverified
-  for (int p = 0; p < count; p += 2) {
+  for (int p = 0; p < count; p += 4) {
     // every lane runs the pass (warp-wide request reservation); a lane
     // without a block carries the first queued one and checks nothing
-    const int item = p + (lane >> 4);
+    const int item = p + (lane >> 3);
     const bool act = item < count;
     const SlowItem& it = sm.queue[warp][act ? item : 0];
-    float c = g ? it.cov[k].y : it.cov[k].x;
-    const float vw = g ? it.vw.y : it.vw.x;
+    float2 c = it.cov[k];
+    const float2 vw = it.vw;
     const int s0 = it.s & 255;
     const int nrows = act ? kRows * (it.s >> 8) : 0;
-    // the two blocks of a pass may differ in length: the row loop below runs
-    // the longer length on every lane (its ballot needs the whole warp)
+    // the blocks of a pass may differ in length: the row loop below runs
+    // the longest on every lane (its ballots need the whole warp)
     const int nrows_w = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(nrows)));
     const int r0 = s0 * kRows;
     const int cb0 = 8 * (s0 + it.owner) + k;  // staged column at row 0
@@ -451,12 +483,12 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
     for (int rr = nrows - 1; rr >= 0; --rr) {
       const float4 rf = sm.r_fg[r0 + rr];
       const float4 cf = col_fg(sm, padc(ringc(cx.ring0, cb0 + rr)));
-      const float dfr = g ? rf.y : rf.x, dgr = g ? rf.w : rf.z;
-      const float dfc = g ? cf.y : cf.x, dgc = g ? cf.w : cf.z;
-      c = fmaf(-dfr, dgc, c);
-      c = fmaf(-dfc, dgr, c);
+      c = fma2(make_float2(-rf.x, -rf.y), make_float2(cf.z, cf.w), c);
+      c = fma2(make_float2(-cf.x, -cf.y), make_float2(rf.z, rf.w), c);
     }
-    const float vk = kBoundC * kEps * sqrtf(kRows * vw);
+    const float2 vk = make_float2(kBoundC * kEps * sqrtf(kRows * vw.x),
+                                  kBoundC * kEps * sqrtf(kRows * vw.y));
+    const int64_t jd = cx.D0 + it.owner * kDiags + k;  // the lane's diagonal
 #pragma unroll 1
     for (int rw = 0; rw < nrows_w; ++rw) {
       const bool live = rw < nrows;
@@ -465,72 +497,56 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
       const int rcs = ringc(cx.ring0, cs);  // its ring column
       const float4 rf = sm.r_fg[r0 + rr];
       const float4 cf = col_fg(sm, padc(rcs));
-      const float2 ivr2 = sm.r_iv[r0 + rr];
-      const float2 ivc2 = sm.u.s.c_iv[padc(rcs)];
-      const float ivr = g ? ivr2.y : ivr2.x, ivc = g ? ivc2.y : ivc2.x;
-      const float rv = (c * ivc) * ivr;  // the fast path's rounding
-      const float mk = vk * ivc * ivr;
-      const float rb = g ? sm.r_best[r0 + rr].y : sm.r_best[r0 + rr].x;
-      const float cbv = g ? sm.c_best[rcs].y : sm.c_best[rcs].x;
+      const float2 ivr = sm.r_iv[r0 + rr];
+      const float2 ivc = sm.u.s.c_iv[padc(rcs)];
+      const float2 rv = mul2(mul2(c, ivc), ivr);  // the fast path's rounding
+      const float2 mk = mul2(mul2(vk, ivc), ivr);
+      const float2 rb = sm.r_best[r0 + rr];
+      const float2 cbv = sm.c_best[rcs];
       // the value to beat: the row's and column's bests, or the threshold
-      const float tgt = cx.sum_mode ? cx.thr : fminf(rb, cbv);
-      const bool cand = live && rv + mk > tgt;
+      const float tx = cx.sum_mode ? cx.thr : fminf(rb.x, cbv.x);
+      const float ty = cx.sum_mode ? cx.thr : fminf(rb.y, cbv.y);
+      const bool cx_ = live && rv.x + mk.x > tx;
+      const bool cy_ = live && rv.y + mk.y > ty;
       // SUM_THRESH: a cell surely above the threshold counts with its FP32 r
-      const bool req = cand && mk > kTrust && !(cx.sum_mode && rv - mk > tgt);
-      const unsigned rmask = __ballot_sync(0xffffffffu, req);
-      unsigned long long slot = 0;
-      if (rmask) {
-        const int leader = __ffs(rmask) - 1;
-        if (lane == leader) slot = atomicAdd(cx.vcount, static_cast<unsigned long long>(__popc(rmask)));
-        slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(rmask & ((1u << lane) - 1u));
+      const bool qx = cx_ && mk.x > kTrust && !(cx.sum_mode && rv.x - mk.x > tx);
+      const bool qy = cy_ && mk.y > kTrust && !(cx.sum_mode && rv.y - mk.y > ty);
+      const unsigned mx = __ballot_sync(0xffffffffu, qx), my = __ballot_sync(0xffffffffu, qy);
+      unsigned long long sx = 0, sy = 0;
+      if (mx | my) {
+        const int leader = __ffs(mx | my) - 1;
+        unsigned long long base = 0;
+        if (lane == leader)
+          base = atomicAdd(cx.vcount, static_cast<unsigned long long>(__popc(mx) + __popc(my)));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        const unsigned lt = (1u << lane) - 1u;
+        sx = base + __popc(mx & lt) + __popc(my & lt);
+        sy = sx + (qx ? 1u : 0u);
       }
-      float add = 0.f;  // SUM_THRESH: what the cell adds to its row and column
-      if (cand) {
-        const int64_t i = cx.rbase[g] + r0 + rr;
-        const int64_t j = i + cx.D0 + it.owner * kDiags + k;
-        if (req) {
-          ++nreq;
-          if (slot < static_cast<unsigned long long>(cx.vcap)) {
-            // (1NN: the lower bound raises the filters at once; a k-best
-            // list would keep it beside the verified value)
-            if (!cx.sum_mode && !cx.knn_k) publish(sm, cx, rv - mk, i, j, r0 + rr, rcs, g);
-            VerifyReq q;
-            q.i = static_cast<uint64_t>(i) | (static_cast<uint64_t>(cx.prob) << 40);
-            q.d = static_cast<uint32_t>(j - i);
-            q.ub = rv + mk;
-            cx.vreq[slot] = q;
-          } else {
-            // request buffer full: the FP32 value decides, and its margin
-            // enters the join's accuracy statement (a lane-serial direct dot
-            // here would stall the warp for every such cell)
-            if (cx.sum_mode) add = rv > cx.thr ? rv : 0.f;
-            else if (cx.knn_k) knn_publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
-            else publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
-            tmax = fmaxf(tmax, mk);
-          }
-        } else if (cx.sum_mode) {
-          add = rv > cx.thr ? rv : 0.f;
-          if (add != 0.f) tmax = fmaxf(tmax, mk);
-        } else {
-          if (cx.knn_k) knn_publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
-          else publish(sm, cx, rv, i, j, r0 + rr, rcs, g);
-          tmax = fmaxf(tmax, mk);
-        }
+      float ax = 0.f, ay = 0.f;  // SUM_THRESH: what the cells add to their rows and column
+      if (cx_ || cy_) {
+        const int64_t i0 = cx.rbase[0] + r0 + rr, i1 = cx.rbase[1] + r0 + rr;
+        exact_cell(sm, cx, rv.x, mk.x, cx_, qx, sx, i0, i0 + jd, r0 + rr, rcs, 0, ax, tmax, nreq);
+        exact_cell(sm, cx, rv.y, mk.y, cy_, qy, sy, i1, i1 + jd, r0 + rr, rcs, 1, ay, tmax, nreq);
       }
       if (cx.sum_mode) {
-        // the 8 diagonals of a block meet in one row: reduce over lanes
-        // (k = lane bits 1-3) before the shared-memory atomic
-        if (add != 0.f) atomicAdd(g ? &sm.c_best[rcs].y : &sm.c_best[rcs].x, add);
-        float rs = add;
-        rs += __shfl_xor_sync(0xffffffffu, rs, 2);
-        rs += __shfl_xor_sync(0xffffffffu, rs, 4);
-        rs += __shfl_xor_sync(0xffffffffu, rs, 8);
-        if (k == 0 && rs != 0.f) atomicAdd(g ? &sm.r_best[r0 + rr].y : &sm.r_best[r0 + rr].x, rs);
+        // the 8 diagonals of a block meet in one row: reduce over its lanes
+        // (k = lane bits 0-2) before the shared-memory atomics
+        if (ax != 0.f) atomicAdd(&sm.c_best[rcs].x, ax);
+        if (ay != 0.f) atomicAdd(&sm.c_best[rcs].y, ay);
+        float2 rs = make_float2(ax, ay);
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+          rs.x += __shfl_xor_sync(0xffffffffu, rs.x, o);
+          rs.y += __shfl_xor_sync(0xffffffffu, rs.y, o);
+        }
+        if (k == 0) {
+          if (rs.x != 0.f) atomicAdd(&sm.r_best[r0 + rr].x, rs.x);
+          if (rs.y != 0.f) atomicAdd(&sm.r_best[r0 + rr].y, rs.y);
+        }
       }
-      const float dfr = g ? rf.y : rf.x, dgr = g ? rf.w : rf.z;
-      const float dfc = g ? cf.y : cf.x, dgc = g ? cf.w : cf.z;
-      c = fmaf(dfc, dgr, c);
-      c = fmaf(dfr, dgc, c);
+      c = fma2(make_float2(cf.x, cf.y), make_float2(rf.z, rf.w), c);
+      c = fma2(make_float2(rf.x, rf.y), make_float2(cf.z, cf.w), c);
     }
   }
   // the trusted margins, one atomic per drain (non-negative floats order as
@@ -542,31 +558,107 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
   return nreq;
 }
 
-// SUM_THRESH fast path of one thread-step whose cells all lie above the
-// threshold by more than the step's margin (fx, fy per segment): the block
-// is rewound from the covariances at the step's end (as the exact path
-// rewinds) and walked again; every valid cell adds its FP32 r to its row's
-// and its column's slab sums.  Rows are reduced over the warp (every lane
-// calls this, adding nothing where its flags are off), columns over
-// neighbouring threads: thread t's columns 8..14 are thread t + 1's 0..6.
-__device__ __noinline__ void fast_add_block(Smem& sm, const float2 (&cov_end)[kDiags], int s,
-                                            int t, int lane, bool fx, bool fy) {
-  const SlowCtx& cx = sm.cx;
-  const int r0 = s * kRows;
-  const int cb0 = 8 * (s + t);  // slab-relative column of (row 0, diagonal 0)
-  float2 c[kDiags];
-#pragma unroll
-  for (int k = 0; k < kDiags; ++k) c[k] = cov_end[k];
+// Rewinds a thread-step's covariances from their values at its end to its
+// first row (the exact path's rewind).
+__device__ __forceinline__ void rewind_block(const Smem& sm, float2 (&c)[kDiags], int r0, int cb0) {
 #pragma unroll 1
   for (int rr = kRows - 1; rr >= 0; --rr) {
     const float4 rf = sm.r_fg[r0 + rr];
 #pragma unroll
     for (int k = 0; k < kDiags; ++k) {
-      const float4 cf = col_fg(sm, padc(ringc(cx.ring0, cb0 + rr + k)));
+      const float4 cf = col_fg(sm, padc(ringc(sm.cx.ring0, cb0 + rr + k)));
       c[k] = fma2(make_float2(-rf.x, -rf.y), make_float2(cf.z, cf.w), c[k]);
       c[k] = fma2(make_float2(-cf.x, -cf.y), make_float2(rf.z, rf.w), c[k]);
     }
   }
+}
+
+// SUM_THRESH: the cells of a thread-step that lie within the step's margin m
+// of the threshold (bit 8 rr + k of ux / uy per segment; rare), walked again
+// by their lane alone: decided by the FP32 r when m is within kTrust, else
+// requested for verification (a full request buffer lets the FP32 r decide,
+// its margin stated with the join's accuracy).  Adds go straight to the
+// slab's shared-memory sums.  Returns the lane's number of requests.
+__device__ __noinline__ int sum_uncertain(Smem& sm, const float2 (&cov_end)[kDiags], int s, int t,
+                                          uint64_t ux, uint64_t uy, float2 mstep) {
+  const SlowCtx& cx = sm.cx;
+  const int r0 = s * kRows;
+  const int cb0 = 8 * (s + t);
+  float2 c[kDiags];
+#pragma unroll
+  for (int k = 0; k < kDiags; ++k) c[k] = cov_end[k];
+  rewind_block(sm, c, r0, cb0);
+  int nreq = 0;
+#pragma unroll 1
+  for (int rr = 0; rr < kRows; ++rr) {
+    const float4 rf = sm.r_fg[r0 + rr];
+    const float2 ivr = sm.r_iv[r0 + rr];
+#pragma unroll
+    for (int k = 0; k < kDiags; ++k) {
+      const int rcx = ringc(cx.ring0, cb0 + rr + k);
+      const int slot = padc(rcx);
+      const int bit = rr * kDiags + k;
+      if (((ux | uy) >> bit) & 1) {
+        const float2 r2 = mul2(mul2(c[k], sm.u.s.c_iv[slot]), ivr);
+#pragma unroll 1
+        for (int g = 0; g < 2; ++g) {
+          if (!(((g ? uy : ux) >> bit) & 1)) continue;
+          const float r = g ? r2.y : r2.x;
+          const float m = g ? mstep.y : mstep.x;
+          bool add = false;
+          if (m <= kTrust) {
+            add = r > cx.thr;
+          } else {
+            const int64_t i = cx.rbase[g] + r0 + rr;
+            const int64_t j = i + cx.D0 + t * kDiags + k;
+            const unsigned long long sl = atomicAdd(cx.vcount, 1ull);
+            ++nreq;
+            if (sl < static_cast<unsigned long long>(cx.vcap)) {
+              VerifyReq q;
+              q.i = static_cast<uint64_t>(i) | (static_cast<uint64_t>(cx.prob) << 40);
+              q.d = static_cast<uint32_t>(j - i);
+              q.ub = r + m;
+              cx.vreq[sl] = q;
+            } else if (r > cx.thr) {
+              add = true;
+              atomicMax(cx.tmargin, static_cast<unsigned long long>(__float_as_uint(m)));
+            }
+          }
+          if (add) {
+            atomicAdd(g ? &sm.r_best[r0 + rr].y : &sm.r_best[r0 + rr].x, r);
+            atomicAdd(g ? &sm.c_best[rcx].y : &sm.c_best[rcx].x, r);
+          }
+        }
+      }
+      const float4 cf = col_fg(sm, slot);
+      c[k] = fma2(make_float2(cf.x, cf.y), make_float2(rf.z, rf.w), c[k]);
+      c[k] = fma2(make_float2(rf.x, rf.y), make_float2(cf.z, cf.w), c[k]);
+    }
+  }
+  return nreq;
+}
+
+// SUM_THRESH, per-cell path of one thread-step that may hold cells above the
+// threshold (flags fx, fy per segment; every lane calls it, adding nothing
+// where its flags are off): the block is rewound from the covariances at
+// the step's end (as the exact path rewinds) and walked again.  A cell above
+// the threshold by more than the step's margin m (per segment) adds its FP32
+// r; cells within m of it go to sum_uncertain.  Rows are reduced over the
+// warp, columns over neighbouring threads (thread t's columns 8..14 are
+// thread t + 1's 0..6) before the shared-memory atomics.  Returns the lane's
+// number of verification requests.
+__device__ __noinline__ int sum_block(Smem& sm, const float2 (&cov_end)[kDiags], int s, int t,
+                                      int lane, bool fx, bool fy, float2 mstep) {
+  const SlowCtx& cx = sm.cx;
+  const int r0 = s * kRows;
+  const int cb0 = 8 * (s + t);  // slab-relative column of (row 0, diagonal 0)
+  const float2 hi = make_float2(cx.thr + mstep.x, cx.thr + mstep.y);
+  const float2 lo = make_float2(cx.thr - mstep.x, cx.thr - mstep.y);
+  float2 c[kDiags];
+#pragma unroll
+  for (int k = 0; k < kDiags; ++k) c[k] = cov_end[k];
+  rewind_block(sm, c, r0, cb0);
+  uint64_t ux = 0, uy = 0;  // cells within the margin of the threshold
   float2 cacc[15];
 #pragma unroll
   for (int x = 0; x < 15; ++x) cacc[x] = make_float2(0.f, 0.f);
@@ -580,8 +672,11 @@ __device__ __noinline__ void fast_add_block(Smem& sm, const float2 (&cov_end)[kD
     for (int k = 0; k < kDiags; ++k) {
       const int slot = padc(ringc(cx.ring0, cb0 + rr + k));
       const float2 r2 = mul2(mul2(c[k], sm.u.s.c_iv[slot]), ivr);
-      const float vx = (fx && r2.x == r2.x) ? r2.x : 0.f;  // NaN cells add nothing
-      const float vy = (fy && r2.y == r2.y) ? r2.y : 0.f;
+      // NaN cells compare false everywhere and add nothing
+      const float vx = (fx && r2.x > hi.x) ? r2.x : 0.f;
+      const float vy = (fy && r2.y > hi.y) ? r2.y : 0.f;
+      ux |= static_cast<uint64_t>(fx && r2.x > lo.x && !(r2.x > hi.x)) << (rr * kDiags + k);
+      uy |= static_cast<uint64_t>(fy && r2.y > lo.y && !(r2.y > hi.y)) << (rr * kDiags + k);
       rs.x += vx;
       rs.y += vy;
       cacc[rr + k].x += vx;
@@ -602,11 +697,11 @@ __device__ __noinline__ void fast_add_block(Smem& sm, const float2 (&cov_end)[kD
   }
 #pragma unroll
   for (int x = 0; x < 7; ++x) {
-    const float ux = __shfl_up_sync(0xffffffffu, cacc[8 + x].x, 1);
-    const float uy = __shfl_up_sync(0xffffffffu, cacc[8 + x].y, 1);
+    const float vx = __shfl_up_sync(0xffffffffu, cacc[8 + x].x, 1);
+    const float vy = __shfl_up_sync(0xffffffffu, cacc[8 + x].y, 1);
     if (lane > 0) {
-      cacc[x].x += ux;
-      cacc[x].y += uy;
+      cacc[x].x += vx;
+      cacc[x].y += vy;
     }
   }
 #pragma unroll
@@ -617,6 +712,7 @@ __device__ __noinline__ void fast_add_block(Smem& sm, const float2 (&cov_end)[kD
       if (cacc[x].y != 0.f) atomicAdd(&sm.c_best[rcx].y, cacc[x].y);
     }
   }
+  return (ux | uy) ? sum_uncertain(sm, cov_end, s, t, ux, uy, mstep) : 0;
 }
 
 // MATRIX_SUMMARY: a thread's running maxima (per segment and target).
@@ -1133,9 +1229,8 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
         const float2 tt = fma2(make_float2(-kStepMarginC, -kStepMarginC), mg, tb);
         const float tx = tt.x, ty = tt.y;
 
-        // fast path: recurrence + block maximum (SUM_THRESH: and minimum)
+        // fast path: recurrence + block maximum
         float bx = -3.f, by = -3.f;
-        float lx = 3.f, ly = 3.f;
         if constexpr (kCoarse) {
           // largest covariance of the block (NaN diagonals ignored), then
           // the bound max(cov, 0) * max inv_c * max inv_r of every r in it
@@ -1168,7 +1263,7 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
           bx = bnd.x;
           by = bnd.y;
         } else {
-          float2 rprev, lprev;
+          float2 rprev;
 #pragma unroll
           for (int rr = 0; rr < kRows; ++rr) {
             {
@@ -1182,17 +1277,12 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
             // the row's largest cov * inv_c, times inv_r (> 0): the largest r
             // of the row, rounded exactly as (cov * inv_c) * inv_r per cell
             float mx = -3.f, my = -3.f;
-            float nx = 3.f, ny = 3.f;  // SUM_THRESH: the row's smallest as well
 #pragma unroll
             for (int k = 0; k < kDiags; k += 2) {
               const float2 pa = mul2(cov[k], ciw[(8 * P + rr + k) & 15]);
               const float2 pb = mul2(cov[k + 1], ciw[(8 * P + rr + k + 1) & 15]);
               mx = max3(mx, pa.x, pb.x);
               my = max3(my, pa.y, pb.y);
-              if constexpr (kSum) {
-                nx = min3(nx, pa.x, pb.x);
-                ny = min3(ny, pa.y, pb.y);
-              }
             }
             const float2 rm = mul2(make_float2(mx, my), ivr);
             if (rr & 1) {
@@ -1200,15 +1290,6 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
               by = max3(by, rprev.y, rm.y);
             } else {
               rprev = rm;
-            }
-            if constexpr (kSum) {
-              const float2 rn = mul2(make_float2(nx, ny), ivr);
-              if (rr & 1) {
-                lx = min3(lx, lprev.x, rn.x);
-                ly = min3(ly, lprev.y, rn.y);
-              } else {
-                lprev = rn;
-              }
             }
 #pragma unroll
             for (int k = 0; k < kDiags; ++k) {
@@ -1267,22 +1348,17 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
           if (nonuni[0] || nonuni[1]) mat_cells_block(sm, cov, s, t, nonuni[0], nonuni[1]);
         }
         if constexpr (kSum && !kCoarse) {
-          // A segment whose every valid cell is above the threshold by more
-          // than the step's margin needs no exact path: each of its cells
-          // adds its FP32 r, as the exact path would add it (its per-cell
-          // margin is never larger).  The block is walked again from the
-          // step's start, the rows' sums reduced over the warp and the
-          // columns' sums over neighbouring threads (thread t's columns 8..14
-          // are thread t + 1's 0..6) before the shared-memory atomics.
-          const float2 ut = fma2(make_float2(kStepMarginC, kStepMarginC), mg, tb);
-          const bool ax = lx > ut.x && bx > tx, ay = ly > ut.y && by > ty;
-          trig = (bx > tx && !ax) || (by > ty && !ay);
-          const bool fx = ax && !trig, fy = ay && !trig;
+          // SUM_THRESH: a segment that may hold a cell above the threshold
+          // is decided cell by cell on the owner's warp (sum_block); the
+          // exact path is not needed.  Its FP32 values carry at most the
+          // step's margin.
+          trig = false;
+          const bool fx = bx > tx, fy = by > ty;
           if (__any_sync(0xffffffffu, fx || fy)) {
-            fast_add_block(sm, cov, s, t, lane, fx, fy);
             const float2 smg = mul2(make_float2(kStepMarginC, kStepMarginC), mg);
-            if (fx) tfast = fmaxf(tfast, smg.x);
-            if (fy) tfast = fmaxf(tfast, smg.y);
+            n_verify += sum_block(sm, cov, s, t, lane, fx, fy, smg);
+            if (fx && smg.x <= kTrust) tfast = fmaxf(tfast, smg.x);
+            if (fy && smg.y <= kTrust) tfast = fmaxf(tfast, smg.y);
           }
         }
         const unsigned tmask = __ballot_sync(0xffffffffu, trig);
