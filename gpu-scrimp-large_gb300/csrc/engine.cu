@@ -561,9 +561,8 @@ int tc_self_check(Workspace& ws, cudaStream_t st, std::string* msg, bool wait_te
 // Seeding pre-pass of the mixed 1NN join: when and how.  The block-averaged
 // join costs ~1/64 of the join's cells; below a few 1e9 cells it does not pay.
 constexpr float kSeedFloor = 0.8f;  // partners below it are not worth a seed
-// Smallest averaged window of a batch's pre-pass (shorter ones pair blocks
-// at random).
-constexpr int64_t kBatchSeedMinWindow = 8;
+// Shortest window seeded by the pre-pass (single joins and batches): below
+// it the averaged windows (< 16 samples) pair blocks almost at random.
 constexpr int64_t kSeedMinWindow = 64;
 
 // Block size of the pre-pass: the largest power of two <= m / 16 within
@@ -995,7 +994,10 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
     if (kind == K_MIXED) {
       // random-walk-like series ask for ~7 (K = 512) to ~18 (K = 1024)
       // 1NN requests per window
-      int64_t want = std::max<int64_t>(kMinVerifyReqs, 32 * (nsz[0] + nsz[1]));
+      // (k-best lists: a window keeps k candidates open, and cold lists
+      // ask for more)
+      int64_t want = std::max<int64_t>(kMinVerifyReqs, 32 * (nsz[0] + nsz[1]) *
+                                                           (knn_mixed ? 4 * knn_k : 1));
       want = std::max<int64_t>(want, ws.vreq_seen + ws.vreq_seen / 4);
       want = std::max<int64_t>(std::min<int64_t>(want, kMaxVerifyReqs), ws.vreq_cap);
       void* q;
@@ -1225,14 +1227,16 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
 // (SCAMP_ERR_DEVICE_TIMEOUT when a bounded wait on the device gave up).
 int read_times(Workspace& ws, scamp_c_result* res, std::string* msg = nullptr) {
   res->steps = res->slow_steps = res->verifications = 0;
+  res->inplace_verifications = 0;
   int status = SCAMP_OK;
   if (ws.timed_kernel && ws.bufs.size() > S_COUNTER && ws.bufs[S_COUNTER].p) {
-    unsigned long long c[7] = {0, 0, 0, 0, 0, 0, 0};
+    unsigned long long c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (cudaMemcpy(c, ws.bufs[S_COUNTER].p, sizeof(c), cudaMemcpyDeviceToHost) == cudaSuccess) {
       res->steps = c[1];
       res->slow_steps = c[2];
       res->verifications = c[3];
-      ws.vreq_seen = std::max<int64_t>(ws.vreq_seen, static_cast<int64_t>(c[4]));
+      res->inplace_verifications = static_cast<uint32_t>(std::min<unsigned long long>(c[7], UINT32_MAX));
+      ws.vreq_seen = std::max<int64_t>(ws.vreq_seen, static_cast<int64_t>(c[4] + c[7]));
       float tm;
       const uint32_t bits = static_cast<uint32_t>(c[5]);
       std::memcpy(&tm, &bits, 4);
@@ -2057,7 +2061,7 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
       const int f = seed_factor(b.m);
       const int64_t n2 = b.n / f, m2 = b.m / f;
       const int64_t ns2 = n2 - m2 + 1, excl2 = m2 / 4;
-      if (m2 >= kBatchSeedMinWindow && ns2 > excl2 && diag_cells(ns2, ns2, excl2, ns2) > 0) {
+      if (b.m >= kSeedMinWindow && ns2 > excl2 && diag_cells(ns2, ns2, excl2, ns2) > 0) {
         b.f = f;
         b.n2 = n2;
         b.m2 = m2;
@@ -2416,12 +2420,13 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   read_times(ws, &tot);
   if (!probs.empty()) {
     // the batch's work counters live in its arena, not in the join counters
-    unsigned long long c[6] = {0, 0, 0, 0, 0, 0};
+    unsigned long long c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (cudaMemcpy(c, d_counter, sizeof(c), cudaMemcpyDeviceToHost) == cudaSuccess) {
       tot.steps = c[1];
       tot.slow_steps = c[2];
       tot.verifications = c[3];
-      ws.vreq_seen = std::max<int64_t>(ws.vreq_seen, static_cast<int64_t>(c[4]));
+      tot.inplace_verifications = static_cast<uint32_t>(std::min<unsigned long long>(c[7], UINT32_MAX));
+      ws.vreq_seen = std::max<int64_t>(ws.vreq_seen, static_cast<int64_t>(c[4] + c[7]));
       const uint32_t bits = static_cast<uint32_t>(c[5]);
       float tm;
       std::memcpy(&tm, &bits, 4);
@@ -2437,6 +2442,7 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     res[k].steps = tot.steps;
     res[k].slow_steps = tot.slow_steps;
     res[k].verifications = tot.verifications;
+    res[k].inplace_verifications = tot.inplace_verifications;
     res[k].max_abs_r_err = final_eval_bound(ser[k].m, kl.frac_bits);
     res[k].max_tie_margin = tot.max_tie_margin;
   }

@@ -152,7 +152,8 @@ struct JoinParams {
   int64_t total_units;
   unsigned long long* unit_counter; // persistent work queue head
   // [steps, slow steps, verifications, requests, largest trusted margin
-  // (float bits, mixed form)]
+  // (float bits, mixed form), (error word), candidates verified in place
+  // because the request buffer was full]
   unsigned long long* counters;
   VerifyReq* vreq;                  // verification requests (mixed 1NN)
   int64_t vreq_cap;

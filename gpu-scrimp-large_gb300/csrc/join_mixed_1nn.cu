@@ -167,6 +167,7 @@ struct SlowCtx {
   unsigned long long* vcount;      // their count (may exceed vcap)
   int64_t vcap;
   unsigned long long* tmargin;     // largest drift margin of a trusted FP32 value (float bits)
+  unsigned long long* overflow;    // candidates verified in place (request buffer full)
   // MATRIX_SUMMARY: the grid and its geometry (JoinParams), the current
   // problem's targets
   int knn_k;  // APPROX_ALL_NEIGHBORS: list length (0 otherwise)
@@ -431,13 +432,14 @@ __device__ __forceinline__ void exact_cell(Smem& sm, const SlowCtx& cx, float rv
       q.ub = rv + mk;
       cx.vreq[slot] = q;
     } else {
-      // request buffer full: the FP32 value decides, and its margin enters
-      // the join's accuracy statement (a lane-serial direct dot here would
-      // stall the warp for every such cell)
-      if (cx.sum_mode) add = rv > cx.thr ? rv : 0.f;
-      else if (cx.knn_k) knn_publish(sm, cx, rv, i, j, rslot, cslot, g);
-      else publish(sm, cx, rv, i, j, rslot, cslot, g);
-      tmax = fmaxf(tmax, mk);
+      // request buffer full: verified in place by this lane (slow: the
+      // counted overflow makes later joins size the buffer for it)
+      const Problem& pr = *cx.pr;
+      const float ev = (verify_cov_lane(pr.R, pr.C, i, j, cx.m) * pr.C.inv32[j]) * pr.R.inv32[i];
+      atomicAdd(cx.overflow, 1ull);
+      if (cx.sum_mode) add = ev > cx.thr ? ev : 0.f;
+      else if (cx.knn_k) knn_publish(sm, cx, ev, i, j, rslot, cslot, g);
+      else publish(sm, cx, ev, i, j, rslot, cslot, g);
     }
   } else if (cx.sum_mode) {
     add = rv > cx.thr ? rv : 0.f;
@@ -603,7 +605,7 @@ __device__ __noinline__ int sum_uncertain(Smem& sm, const float2 (&cov_end)[kDia
 #pragma unroll 1
         for (int g = 0; g < 2; ++g) {
           if (!(((g ? uy : ux) >> bit) & 1)) continue;
-          const float r = g ? r2.y : r2.x;
+          float r = g ? r2.y : r2.x;
           const float m = g ? mstep.y : mstep.x;
           bool add = false;
           if (m <= kTrust) {
@@ -619,9 +621,14 @@ __device__ __noinline__ int sum_uncertain(Smem& sm, const float2 (&cov_end)[kDia
               q.d = static_cast<uint32_t>(j - i);
               q.ub = r + m;
               cx.vreq[sl] = q;
-            } else if (r > cx.thr) {
-              add = true;
-              atomicMax(cx.tmargin, static_cast<unsigned long long>(__float_as_uint(m)));
+            } else {
+              // request buffer full: verified in place (counted)
+              const Problem& pr = *cx.pr;
+              const float ev =
+                  (verify_cov_lane(pr.R, pr.C, i, j, cx.m) * pr.C.inv32[j]) * pr.R.inv32[i];
+              atomicAdd(cx.overflow, 1ull);
+              add = ev > cx.thr;
+              r = ev;
             }
           }
           if (add) {
@@ -1038,6 +1045,7 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
       cx.vcount = P.counters + 3;
       cx.vcap = P.vreq_cap;
       cx.tmargin = P.counters + 4;
+      cx.overflow = P.counters + 6;
       cx.sum_mode = kSum;
       cx.thr = static_cast<float>(P.threshold);
       cx.knn_k = kKnn ? P.knn_k : 0;

@@ -256,6 +256,7 @@ def join(a, b=None, m=None, profile="1NN_INDEX", precision="double",
     out["gpu_launches"] = int(res.gpu_launches)
     out["counters"] = {"steps": int(res.steps), "slow_steps": int(res.slow_steps),
                        "verifications": int(res.verifications),
+                       "inplace_verifications": int(res.inplace_verifications),
                        "verify_kernel_ms": float(res.verify_kernel_ms)}
     out["max_abs_r_err"] = float(res.max_abs_r_err)
     out["max_tie_margin"] = float(res.max_tie_margin)
@@ -300,6 +301,7 @@ def join_device(a_ptr, len_a, m, b_ptr=None, len_b=0, profile="1NN_INDEX",
     return {"elapsed_ms": res.elapsed_ms, "join_kernel_ms": res.join_kernel_ms,
             "counters": {"steps": int(res.steps), "slow_steps": int(res.slow_steps),
                          "verifications": int(res.verifications),
+                       "inplace_verifications": int(res.inplace_verifications),
                          "verify_kernel_ms": float(res.verify_kernel_ms)},
             "comparisons": int(res.comparisons),
             "gpu_launches": int(res.gpu_launches),
@@ -373,6 +375,7 @@ def join_batch(series, windows, precision="mixed", return_corr=False, device=0,
              "gpu_launches": int(cres[k].gpu_launches),
              "counters": {"steps": int(cres[k].steps), "slow_steps": int(cres[k].slow_steps),
                           "verifications": int(cres[k].verifications),
+                          "inplace_verifications": int(cres[k].inplace_verifications),
                           "verify_kernel_ms": float(cres[k].verify_kernel_ms)},
              "max_abs_r_err": float(cres[k].max_abs_r_err),
              "max_tie_margin": float(cres[k].max_tie_margin)}

@@ -96,7 +96,7 @@ class CResult(ctypes.Structure):
         ("join_kernel_ms", ctypes.c_double),
         ("comparisons", ctypes.c_uint64),
         ("gpu_launches", ctypes.c_uint32),
-        ("reserved0", ctypes.c_uint32),
+        ("inplace_verifications", ctypes.c_uint32),
         ("steps", ctypes.c_uint64),
         ("slow_steps", ctypes.c_uint64),
         ("verifications", ctypes.c_uint64),

@@ -115,7 +115,10 @@ typedef struct scamp_c_result {
                          * verification of deferred candidates) */
   uint64_t comparisons; /* distance-matrix cells evaluated */
   uint32_t gpu_launches;/* kernels launched by this call */
-  uint32_t reserved0;
+  uint32_t inplace_verifications; /* mixed forms: candidate cells verified by
+                         * a direct dot product inside the band kernel because
+                         * the request buffer was full (slow; the next join on
+                         * the device sizes the buffer for them); saturates */
   /* Work counters of the mixed 1NN_INDEX form (0 otherwise): 8-row steps
    * of one thread, steps recomputed on the exact path, and candidate cells
    * sent to verification by a direct dot product. */

@@ -162,9 +162,9 @@ def test_matrix_summary(gpu_engine, precision):
     C[jj - ii < m // 4] = np.nan
     check_matrix(r["matrix"].astype(np.float64), C, 20, 30, 0.2, tol)
     if precision == "mixed":
-        # the band kernel's form (grid entries of >= 64 windows each), with
-        # its error statement
-        assert 0 <= r["max_abs_r_err"] <= TOL_MIXED
+        # the band kernel's form (grid entries of >= 64 windows each) states
+        # its bound: the largest drift margin of a published maximum
+        assert 0 < r["max_abs_r_err"] < 1e-3
     # AB-join: every (window of b, window of a) cell
     r = gpu_engine.join(a, b, m, "MATRIX_SUMMARY", precision, computing_rows=False,
                         matrix_height=17, matrix_width=23)
@@ -202,7 +202,8 @@ def test_matrix_summary_mixed_vs_fp64(gpu_engine, shape):
         # an entry on one side only lies at the threshold's edge
         assert np.all(fm[(fm >= -1) & (xm < -1)] <= 0.5 + TOL_MIXED)
         assert np.all(xm[(xm >= -1) & (fm < -1)] <= 0.5 + TOL_MIXED)
-        assert 0 < x["max_abs_r_err"] <= TOL_MIXED
+        # the stated bound covers the observed error
+        assert np.max(np.abs(fm[both] - xm[both]), initial=0.0) <= x["max_abs_r_err"] < 1e-3
 
 
 def test_matrix_merges_into_given_matrix(gpu_engine):
