@@ -146,7 +146,8 @@ __device__ __forceinline__ float key_corr_floor(u64 key, const KeyLayout& kl) {
 struct SlowItem {
   float2 cov[kDiags];  // covariances after the item's last step
   float2 vw;
-  int s;      // first step within the slab | number of steps (1 or 2) << 8
+  int s;      // first step within the slab | number of steps (1 or 2) << 8 |
+              // segments to walk << 16 (bits 0-1 first step, 2-3 second)
   int owner;  // thread index of the owner
 };
 
@@ -435,7 +436,9 @@ __device__ __forceinline__ void exact_cell(Smem& sm, const SlowCtx& cx, float rv
       // request buffer full: verified in place by this lane (slow: the
       // counted overflow makes later joins size the buffer for it)
       const Problem& pr = *cx.pr;
-      const float ev = (verify_cov_lane(pr.R, pr.C, i, j, cx.m) * pr.C.inv32[j]) * pr.R.inv32[i];
+      // (the dot inline: a call from here makes every band kernel that
+      // calls the exact path keep more registers live across it)
+      const float ev = (cov_part(pr.R, pr.C, i, j, 0, cx.m) * pr.C.inv32[j]) * pr.R.inv32[i];
       atomicAdd(cx.overflow, 1ull);
       if (cx.sum_mode) add = ev > cx.thr ? ev : 0.f;
       else if (cx.knn_k) knn_publish(sm, cx, ev, i, j, rslot, cslot, g);
@@ -475,7 +478,8 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
     float2 c = it.cov[k];
     const float2 vw = it.vw;
     const int s0 = it.s & 255;
-    const int nrows = act ? kRows * (it.s >> 8) : 0;
+    const int nrows = act ? kRows * ((it.s >> 8) & 255) : 0;
+    const int msk = (it.s >> 16) & 15;  // segments to walk, per step of the block
     // the blocks of a pass may differ in length: the row loop below runs
     // the longest on every lane (its ballots need the whole warp)
     const int nrows_w = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(nrows)));
@@ -508,8 +512,9 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
       // the value to beat: the row's and column's bests, or the threshold
       const float tx = cx.sum_mode ? cx.thr : fminf(rb.x, cbv.x);
       const float ty = cx.sum_mode ? cx.thr : fminf(rb.y, cbv.y);
-      const bool cx_ = live && rv.x + mk.x > tx;
-      const bool cy_ = live && rv.y + mk.y > ty;
+      const int sm2 = msk >> (2 * (rw >> 3));
+      const bool cx_ = live && (sm2 & 1) && rv.x + mk.x > tx;
+      const bool cy_ = live && (sm2 & 2) && rv.y + mk.y > ty;
       // SUM_THRESH: a cell surely above the threshold counts with its FP32 r
       const bool qx = cx_ && mk.x > kTrust && !(cx.sum_mode && rv.x - mk.x > tx);
       const bool qy = cy_ && mk.y > kTrust && !(cx.sum_mode && rv.y - mk.y > ty);
@@ -558,168 +563,6 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
   if (lane == 0 && tmax > 0.f) atomicMax(cx.tmargin, static_cast<unsigned long long>(__float_as_uint(tmax)));
   __syncwarp();
   return nreq;
-}
-
-// Rewinds a thread-step's covariances from their values at its end to its
-// first row (the exact path's rewind).
-__device__ __forceinline__ void rewind_block(const Smem& sm, float2 (&c)[kDiags], int r0, int cb0) {
-#pragma unroll 1
-  for (int rr = kRows - 1; rr >= 0; --rr) {
-    const float4 rf = sm.r_fg[r0 + rr];
-#pragma unroll
-    for (int k = 0; k < kDiags; ++k) {
-      const float4 cf = col_fg(sm, padc(ringc(sm.cx.ring0, cb0 + rr + k)));
-      c[k] = fma2(make_float2(-rf.x, -rf.y), make_float2(cf.z, cf.w), c[k]);
-      c[k] = fma2(make_float2(-cf.x, -cf.y), make_float2(rf.z, rf.w), c[k]);
-    }
-  }
-}
-
-// SUM_THRESH: the cells of a thread-step that lie within the step's margin m
-// of the threshold (bit 8 rr + k of ux / uy per segment; rare), walked again
-// by their lane alone: decided by the FP32 r when m is within kTrust, else
-// requested for verification (a full request buffer lets the FP32 r decide,
-// its margin stated with the join's accuracy).  Adds go straight to the
-// slab's shared-memory sums.  Returns the lane's number of requests.
-__device__ __noinline__ int sum_uncertain(Smem& sm, const float2 (&cov_end)[kDiags], int s, int t,
-                                          uint64_t ux, uint64_t uy, float2 mstep) {
-  const SlowCtx& cx = sm.cx;
-  const int r0 = s * kRows;
-  const int cb0 = 8 * (s + t);
-  float2 c[kDiags];
-#pragma unroll
-  for (int k = 0; k < kDiags; ++k) c[k] = cov_end[k];
-  rewind_block(sm, c, r0, cb0);
-  int nreq = 0;
-#pragma unroll 1
-  for (int rr = 0; rr < kRows; ++rr) {
-    const float4 rf = sm.r_fg[r0 + rr];
-    const float2 ivr = sm.r_iv[r0 + rr];
-#pragma unroll
-    for (int k = 0; k < kDiags; ++k) {
-      const int rcx = ringc(cx.ring0, cb0 + rr + k);
-      const int slot = padc(rcx);
-      const int bit = rr * kDiags + k;
-      if (((ux | uy) >> bit) & 1) {
-        const float2 r2 = mul2(mul2(c[k], sm.u.s.c_iv[slot]), ivr);
-#pragma unroll 1
-        for (int g = 0; g < 2; ++g) {
-          if (!(((g ? uy : ux) >> bit) & 1)) continue;
-          float r = g ? r2.y : r2.x;
-          const float m = g ? mstep.y : mstep.x;
-          bool add = false;
-          if (m <= kTrust) {
-            add = r > cx.thr;
-          } else {
-            const int64_t i = cx.rbase[g] + r0 + rr;
-            const int64_t j = i + cx.D0 + t * kDiags + k;
-            const unsigned long long sl = atomicAdd(cx.vcount, 1ull);
-            ++nreq;
-            if (sl < static_cast<unsigned long long>(cx.vcap)) {
-              VerifyReq q;
-              q.i = static_cast<uint64_t>(i) | (static_cast<uint64_t>(cx.prob) << 40);
-              q.d = static_cast<uint32_t>(j - i);
-              q.ub = r + m;
-              cx.vreq[sl] = q;
-            } else {
-              // request buffer full: verified in place (counted)
-              const Problem& pr = *cx.pr;
-              const float ev =
-                  (verify_cov_lane(pr.R, pr.C, i, j, cx.m) * pr.C.inv32[j]) * pr.R.inv32[i];
-              atomicAdd(cx.overflow, 1ull);
-              add = ev > cx.thr;
-              r = ev;
-            }
-          }
-          if (add) {
-            atomicAdd(g ? &sm.r_best[r0 + rr].y : &sm.r_best[r0 + rr].x, r);
-            atomicAdd(g ? &sm.c_best[rcx].y : &sm.c_best[rcx].x, r);
-          }
-        }
-      }
-      const float4 cf = col_fg(sm, slot);
-      c[k] = fma2(make_float2(cf.x, cf.y), make_float2(rf.z, rf.w), c[k]);
-      c[k] = fma2(make_float2(rf.x, rf.y), make_float2(cf.z, cf.w), c[k]);
-    }
-  }
-  return nreq;
-}
-
-// SUM_THRESH, per-cell path of one thread-step that may hold cells above the
-// threshold (flags fx, fy per segment; every lane calls it, adding nothing
-// where its flags are off): the block is rewound from the covariances at
-// the step's end (as the exact path rewinds) and walked again.  A cell above
-// the threshold by more than the step's margin m (per segment) adds its FP32
-// r; cells within m of it go to sum_uncertain.  Rows are reduced over the
-// warp, columns over neighbouring threads (thread t's columns 8..14 are
-// thread t + 1's 0..6) before the shared-memory atomics.  Returns the lane's
-// number of verification requests.
-__device__ __noinline__ int sum_block(Smem& sm, const float2 (&cov_end)[kDiags], int s, int t,
-                                      int lane, bool fx, bool fy, float2 mstep) {
-  const SlowCtx& cx = sm.cx;
-  const int r0 = s * kRows;
-  const int cb0 = 8 * (s + t);  // slab-relative column of (row 0, diagonal 0)
-  const float2 hi = make_float2(cx.thr + mstep.x, cx.thr + mstep.y);
-  const float2 lo = make_float2(cx.thr - mstep.x, cx.thr - mstep.y);
-  float2 c[kDiags];
-#pragma unroll
-  for (int k = 0; k < kDiags; ++k) c[k] = cov_end[k];
-  rewind_block(sm, c, r0, cb0);
-  uint64_t ux = 0, uy = 0;  // cells within the margin of the threshold
-  float2 cacc[15];
-#pragma unroll
-  for (int x = 0; x < 15; ++x) cacc[x] = make_float2(0.f, 0.f);
-#pragma unroll
-  for (int rr = 0; rr < kRows; ++rr) {
-    const float4 rf = sm.r_fg[r0 + rr];
-    const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
-    const float2 ivr = sm.r_iv[r0 + rr];
-    float2 rs = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int k = 0; k < kDiags; ++k) {
-      const int slot = padc(ringc(cx.ring0, cb0 + rr + k));
-      const float2 r2 = mul2(mul2(c[k], sm.u.s.c_iv[slot]), ivr);
-      // NaN cells compare false everywhere and add nothing
-      const float vx = (fx && r2.x > hi.x) ? r2.x : 0.f;
-      const float vy = (fy && r2.y > hi.y) ? r2.y : 0.f;
-      ux |= static_cast<uint64_t>(fx && r2.x > lo.x && !(r2.x > hi.x)) << (rr * kDiags + k);
-      uy |= static_cast<uint64_t>(fy && r2.y > lo.y && !(r2.y > hi.y)) << (rr * kDiags + k);
-      rs.x += vx;
-      rs.y += vy;
-      cacc[rr + k].x += vx;
-      cacc[rr + k].y += vy;
-      const float4 cf = col_fg(sm, slot);
-      c[k] = fma2(make_float2(cf.x, cf.y), dgr, c[k]);
-      c[k] = fma2(dfr, make_float2(cf.z, cf.w), c[k]);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      rs.x += __shfl_xor_sync(0xffffffffu, rs.x, o);
-      rs.y += __shfl_xor_sync(0xffffffffu, rs.y, o);
-    }
-    if (lane == 0) {
-      if (rs.x != 0.f) atomicAdd(&sm.r_best[r0 + rr].x, rs.x);
-      if (rs.y != 0.f) atomicAdd(&sm.r_best[r0 + rr].y, rs.y);
-    }
-  }
-#pragma unroll
-  for (int x = 0; x < 7; ++x) {
-    const float vx = __shfl_up_sync(0xffffffffu, cacc[8 + x].x, 1);
-    const float vy = __shfl_up_sync(0xffffffffu, cacc[8 + x].y, 1);
-    if (lane > 0) {
-      cacc[x].x += vx;
-      cacc[x].y += vy;
-    }
-  }
-#pragma unroll
-  for (int x = 0; x < 15; ++x) {
-    if (x < 8 || lane == 31) {
-      const int rcx = ringc(cx.ring0, cb0 + x);
-      if (cacc[x].x != 0.f) atomicAdd(&sm.c_best[rcx].x, cacc[x].x);
-      if (cacc[x].y != 0.f) atomicAdd(&sm.c_best[rcx].y, cacc[x].y);
-    }
-  }
-  return (ux | uy) ? sum_uncertain(sm, cov_end, s, t, ux, uy, mstep) : 0;
 }
 
 // MATRIX_SUMMARY: a thread's running maxima (per segment and target).
@@ -1197,6 +1040,9 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
       float4 cfw[16];
       float2 ciw[16];
       int pend = -1;
+      // segments of the pending block, per step (bits 0-1, 2-3; SUM_THRESH,
+      // every segment otherwise)
+      int pmsk = 15;
       float2 vlast = make_float2(0.f, 0.f);
       auto step = [&](const int s, auto parity) {
         constexpr int P = decltype(parity)::value;
@@ -1270,6 +1116,91 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
           const float2 bnd = mul2(mul2(make_float2(fmaxf(bx, 0.f), fmaxf(by, 0.f)), icm), irm);
           bx = bnd.x;
           by = bnd.y;
+        } else if constexpr (kSum) {
+          // SUM_THRESH: every cell's r (rounded as the exact path rounds it)
+          // against the threshold, where the segment's step margin is within
+          // kTrust (elsewhere `the` is out of reach and the segment goes to
+          // the exact path if it reaches the threshold); row sums per step
+          // row, column sums per step column, reduced after the step.  The
+          // column values come straight from shared memory (no carried
+          // window: its registers hold the sums).
+          const float2 smg = mul2(make_float2(kStepMarginC, kStepMarginC), mg);
+          const float thx = smg.x <= kTrust ? thr : kNoTarget;
+          const float thy = smg.y <= kTrust ? thr : kNoTarget;
+          float2 rsum[kRows];
+          float2 cacc[kRows + kDiags - 1];
+#pragma unroll
+          for (int x = 0; x < kRows + kDiags - 1; ++x) cacc[x] = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int rr = 0; rr < kRows; ++rr) {
+            const float4 rf = sm.r_fg[r0 + rr];
+            const float2 dfr = make_float2(rf.x, rf.y), dgr = make_float2(rf.z, rf.w);
+            const float2 ivr = sm.r_iv[r0 + rr];
+            rsum[rr] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < kDiags; ++k) {
+              const int x = rr + k;
+              const int slot = base + x + (x >> 3);
+              const float4 c4 = col_fg(sm, slot);
+              const float2 r2 = mul2(mul2(cov[k], sm.u.s.c_iv[slot]), ivr);
+              bx = fmaxf(bx, r2.x);  // NaN cells are ignored
+              by = fmaxf(by, r2.y);
+              const float vx = r2.x > thx ? r2.x : 0.f;
+              const float vy = r2.y > thy ? r2.y : 0.f;
+              rsum[rr] = make_float2(rsum[rr].x + vx, rsum[rr].y + vy);
+              cacc[x] = make_float2(cacc[x].x + vx, cacc[x].y + vy);
+              cov[k] = fma2(make_float2(c4.x, c4.y), dgr, cov[k]);
+              cov[k] = fma2(dfr, make_float2(c4.z, c4.w), cov[k]);
+            }
+          }
+          // rows: a reduce-scatter over the warp (lanes 4 r .. 4 r + 3 end
+          // with row r's total), one shared-memory atomic per row
+          {
+            float2 w4[4], w2[2];
+            const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const float2 snd = b16 ? rsum[i] : rsum[i + 4];
+              const float2 kp = b16 ? rsum[i + 4] : rsum[i];
+              w4[i] = make_float2(kp.x + __shfl_xor_sync(0xffffffffu, snd.x, 16),
+                                  kp.y + __shfl_xor_sync(0xffffffffu, snd.y, 16));
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+              const float2 snd = b8 ? w4[i] : w4[i + 2];
+              const float2 kp = b8 ? w4[i + 2] : w4[i];
+              w2[i] = make_float2(kp.x + __shfl_xor_sync(0xffffffffu, snd.x, 8),
+                                  kp.y + __shfl_xor_sync(0xffffffffu, snd.y, 8));
+            }
+            const float2 snd = b4 ? w2[0] : w2[1];
+            float2 z = b4 ? w2[1] : w2[0];
+            z.x += __shfl_xor_sync(0xffffffffu, snd.x, 4);
+            z.y += __shfl_xor_sync(0xffffffffu, snd.y, 4);
+            z.x += __shfl_xor_sync(0xffffffffu, z.x, 2);
+            z.y += __shfl_xor_sync(0xffffffffu, z.y, 2);
+            z.x += __shfl_xor_sync(0xffffffffu, z.x, 1);
+            z.y += __shfl_xor_sync(0xffffffffu, z.y, 1);
+            const int row = (b16 ? 4 : 0) + (b8 ? 2 : 0) + (b4 ? 1 : 0);
+            if ((lane & 3) == 0) {
+              if (z.x != 0.f) atomicAdd(&sm.r_best[r0 + row].x, z.x);
+              if (z.y != 0.f) atomicAdd(&sm.r_best[r0 + row].y, z.y);
+            }
+          }
+          // columns: thread t's step columns 8..14 are thread t + 1's 0..6
+#pragma unroll
+          for (int x = 0; x < kDiags - 1; ++x) {
+            const float ux = __shfl_up_sync(0xffffffffu, cacc[8 + x].x, 1);
+            const float uy = __shfl_up_sync(0xffffffffu, cacc[8 + x].y, 1);
+            if (lane > 0) cacc[x] = make_float2(cacc[x].x + ux, cacc[x].y + uy);
+          }
+#pragma unroll
+          for (int x = 0; x < kRows + kDiags - 1; ++x) {
+            if (x < 8 || lane == 31) {
+              const int rcx = ringc(ring0, 8 * (s + t) + x);
+              if (cacc[x].x != 0.f) atomicAdd(&sm.c_best[rcx].x, cacc[x].x);
+              if (cacc[x].y != 0.f) atomicAdd(&sm.c_best[rcx].y, cacc[x].y);
+            }
+          }
         } else {
           float2 rprev;
 #pragma unroll
@@ -1355,39 +1286,69 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
           }
           if (nonuni[0] || nonuni[1]) mat_cells_block(sm, cov, s, t, nonuni[0], nonuni[1]);
         }
+        // segments the exact path walks (bit 0: first, bit 1: second)
+        [[maybe_unused]] int smask = 3;
         if constexpr (kSum && !kCoarse) {
-          // SUM_THRESH: a segment that may hold a cell above the threshold
-          // is decided cell by cell on the owner's warp (sum_block); the
-          // exact path is not needed.  Its FP32 values carry at most the
-          // step's margin.
-          trig = false;
-          const bool fx = bx > tx, fy = by > ty;
-          if (__any_sync(0xffffffffu, fx || fy)) {
-            const float2 smg = mul2(make_float2(kStepMarginC, kStepMarginC), mg);
-            n_verify += sum_block(sm, cov, s, t, lane, fx, fy, smg);
-            if (fx && smg.x <= kTrust) tfast = fmaxf(tfast, smg.x);
-            if (fy && smg.y <= kTrust) tfast = fmaxf(tfast, smg.y);
-          }
+          // SUM_THRESH: cells of trusted segments were added above; an
+          // untrusted segment that reaches the threshold goes to the exact
+          // path (its cells alone), whose per-cell margins decide or verify.
+          const float2 smg = mul2(make_float2(kStepMarginC, kStepMarginC), mg);
+          const bool ux = smg.x > kTrust && bx > tx, uy = smg.y > kTrust && by > ty;
+          if (!ux && bx > tx) tfast = fmaxf(tfast, smg.x);
+          if (!uy && by > ty) tfast = fmaxf(tfast, smg.y);
+          trig = ux || uy;
+          smask = (ux ? 1 : 0) | (uy ? 2 : 0);
         }
-        const unsigned tmask = __ballot_sync(0xffffffffu, trig);
-        if (tmask) {
-          // queue the triggered lanes in rank order while there is room
-          const int rank = __popc(tmask & ((1u << lane) - 1u));
-          if (trig) {
-            if (qn + rank < kQueue) {
-              SlowItem& it = sm.queue[warp][qn + rank];
+        if constexpr (kSum && !kCoarse) {
+          // A step of a pair whose first step is pending joins that pending
+          // two-step block (its segments in mask bits 2, 3); others queue in
+          // rank order while there is room, else become the pending step.
+          // (The sums must not walk a segment twice.)
+          const bool want_q = trig && pend < 0;
+          if (trig && pend >= 0) pmsk |= smask << 2;
+          const unsigned tmask = __ballot_sync(0xffffffffu, want_q);
+          if (tmask) {
+            const int rank = __popc(tmask & ((1u << lane) - 1u));
+            if (want_q) {
+              if (qn + rank < kQueue) {
+                SlowItem& it = sm.queue[warp][qn + rank];
 #pragma unroll
-              for (int k = 0; k < kDiags; ++k) it.cov[k] = cov[k];
-              it.vw = make_float2(vx, vy);
-              it.s = s | (1 << 8);
-              it.owner = t;
-            } else if (pend < 0) {
-              pend = s;
+                for (int k = 0; k < kDiags; ++k) it.cov[k] = cov[k];
+                it.vw = make_float2(vx, vy);
+                it.s = s | (1 << 8) | (smask << 16);
+                it.owner = t;
+              } else {
+                pend = s;
+                pmsk = smask;
+              }
             }
+            const int nq = qn + __popc(tmask);
+            qn = nq < kQueue ? nq : kQueue;
           }
-          const int nq = qn + __popc(tmask);
-          qn = nq < kQueue ? nq : kQueue;
           n_slow += trig ? 1u : 0u;
+        } else {
+          // queue the triggered lanes in rank order while there is room;
+          // the exact path walks both segments of every step of the block
+          // (a cell of 1NN_INDEX published twice changes nothing)
+          const unsigned tmask = __ballot_sync(0xffffffffu, trig);
+          if (tmask) {
+            const int rank = __popc(tmask & ((1u << lane) - 1u));
+            if (trig) {
+              if (qn + rank < kQueue) {
+                SlowItem& it = sm.queue[warp][qn + rank];
+#pragma unroll
+                for (int k = 0; k < kDiags; ++k) it.cov[k] = cov[k];
+                it.vw = make_float2(vx, vy);
+                it.s = s | (1 << 8) | (15 << 16);
+                it.owner = t;
+              } else if (pend < 0) {
+                pend = s;
+              }
+            }
+            const int nq = qn + __popc(tmask);
+            qn = nq < kQueue ? nq : kQueue;
+            n_slow += trig ? 1u : 0u;
+          }
         }
         vlast = make_float2(vx, vy);
       };
@@ -1395,10 +1356,12 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
       for (int s = 0; s < kSteps; s += 2) {
         {
           const int rb = (rq + s + t) < kBlocks ? (rq + s + t) : (rq + s + t - kBlocks);
+          if constexpr (!(kSum && !kCoarse)) {
 #pragma unroll
-          for (int x = 0; x < kDiags - 1; ++x) {
-            cfw[x] = col_fg(sm, 9 * rb + x);  // padc(ring column 8 rb + x), x < 8
-            if constexpr (!kCoarse) ciw[x] = sm.u.s.c_iv[9 * rb + x];
+            for (int x = 0; x < kDiags - 1; ++x) {
+              cfw[x] = col_fg(sm, 9 * rb + x);  // padc(ring column 8 rb + x), x < 8
+              if constexpr (!kCoarse) ciw[x] = sm.u.s.c_iv[9 * rb + x];
+            }
           }
         }
         step(s, Parity<0>());
@@ -1419,7 +1382,7 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
 #pragma unroll
               for (int k = 0; k < kDiags; ++k) it.cov[k] = cov[k];
               it.vw = vlast;
-              it.s = pend | ((s + 2 - pend) << 8);
+              it.s = pend | ((s + 2 - pend) << 8) | (pmsk << 16);
               it.owner = t;
             }
             const int take = (np - done) < kQueue ? (np - done) : kQueue;
