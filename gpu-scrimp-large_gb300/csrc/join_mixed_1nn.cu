@@ -565,6 +565,89 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
   return nreq;
 }
 
+// SUM_THRESH: the cells of a thread-step that lie within the step's margin
+// m of the threshold (flags fx, fy per segment; rare), walked again by their
+// lane alone from the step's start (rewound from the covariances at its
+// end, as the exact path rewinds).  Each such cell is decided by its own
+// margin mk = vk inv_c inv_r (vk per segment, the exact path's formula): by
+// its FP32 r when mk is within kTrust, else by a verification request (a
+// full request buffer verifies it in place).  Adds go straight to the slab's
+// shared-memory sums.  Returns the lane's number of requests.
+__device__ __noinline__ int sum_near(Smem& sm, const float2 (&cov_end)[kDiags], int s, int t,
+                                     bool fx, bool fy, float2 m, float2 vk) {
+  const SlowCtx& cx = sm.cx;
+  const int r0 = s * kRows;
+  const int cb0 = 8 * (s + t);
+  float2 c[kDiags];
+#pragma unroll
+  for (int k = 0; k < kDiags; ++k) c[k] = cov_end[k];
+#pragma unroll 1
+  for (int rr = kRows - 1; rr >= 0; --rr) {
+    const float4 rf = sm.r_fg[r0 + rr];
+#pragma unroll
+    for (int k = 0; k < kDiags; ++k) {
+      const float4 cf = col_fg(sm, padc(ringc(cx.ring0, cb0 + rr + k)));
+      c[k] = fma2(make_float2(-rf.x, -rf.y), make_float2(cf.z, cf.w), c[k]);
+      c[k] = fma2(make_float2(-cf.x, -cf.y), make_float2(rf.z, rf.w), c[k]);
+    }
+  }
+  int nreq = 0;
+  float tmax = 0.f;
+#pragma unroll 1
+  for (int rr = 0; rr < kRows; ++rr) {
+    const float4 rf = sm.r_fg[r0 + rr];
+    const float2 ivr = sm.r_iv[r0 + rr];
+#pragma unroll 1
+    for (int k = 0; k < kDiags; ++k) {
+      const int rcx = ringc(cx.ring0, cb0 + rr + k);
+      const int slot = padc(rcx);
+      const float2 ivc = sm.u.s.c_iv[slot];
+      const float2 r2 = mul2(mul2(c[k], ivc), ivr);
+      const float2 mk2 = mul2(mul2(vk, ivc), ivr);
+#pragma unroll 1
+      for (int g = 0; g < 2; ++g) {
+        const float r = g ? r2.y : r2.x;
+        if (!((g ? fy : fx) && fabsf(r - cx.thr) <= (g ? m.y : m.x))) continue;  // NaN: skip
+        const float mk = g ? mk2.y : mk2.x;
+        float add = 0.f;
+        if (mk <= kTrust) {
+          if (r > cx.thr) {
+            add = r;
+            tmax = fmaxf(tmax, mk);
+          }
+        } else {
+          const int64_t i = cx.rbase[g] + r0 + rr;
+          const int64_t j = i + cx.D0 + t * kDiags + k;
+          const unsigned long long sl = atomicAdd(cx.vcount, 1ull);
+          ++nreq;
+          if (sl < static_cast<unsigned long long>(cx.vcap)) {
+            VerifyReq q;
+            q.i = static_cast<uint64_t>(i) | (static_cast<uint64_t>(cx.prob) << 40);
+            q.d = static_cast<uint32_t>(j - i);
+            q.ub = r + mk;
+            cx.vreq[sl] = q;
+          } else {
+            // request buffer full: verified in place (counted)
+            const Problem& pr = *cx.pr;
+            const float ev = (cov_part(pr.R, pr.C, i, j, 0, cx.m) * pr.C.inv32[j]) * pr.R.inv32[i];
+            atomicAdd(cx.overflow, 1ull);
+            if (ev > cx.thr) add = ev;
+          }
+        }
+        if (add != 0.f) {
+          atomicAdd(g ? &sm.r_best[r0 + rr].y : &sm.r_best[r0 + rr].x, add);
+          atomicAdd(g ? &sm.c_best[rcx].y : &sm.c_best[rcx].x, add);
+        }
+      }
+      const float4 cf = col_fg(sm, slot);
+      c[k] = fma2(make_float2(cf.x, cf.y), make_float2(rf.z, rf.w), c[k]);
+      c[k] = fma2(make_float2(rf.x, rf.y), make_float2(cf.z, cf.w), c[k]);
+    }
+  }
+  if (tmax > 0.f) atomicMax(cx.tmargin, static_cast<unsigned long long>(__float_as_uint(tmax)));
+  return nreq;
+}
+
 // MATRIX_SUMMARY: a thread's running maxima (per segment and target).
 struct MatRun {
   int cell[2][2];
@@ -1045,7 +1128,7 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
       int pmsk = 15;
       float2 vlast = make_float2(0.f, 0.f);
       auto step = [&](const int s, auto parity) {
-        constexpr int P = decltype(parity)::value;
+        [[maybe_unused]] constexpr int P = decltype(parity)::value;
         const int r0 = s * kRows;
         // ring block of the step's first column 8(s + t)
         const int rb = (rq + s + t) < kBlocks ? (rq + s + t) : (rq + s + t - kBlocks);
@@ -1124,9 +1207,12 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
           // row, column sums per step column, reduced after the step.  The
           // column values come straight from shared memory (no carried
           // window: its registers hold the sums).
+          // a cell above the threshold by more than the step's margin (which
+          // bounds every cell's own margin) adds its r; cells within it are
+          // rare and settled by sum_near after the step
           const float2 smg = mul2(make_float2(kStepMarginC, kStepMarginC), mg);
-          const float thx = smg.x <= kTrust ? thr : kNoTarget;
-          const float thy = smg.y <= kTrust ? thr : kNoTarget;
+          const float thx = thr + smg.x, thy = thr + smg.y;
+          float2 dmin = make_float2(3.f, 3.f);  // nearest |r - thr| of the step
           float2 rsum[kRows];
           float2 cacc[kRows + kDiags - 1];
 #pragma unroll
@@ -1145,10 +1231,11 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
               const float2 r2 = mul2(mul2(cov[k], sm.u.s.c_iv[slot]), ivr);
               bx = fmaxf(bx, r2.x);  // NaN cells are ignored
               by = fmaxf(by, r2.y);
-              const float vx = r2.x > thx ? r2.x : 0.f;
-              const float vy = r2.y > thy ? r2.y : 0.f;
-              rsum[rr] = make_float2(rsum[rr].x + vx, rsum[rr].y + vy);
-              cacc[x] = make_float2(cacc[x].x + vx, cacc[x].y + vy);
+              dmin = make_float2(fminf(dmin.x, fabsf(r2.x - thr)), fminf(dmin.y, fabsf(r2.y - thr)));
+              const float ax = r2.x > thx ? r2.x : 0.f;
+              const float ay = r2.y > thy ? r2.y : 0.f;
+              rsum[rr] = make_float2(rsum[rr].x + ax, rsum[rr].y + ay);
+              cacc[x] = make_float2(cacc[x].x + ax, cacc[x].y + ay);
               cov[k] = fma2(make_float2(c4.x, c4.y), dgr, cov[k]);
               cov[k] = fma2(dfr, make_float2(c4.z, c4.w), cov[k]);
             }
@@ -1201,6 +1288,15 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
               if (cacc[x].y != 0.f) atomicAdd(&sm.c_best[rcx].y, cacc[x].y);
             }
           }
+          const bool nx = dmin.x <= smg.x, ny = dmin.y <= smg.y;
+          if (nx || ny) {
+            const float2 vk = make_float2(kBoundC * kEps * sqrtf(kRows * vx),
+                                          kBoundC * kEps * sqrtf(kRows * vy));
+            n_verify += sum_near(sm, cov, s, t, nx, ny, smg, vk);
+          }
+          // the largest margin of a value added from FP32 by this step
+          if (bx > thx) tfast = fmaxf(tfast, smg.x);
+          if (by > thy) tfast = fmaxf(tfast, smg.y);
         } else {
           float2 rprev;
 #pragma unroll
@@ -1289,15 +1385,10 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
         // segments the exact path walks (bit 0: first, bit 1: second)
         [[maybe_unused]] int smask = 3;
         if constexpr (kSum && !kCoarse) {
-          // SUM_THRESH: cells of trusted segments were added above; an
-          // untrusted segment that reaches the threshold goes to the exact
-          // path (its cells alone), whose per-cell margins decide or verify.
-          const float2 smg = mul2(make_float2(kStepMarginC, kStepMarginC), mg);
-          const bool ux = smg.x > kTrust && bx > tx, uy = smg.y > kTrust && by > ty;
-          if (!ux && bx > tx) tfast = fmaxf(tfast, smg.x);
-          if (!uy && by > ty) tfast = fmaxf(tfast, smg.y);
-          trig = ux || uy;
-          smask = (ux ? 1 : 0) | (uy ? 2 : 0);
+          // SUM_THRESH: every cell was decided above (sum_near for the ones
+          // near the threshold); the exact path is not needed
+          trig = false;
+          smask = 0;
         }
         if constexpr (kSum && !kCoarse) {
           // A step of a pair whose first step is pending joins that pending
