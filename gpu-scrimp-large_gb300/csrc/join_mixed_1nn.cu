@@ -1592,8 +1592,13 @@ verify_requests_kernel(JoinParams P) {
     if (P.knn_k > 0) {  // APPROX_ALL_NEIGHBORS: into the k-best lists
       const int k = P.knn_k;
       const float thr = static_cast<float>(P.threshold);
-      const bool ro = pr.key_row && rq.ub > knn_floor(pr.key_row + i * k, k, thr, P.kl);
-      const bool co = pr.key_col && rq.ub > knn_floor(pr.key_col + j * k, k, thr, P.kl);
+      // decided by lane 0 for the warp: the lists change under other
+      // warps' (and lane 0's own) atomics, and the lanes' loads of them need
+      // not agree, while the shuffles of the dot need every lane
+      bool ro = pr.key_row && rq.ub > knn_floor(pr.key_row + i * k, k, thr, P.kl);
+      bool co = pr.key_col && rq.ub > knn_floor(pr.key_col + j * k, k, thr, P.kl);
+      ro = __shfl_sync(0xffffffffu, ro, 0);
+      co = __shfl_sync(0xffffffffu, co, 0);
       if (!ro && !co) continue;
       const float cv = verify_cov_warp(pr.R, pr.C, i, j, pr.m, lane);
       if (lane == 0) {
@@ -1608,8 +1613,11 @@ verify_requests_kernel(JoinParams P) {
       }
       continue;
     }
-    const bool row_open = pr.key_row && rq.ub > key_corr_floor(pr.key_row[i], P.kl);
-    const bool col_open = pr.key_col && rq.ub > key_corr_floor(pr.key_col[j], P.kl);
+    // warp-uniform by lane 0's view, as above
+    bool row_open = pr.key_row && rq.ub > key_corr_floor(pr.key_row[i], P.kl);
+    bool col_open = pr.key_col && rq.ub > key_corr_floor(pr.key_col[j], P.kl);
+    row_open = __shfl_sync(0xffffffffu, row_open, 0);
+    col_open = __shfl_sync(0xffffffffu, col_open, 0);
     if (!row_open && !col_open) continue;
     const float cv = verify_cov_warp(pr.R, pr.C, i, j, pr.m, lane);
     if (lane == 0) {
