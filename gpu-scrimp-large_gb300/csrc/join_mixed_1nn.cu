@@ -565,18 +565,16 @@ __device__ __noinline__ int drain_queue(Smem& sm, int warp, int count, int lane)
   return nreq;
 }
 
-// SUM_THRESH: the cells of a thread-step that the main loop found within
-// their own margin mk = vk inv_c inv_r of the threshold (bit 8 rr + k of ux,
-// uy per segment; rare), walked again by their lane alone from the step's
-// start (rewound from the covariances at its end, as the exact path
-// rewinds).  Each is decided by its FP32 r when mk is within kTrust, else by
-// a verification request (a full request buffer verifies it in place).  The
-// main loop added every other cell above the threshold, so the masks, not a
-// recomputed classification, pick the cells: no cell counts twice.  Adds go
-// straight to the slab's shared-memory sums.  Returns the lane's number of
-// requests.
+// SUM_THRESH: the cells of a thread-step that lie within the step's margin
+// m of the threshold (flags fx, fy per segment; rare), walked again by their
+// lane alone from the step's start (rewound from the covariances at its
+// end, as the exact path rewinds).  Each such cell is decided by its own
+// margin mk = vk inv_c inv_r (vk per segment, the exact path's formula): by
+// its FP32 r when mk is within kTrust, else by a verification request (a
+// full request buffer verifies it in place).  Adds go straight to the slab's
+// shared-memory sums.  Returns the lane's number of requests.
 __device__ __noinline__ int sum_near(Smem& sm, const float2 (&cov_end)[kDiags], int s, int t,
-                                     uint64_t ux, uint64_t uy, float2 vk) {
+                                     bool fx, bool fy, float2 m, float2 vk) {
   const SlowCtx& cx = sm.cx;
   const int r0 = s * kRows;
   const int cb0 = 8 * (s + t);
@@ -608,9 +606,8 @@ __device__ __noinline__ int sum_near(Smem& sm, const float2 (&cov_end)[kDiags], 
       const float2 mk2 = mul2(mul2(vk, ivc), ivr);
 #pragma unroll 1
       for (int g = 0; g < 2; ++g) {
-        // the cells the main loop found within their margin (bit 8 rr + k)
-        if (!(((g ? uy : ux) >> (rr * kDiags + k)) & 1)) continue;
         const float r = g ? r2.y : r2.x;
+        if (!((g ? fy : fx) && fabsf(r - cx.thr) <= (g ? m.y : m.x))) continue;  // NaN: skip
         const float mk = g ? mk2.y : mk2.x;
         float add = 0.f;
         if (mk <= kTrust) {
@@ -1210,14 +1207,12 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
           // row, column sums per step column, reduced after the step.  The
           // column values come straight from shared memory (no carried
           // window: its registers hold the sums).
-          // a cell above the threshold by more than its own margin
-          // mk = vk inv_c inv_r (the exact path's formula) adds its r; cells
-          // within mk of it are rare, marked, and settled by sum_near after
-          // the step
-          const float2 vk = make_float2(kBoundC * kEps * sqrtf(kRows * vx),
-                                        kBoundC * kEps * sqrtf(kRows * vy));
-          uint64_t ux = 0, uy = 0;
-          float2 tmk = make_float2(0.f, 0.f);  // largest margin of an added value
+          // a cell above the threshold by more than the step's margin (which
+          // bounds every cell's own margin) adds its r; cells within it are
+          // rare and settled by sum_near after the step
+          const float2 smg = mul2(make_float2(kStepMarginC, kStepMarginC), mg);
+          const float thx = thr + smg.x, thy = thr + smg.y;
+          float2 dmin = make_float2(3.f, 3.f);  // nearest |r - thr| of the step
           float2 rsum[kRows];
           float2 cacc[kRows + kDiags - 1];
 #pragma unroll
@@ -1233,16 +1228,12 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
               const int x = rr + k;
               const int slot = base + x + (x >> 3);
               const float4 c4 = col_fg(sm, slot);
-              const float2 civ = sm.u.s.c_iv[slot];
-              const float2 r2 = mul2(mul2(cov[k], civ), ivr);
-              const float2 mk = mul2(mul2(vk, civ), ivr);
-              const float dx = r2.x - thr, dy = r2.y - thr;
-              const bool sx = dx > mk.x, sy = dy > mk.y;  // surely above (NaN: false)
-              const float ax = sx ? r2.x : 0.f;
-              const float ay = sy ? r2.y : 0.f;
-              tmk = make_float2(fmaxf(tmk.x, sx ? mk.x : 0.f), fmaxf(tmk.y, sy ? mk.y : 0.f));
-              ux |= static_cast<uint64_t>(fabsf(dx) <= mk.x) << (rr * kDiags + k);
-              uy |= static_cast<uint64_t>(fabsf(dy) <= mk.y) << (rr * kDiags + k);
+              const float2 r2 = mul2(mul2(cov[k], sm.u.s.c_iv[slot]), ivr);
+              bx = fmaxf(bx, r2.x);  // NaN cells are ignored
+              by = fmaxf(by, r2.y);
+              dmin = make_float2(fminf(dmin.x, fabsf(r2.x - thr)), fminf(dmin.y, fabsf(r2.y - thr)));
+              const float ax = r2.x > thx ? r2.x : 0.f;
+              const float ay = r2.y > thy ? r2.y : 0.f;
               rsum[rr] = make_float2(rsum[rr].x + ax, rsum[rr].y + ay);
               cacc[x] = make_float2(cacc[x].x + ax, cacc[x].y + ay);
               cov[k] = fma2(make_float2(c4.x, c4.y), dgr, cov[k]);
@@ -1297,8 +1288,15 @@ __device__ __forceinline__ void band_body(const JoinParams& P) {
               if (cacc[x].y != 0.f) atomicAdd(&sm.c_best[rcx].y, cacc[x].y);
             }
           }
-          if (ux | uy) n_verify += sum_near(sm, cov, s, t, ux, uy, vk);
-          tfast = fmaxf(tfast, fmaxf(tmk.x, tmk.y));
+          const bool nx = dmin.x <= smg.x, ny = dmin.y <= smg.y;
+          if (nx || ny) {
+            const float2 vk = make_float2(kBoundC * kEps * sqrtf(kRows * vx),
+                                          kBoundC * kEps * sqrtf(kRows * vy));
+            n_verify += sum_near(sm, cov, s, t, nx, ny, smg, vk);
+          }
+          // the largest margin of a value added from FP32 by this step
+          if (bx > thx) tfast = fmaxf(tfast, smg.x);
+          if (by > thy) tfast = fmaxf(tfast, smg.y);
         } else {
           float2 rprev;
 #pragma unroll
