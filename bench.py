@@ -52,12 +52,11 @@ CPU_NA, CPU_NB = 1 << 17, 1 << 16
 # Algorithmic work per comparison: 2 FMA (covariance update) + 2 MUL
 # (r = cov * inv_c * inv_r), counted on the FMA pipe.
 OPS_PER_CELL = 4
-# DRAM bytes (read + write) of one launch of the mixed join kernel on this
-# workload: one single-pass ncu capture of the full-size launch
-# (profiles/join_mixed_1nn_cfg2.txt; mean of the five main launches).  Mostly
-# the verification requests (16 B each, 1.5e7 per join) and profile write-back:
-# the series, statistics and profiles stay in the 129 MB L2.
-DRAM_BYTES_PER_LAUNCH = 57.45e6 + 202.48e6
+# DRAM bytes of one launch of the mixed join kernel on this workload: not
+# captured for the current kernel (captures beyond the launch times run on
+# small cases: profiles/join_mixed_1nn_coarse_selfjoin_2e20_m1024.txt for the
+# default workload), so the line reports none.
+DRAM_BYTES_PER_LAUNCH = None
 
 
 def max_over_ranks(x, dist, device):
@@ -410,11 +409,11 @@ def run_batch_workload(args, world, rank, local):
 
 
 # DRAM bytes (read + write) of one band-kernel launch on the 2^24-point
-# self-join: a one-launch ncu capture of the first 2^20 samples (190.7 MB
-# read + 572.8 MB written, profiles/join_mixed_1nn_coarse_selfjoin_2e20_m1024
+# self-join: a one-launch ncu capture of the first 2^20 samples (196.0 MB
+# read + 648.2 MB written, profiles/join_mixed_1nn_coarse_selfjoin_2e20_m1024
 # .txt), scaled by the window count (x16), since the bytes are mostly the
 # 16-byte verification requests, whose number grows with the windows.
-SELF_DRAM_BYTES_PER_LAUNCH = (190.7e6 + 572.8e6) * 16
+SELF_DRAM_BYTES_PER_LAUNCH = (196.0e6 + 648.2e6) * 16
 
 
 def run_self_headline(args, world, rank, local):
