@@ -331,12 +331,35 @@ struct Workspace {
   cudaGraphExec_t batch_exec = nullptr;
   std::vector<int64_t> batch_key;
   std::map<int64_t, int64_t> batch_seg;
+  // Pinned host staging of the batched joins' copies (grow-only): the
+  // gathered series in, the profiles in and out, the correlations out.
+  std::vector<Buf> pinned;
 };
 
 constexpr int64_t kMinVerifyReqs = int64_t{1} << 22;
 constexpr int64_t kMaxVerifyReqs = int64_t{1} << 30;  // 16 GiB of requests
 
 Workspace g_ws[64];
+
+// Pinned host buffer `slot` of at least `bytes` (grow-only; no copy may be in
+// flight on the old one: the batched join ends with a stream sync).
+int ensure_pinned(Workspace& ws, size_t slot, size_t bytes, void** out, std::string* msg) {
+  if (ws.pinned.size() <= slot) ws.pinned.resize(slot + 1);
+  Buf& b = ws.pinned[slot];
+  if (b.bytes < bytes) {
+    if (b.p) cudaFreeHost(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    if (cudaHostAlloc(&b.p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      *msg = "Error: out of pinned host memory";
+      return SCAMP_ERR_OUT_OF_MEMORY;
+    }
+    b.bytes = bytes;
+  }
+  *out = b.p;
+  return SCAMP_OK;
+}
 
 int ensure(Workspace& ws, size_t slot, size_t bytes, void** out, std::string* msg) {
   if (ws.bufs.size() <= slot) ws.bufs.resize(slot + 1);
@@ -2173,11 +2196,16 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
                  d_bhi, d_blo, d_murel, d_keys};
 
   // ---- host side: inputs gathered, every launch's arguments built ----
-  std::vector<double> h_raw(static_cast<size_t>(Nn));
-  std::vector<uint64_t> h_prof(static_cast<size_t>(Nns));
+  void *hp_raw, *hp_prof, *hp_corr = nullptr;
+  if ((rc = ensure_pinned(ws, 0, std::max<size_t>(Nn * 8, 8), &hp_raw, msg))) return rc;
+  if ((rc = ensure_pinned(ws, 1, std::max<size_t>(Nns * 8, 8), &hp_prof, msg))) return rc;
+  if (want_corr && (rc = ensure_pinned(ws, 2, std::max<size_t>(Nns * 8, 8), &hp_corr, msg))) return rc;
+  double* h_raw = static_cast<double*>(hp_raw);
+  uint64_t* h_prof = static_cast<uint64_t*>(hp_prof);
+  double* h_corr = static_cast<double*>(hp_corr);
   for (int k = 0; k < count; ++k) {
-    std::memcpy(h_raw.data() + ser[k].off_n, args[k].timeseries_a, ser[k].n * 8);
-    std::memcpy(h_prof.data() + ser[k].off_ns, res[k].profile_a, ser[k].ns * 8);
+    std::memcpy(h_raw + ser[k].off_n, args[k].timeseries_a, ser[k].n * 8);
+    std::memcpy(h_prof + ser[k].off_ns, res[k].profile_a, ser[k].ns * 8);
   }
   const int chunk = 64;
   std::vector<StatsJob> jobs(count);
@@ -2329,8 +2357,8 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
     CUDA_TRY(cudaMemcpyAsync(d_seed, seed_jobs.data(), sizeof(BatchSeedJob) * nseed_jobs,
                              cudaMemcpyHostToDevice, st));
   }
-  CUDA_TRY(cudaMemcpyAsync(d_raw, h_raw.data(), Nn * 8, cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemcpyAsync(d_prof, h_prof.data(), Nns * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d_raw, h_raw, Nn * 8, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d_prof, h_prof, Nns * 8, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(StatsJob) * count, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(d_jpre, jpre.data(), 8 * (count + 1), cudaMemcpyHostToDevice, st));
   if (!probs.empty()) {
@@ -2414,17 +2442,15 @@ int run_batch(Workspace& ws, const scamp_c_args* args, scamp_c_result* res, int 
   ws.timed_kernel = ws.timed_verify = !probs.empty();
 
   // ---- copies out ----
-  CUDA_TRY(cudaMemcpyAsync(h_prof.data(), d_prof, Nns * 8, cudaMemcpyDeviceToHost, st));
-  std::vector<double> h_corr;
+  CUDA_TRY(cudaMemcpyAsync(h_prof, d_prof, Nns * 8, cudaMemcpyDeviceToHost, st));
   if (want_corr) {
-    h_corr.resize(static_cast<size_t>(Nns));
-    CUDA_TRY(cudaMemcpyAsync(h_corr.data(), d_corr, Nns * 8, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(h_corr, d_corr, Nns * 8, cudaMemcpyDeviceToHost, st));
   }
   CUDA_TRY(cudaEventRecord(ws.ev1, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   for (int k = 0; k < count; ++k) {
-    std::memcpy(res[k].profile_a, h_prof.data() + ser[k].off_ns, ser[k].ns * 8);
-    if (res[k].corr_a) std::memcpy(res[k].corr_a, h_corr.data() + ser[k].off_ns, ser[k].ns * 8);
+    std::memcpy(res[k].profile_a, h_prof + ser[k].off_ns, ser[k].ns * 8);
+    if (res[k].corr_a) std::memcpy(res[k].corr_a, h_corr + ser[k].off_ns, ser[k].ns * 8);
   }
   scamp_c_result tot{};
   read_times(ws, &tot);
