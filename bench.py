@@ -151,9 +151,9 @@ def make_workload(na=None, nb=None):
     from scamp_gb300 import workloads
 
     if WORKLOAD_KIND == "self":
-        a, m = workloads.cfg3_large(n=na or NA, m=SELF_M)
+        a, m = workloads.noisy_walk_selfjoin(n=na or NA, m=SELF_M)
         return a, None, m
-    return workloads.cfg2_abjoin(na=na or NA, nb=nb or NB, m=M)
+    return workloads.motif_abjoin(na=na or NA, nb=nb or NB, m=M)
 
 
 def _cpu_join():
@@ -253,7 +253,7 @@ def run_gaps_workload(args, world, rank, local):
     from scamp_gb300 import workloads
 
     n = 1 << (args.na_log2 or 23)
-    x, m = workloads.cfg5_gaps(n=n, m=4096)
+    x, m = workloads.gapped_walk_selfjoin(n=n, m=4096)
     res = {}
     for prof in args.gaps_profiles.split(","):
         r = None
@@ -311,7 +311,7 @@ def run_batch_workload(args, world, rank, local):
     from scamp_gb300 import workloads
 
     torch.cuda.set_device(local)
-    batch = workloads.cfg4_batch()
+    batch = workloads.walk_batch()
     if args.batch_series:
         batch = batch[: args.batch_series]  # a smaller batch, for profiling captures
     series = [x for x, _ in batch]

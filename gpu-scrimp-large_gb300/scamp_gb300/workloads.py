@@ -16,13 +16,13 @@ def random_walk(rng, n):
     return x
 
 
-def cfg1_selfjoin(n=131072, seed=1):
+def walk_selfjoin(n=131072, seed=1):
     """Self-join, m=100: one seeded random walk."""
     rng = np.random.default_rng(seed)
     return random_walk(rng, n), 100
 
 
-def cfg2_abjoin(na=1 << 20, nb=1 << 19, m=256, motifs=64, motif_len=256,
+def motif_abjoin(na=1 << 20, nb=1 << 19, m=256, motifs=64, motif_len=256,
                 nan_frac=0.001, seed=2):
     """AB-join, m=256: two random walks sharing 64 planted sinusoid motifs
     (sin(2 pi t / P) + 0.1 N(0,1), P ~ U[20, 200], length 256) at seeded
@@ -45,13 +45,13 @@ def cfg2_abjoin(na=1 << 20, nb=1 << 19, m=256, motifs=64, motif_len=256,
     return a, b, m
 
 
-def cfg3_large(n=1 << 24, m=1024, seed=3):
+def noisy_walk_selfjoin(n=1 << 24, m=1024, seed=3):
     """Self-join: random walk plus 0.5 N(0,1) noise."""
     rng = np.random.default_rng(seed)
     return random_walk(rng, n) + 0.5 * rng.standard_normal(n), m
 
 
-def cfg4_batch(count=4096, lo=10, hi=16, seed=4):
+def walk_batch(count=4096, lo=10, hi=16, seed=4):
     """Independent series: lengths round(2^U[lo,hi]), random walks scaled by
     LogU(1e-3, 1e3) and offset by U(-1e4, 1e4), windows from {32, 64, 128}."""
     rng = np.random.default_rng(seed)
@@ -65,7 +65,7 @@ def cfg4_batch(count=4096, lo=10, hi=16, seed=4):
     return out
 
 
-def cfg5_gaps(n=1 << 27, m=4096, gap_frac=0.01, seed=5):
+def gapped_walk_selfjoin(n=1 << 27, m=4096, gap_frac=0.01, seed=5):
     """Self-join: random walk with 1% of samples in NaN gaps of length
     U[1, 500]."""
     rng = np.random.default_rng(seed)

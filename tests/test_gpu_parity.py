@@ -286,7 +286,7 @@ def test_merge_into_best_so_far(gpu_engine, oracle_mod, precision, tol):
 
 @pytest.mark.parametrize("precision,tol", PRECISIONS)
 def test_extreme_scale_and_offset(gpu_engine, oracle_mod, precision, tol):
-    # cfg4-like: random walks scaled by 1e-3..1e3 and offset by up to 1e4
+    # the batched workload's regime: random walks scaled by 1e-3..1e3 and offset by up to 1e4
     rng = np.random.default_rng(31)
     for s, o in [(1e-3, 1e4), (1e3, -1e4), (1.0, 0.0)]:
         a = rw(rng, 3000) * s + o
@@ -298,11 +298,11 @@ def test_extreme_scale_and_offset(gpu_engine, oracle_mod, precision, tol):
 
 
 @pytest.mark.parametrize("precision,tol", PRECISIONS)
-def test_cfg2_shaped_small(gpu_engine, oracle_mod, precision, tol):
+def test_motif_abjoin_small(gpu_engine, oracle_mod, precision, tol):
     from scamp_gb300 import workloads
 
-    a, b, m = workloads.cfg2_abjoin(na=1 << 14, nb=1 << 13, motifs=16)
-    run_1nn(gpu_engine, oracle_mod, a, b, m, precision, tol, keep_rows=True, name="cfg2s")
+    a, b, m = workloads.motif_abjoin(na=1 << 14, nb=1 << 13, motifs=16)
+    run_1nn(gpu_engine, oracle_mod, a, b, m, precision, tol, keep_rows=True, name="motif_ab_small")
 
 
 @pytest.mark.parametrize("precision,tol", PRECISIONS)
@@ -375,7 +375,7 @@ def test_against_reference_golden_fixtures(gpu_engine, precision, tol):
 def test_seeded_abjoin(gpu_engine, oracle_mod, keep_rows):
     from scamp_gb300 import workloads
 
-    a, b, m = workloads.cfg2_abjoin(na=1 << 17, nb=1 << 16, motifs=16)
+    a, b, m = workloads.motif_abjoin(na=1 << 17, nb=1 << 16, motifs=16)
     assert gpu_engine.count_cells(len(a), m, len_b=len(b)) >= 4 << 30
     got, _ = run_1nn(gpu_engine, oracle_mod, a, b, m, "mixed", TOL_MIXED, keep_rows=keep_rows,
                      rows=keep_rows, name="seeded_ab")

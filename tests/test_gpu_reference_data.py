@@ -223,7 +223,7 @@ def test_selfjoin_benchmark_size(gpu_engine, oracle_mod, precision, tol):
     131072 points, m = 100."""
     from scamp_gb300 import workloads
 
-    a, m = workloads.cfg1_selfjoin()
+    a, m = workloads.walk_selfjoin()
     _engine_1nn(gpu_engine, oracle_mod, "selfjoin131072", a, None, m, precision, tol)
 
 
@@ -234,7 +234,7 @@ def test_abjoin_benchmark_quarter_size(gpu_engine, oracle_mod, precision, tol):
     both directions."""
     from scamp_gb300 import workloads
 
-    a, b, m = workloads.cfg2_abjoin(na=1 << 18, nb=1 << 17)
+    a, b, m = workloads.motif_abjoin(na=1 << 18, nb=1 << 17)
     _engine_1nn(gpu_engine, oracle_mod, "ab2e18", a, b, m, precision, tol, keep_rows=True)
 
 

@@ -60,7 +60,7 @@ def test_tc_anchors_abjoin_keep_rows_odd_window(gpu_engine, oracle_mod):
 def test_tc_anchors_nan_gaps_long_window(gpu_engine, oracle_mod):
     from scamp_gb300 import workloads
 
-    x, _ = workloads.cfg5_gaps(n=1 << 18, m=1024)
+    x, _ = workloads.gapped_walk_selfjoin(n=1 << 18, m=1024)
     want = oracle_mod.join(x, None, 1024, exact_flat=True)
     got = gpu_engine.join(x, None, 1024, "1NN_INDEX", "mixed", return_corr=True, anchor_mode=2)
     _, gi = gpu_engine.unpack_profile(got["profile_a"])
