@@ -73,13 +73,17 @@ int64_t default_anchor_interval(int64_t m) {
   return std::min<int64_t>(std::max<int64_t>(1024, 32 * m), std::max<int64_t>(16384, 2 * m));
 }
 
-// Anchor interval of the mixed SUM_THRESH join: much shorter, since every
-// cell within its drift margin of the threshold must be settled one by one
-// (a 1NN join only settles the cells near a window's best).  AB-join of
-// 2^19 x 2^18 random walks, m = 256, r > 0.5: K = 8192 (the 1NN rule) 254
-// ms (2.2e7 verifications), 4096 205, 2048 171, 1024 149, 512 139 (1.0e6);
-// at r > 0.9: 119, 110, 105, 104, 109 ms.
-int64_t sum_anchor_interval(int64_t m) { return std::max<int64_t>(512, 2 * m); }
+// Anchor interval of the mixed SUM_THRESH, k-best and matrix-summary joins:
+// much shorter, since every cell within its drift margin of the threshold
+// (or of a window's k-th best) must be settled one by one, where a 1NN join
+// only settles the cells near a window's best.  AB-join of 2^19 x 2^18
+// random walks, m = 256, sums above 0.5: K = 8192 (the 1NN rule) 254 ms
+// (2.2e7 verifications), 4096 205, 2048 171, 1024 149, 512 139 (1.0e6); above
+// 0.9: 119, 110, 105, 104, 109 ms.  k = 5 best above 0.5, 2^18-sample walks:
+// self-join K = 8192 / 2048 / 1024 / 512 47.3 / 35.5 / 28.4 / 26.1 ms, AB
+// (2^18 x 2^17, both profiles) 192.8 / 102.1 / 48.6 / 36.3 ms; the matrix
+// summary's time does not change (29.5-30.1 ms), its stated bound falls.
+int64_t short_anchor_interval(int64_t m) { return std::max<int64_t>(512, 2 * m); }
 
 // Windows from which the mixed band kernel filters blocks by the per-step
 // covariance bound (join_mixed_1nn.cu, kCoarse) instead of per-cell r: the
@@ -915,9 +919,8 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   const double cells_d = static_cast<double>(plan.cells);
   const int64_t k_lb = static_cast<int64_t>(cells_d / (8.0 * resident * 2.0 * W));
   if (kind == K_MIXED) {
-    const bool sum = !is_1nn && !is_knn && !is_mat;
     K = a->anchor_interval > 0 ? a->anchor_interval
-                               : (sum ? sum_anchor_interval(m) : default_anchor_interval(m));
+                               : (is_1nn ? default_anchor_interval(m) : short_anchor_interval(m));
   } else {
     K = fp64_segment(m);
   }
