@@ -548,7 +548,8 @@ def run_self_headline(args, world, rank, local):
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    # three ~21 s joins of the default workload: about a minute timed
+    p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--fp64-steps", type=int, default=1)
