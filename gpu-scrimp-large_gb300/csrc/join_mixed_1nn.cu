@@ -1,6 +1,7 @@
 // join_mixed_1nn.cu -- the mixed-precision band kernel: FP32 filter over an
-// FP32 recurrence, exact path for the blocks it flags.  Serves 1NN_INDEX
-// (verified candidates) and SUM_THRESH.
+// FP32 recurrence, exact path for the blocks it flags.  One body, five
+// instantiations: 1NN_INDEX (per-cell and per-step-bound filters),
+// SUM_THRESH, APPROX_ALL_NEIGHBORS (k-best lists) and MATRIX_SUMMARY.
 //
 // Work decomposition as in join_fp64.cu (persistent kernel over a device
 // queue of units = band of kBand diagonals x two row segments of seg_len
@@ -22,22 +23,27 @@
 // the kernel accumulates cov^2 and per thread the squared bound of the
 // increments |df_c dg_r| + |df_r dg_c|, and uses
 //   margin = C * 2^-24 * sqrt(rows * (sum cov^2 + sum inc^2)) * inv_c * inv_r.
-// Each warp drains its queue cooperatively (16 lanes per queued block):
-// cells that may improve their row or column are published with their FP32
-// value when the margin is below kTrust; otherwise the lower bound r - margin
-// is published and the cell goes to a request buffer that
-// verify_requests_kernel settles after the join with a direct dot product of
-// the two centred windows.
+// Each warp drains its queue cooperatively (8 lanes per queued block, both
+// segments of a diagonal per lane as an f32x2 pair): cells that may improve
+// their row or column are published with their FP32 value when the margin is
+// below kTrust; otherwise the lower bound r - margin is published and the
+// cell goes to a request buffer that verify_requests_kernel settles after the
+// join with a direct dot product of the two centred windows.  The k-best
+// form filters at each window's k-th best and inserts into its lists instead.
 //
 // SUM_THRESH (the reference's sum of every r above the threshold,
-// src/kernels_compute.h:87-113 and 380-392), join_mixed_sum_kernel: the same
-// filter and exact path with the sum threshold as the value to beat.  A cell
-// above the threshold by more than its margin, or above it with a margin
-// within kTrust, adds its FP32 r to its row's and its column's slab sums in
-// shared memory (flushed to the FP64 profile by atomicAdd when the row's slab
-// ends or the column leaves the column ring).  A cell within a wider margin
-// of the threshold goes to the request buffer, and verify_requests_kernel
-// adds its directly computed r if that is above the threshold.
+// src/kernels_compute.h:87-113 and 380-392), join_mixed_sum_kernel: every
+// cell is decided in the main loop.  A cell above the threshold by more than
+// the step's margin adds its FP32 r to its row's and its column's slab sums
+// in shared memory (flushed to the FP64 profile by atomicAdd when the row's
+// slab ends or the column leaves the column ring); the rare cells within the
+// margin are settled by their own margin (sum_near): by the FP32 r within
+// kTrust, else by a verification request that verify_requests_kernel adds if
+// its directly computed r is above the threshold.
+//
+// MATRIX_SUMMARY: each thread keeps the running maximum of the grid entry its
+// blocks fall in and publishes it when they move on (mat_cells_block routes
+// the cells of a block that crosses a grid boundary).
 //
 // Anchors and verifications read an FP32 copy of each series stored relative
 // to local block offsets (stats.cu), with every factor centred by its
@@ -729,6 +735,8 @@ __device__ __noinline__ void mat_cells_block(Smem& sm, const float2 (&cov_end)[k
 //          tight where the inverse norms of neighbouring windows are close
 //          (long windows); a block it flags goes to the exact path, which
 //          checks every cell with its own r.
+// kMat selects MATRIX_SUMMARY (running grid maxima), kKnn the k-best lists
+// (filters at each window's k-th best); both take the per-cell filter.
 template <bool kSum, bool kCoarse, bool kMat = false, bool kKnn = false>
 __device__ __forceinline__ void band_body(const JoinParams& P) {
   static_assert(!(kMat && (kSum || kCoarse)), "the matrix form takes per-cell maxima");
