@@ -155,13 +155,17 @@ typedef struct scamp_c_result {
    *   deterministic, for corr_a / corr_b (packed float32 entries add their
    *   own rounding, 2^-24 |r|).  Entries given on input and left unchanged
    *   keep their value.
-   *   SUM_THRESH, mixed form: the largest drift margin of an FP32
-   *   correlation added without a direct dot product (a bound under the
-   *   filter's rounding model, see max_tie_margin).
-   *   -1 where no bound is tracked (FP64 SUM_THRESH, APPROX_ALL_NEIGHBORS,
-   *   MATRIX_SUMMARY).
-   * max_tie_margin: mixed 1NN forms: the largest drift margin of an FP32
-   *   recurrence value that chose a partner without a direct dot product.
+   *   APPROX_ALL_NEIGHBORS, mixed form: the same FP64 recomputation of
+   *   every list entry (each list re-sorted by it).
+   *   SUM_THRESH and MATRIX_SUMMARY, mixed forms: the largest drift margin of
+   *   an FP32 correlation added (or published as a grid maximum) without a
+   *   direct dot product (a bound under the filter's rounding model, see
+   *   max_tie_margin).
+   *   -1 where no bound is tracked (the FP64 forms of SUM_THRESH,
+   *   APPROX_ALL_NEIGHBORS and MATRIX_SUMMARY).
+   * max_tie_margin: mixed 1NN and k-best forms: the largest drift margin of
+   *   an FP32 recurrence value that chose a partner without a direct dot
+   *   product.
    *   The reported partner's FP64 correlation is within twice this of the
    *   window's best as long as the FP32 drift stays within its margin (the
    *   filter's model: an Azuma-Hoeffding bound over independent roundings),
