@@ -715,7 +715,7 @@ int run_device(Workspace& ws, const scamp_c_args* a, scamp_c_result* res,
   // lists (up to knn_mixed_max_k() entries); else the visit kernel
   const bool is_knn = a->profile_type == SCAMP_PROFILE_APPROX_ALL_NEIGHBORS;
   const bool knn_mixed = is_knn && mixed && a->max_matches_per_column >= 1 &&
-                         a->max_matches_per_column <= static_cast<uint64_t>(knn_mixed_max_k());
+                         a->max_matches_per_column <= knn_mixed_max_k();
   const bool visit = (is_knn && !knn_mixed) || (is_mat && !mat_mixed);
   const bool ultra = a->precision_type == SCAMP_PRECISION_ULTRA;
   const int64_t m = plan.m;
